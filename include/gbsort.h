@@ -1,0 +1,139 @@
+/*
+ * gbsort.h -- C ABI of the GB300 histogram sort (libgbsort.so).
+ *
+ * Plain pointers and sizes only.  Every entry point returns a gbsort_status;
+ * none of them aborts the process.  Device entry points take device
+ * pointers and a cudaStream_t passed as `void *` (NULL = the library's own
+ * stream of the current device) and return once the work is enqueued on
+ * that stream, except where stated.  Host entry points copy to the current
+ * CUDA device, sort there, copy back and return when the result is in host
+ * memory.
+ *
+ * Sort semantics are those of MP-sort (mpsort.h:1-12): records of `elsize`
+ * bytes ordered ascending by their radix, stably (the reference's merge
+ * sort keeps ties in input order, stdlib/msort.c:76-167, and so does every
+ * path here).  The drop-in `radix_sort` / `mpsort_omp` symbols are declared
+ * in mpsort.h.
+ */
+#ifndef GBSORT_H
+#define GBSORT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "gbsort_key.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gbsort_status {
+    GBSORT_OK = 0,
+    GBSORT_ERR_BAD_ARG = 1,      /* NULL pointer, bad key descriptor, size out of range */
+    GBSORT_ERR_OOM = 2,          /* device or pinned host memory could not be allocated */
+    GBSORT_ERR_CUDA = 3,         /* a CUDA call failed (message: gbsort_last_error) */
+    GBSORT_ERR_NO_DEVICE = 4,    /* no CUDA device is visible */
+    GBSORT_ERR_INTERNAL = 5,     /* a device-side consistency check failed */
+    GBSORT_ERR_UNSUPPORTED = 6   /* this method cannot take this record layout */
+} gbsort_status;
+
+typedef enum gbsort_method {
+    GBSORT_AUTO = 0,             /* histogram sort with the learned lookup where it applies, else LSD */
+    GBSORT_HISTOGRAM_PLAIN = 1,  /* splitters by bisection + binary-search bucket lookup */
+    GBSORT_HISTOGRAM_LEARNED = 2,/* splitters and bucket lookup from the trained CDF model */
+    GBSORT_LSD = 3               /* stable LSD radix sort of key words + one record permutation */
+} gbsort_method;
+
+/* Statistics of the most recent sort on the calling thread's device. */
+typedef struct gbsort_stats {
+    int32_t method;              /* gbsort_method that ran (never GBSORT_AUTO) */
+    uint32_t nbuckets;           /* level-1 buckets */
+    uint32_t sample;             /* sampled keys */
+    uint32_t splitter_rounds;    /* bisection rounds (plain) or training steps (learned) */
+    uint32_t local_sorts;        /* shared-memory bucket sorts */
+    uint32_t splits;             /* buckets split once more on device */
+    uint32_t copies;             /* single-key buckets copied without sorting */
+    uint32_t resplits;           /* sub-buckets over capacity sent to another split round */
+    uint32_t bigbin_passes;      /* extra local passes on clustered keys */
+    uint32_t window_misses;      /* learned lookups that fell back to the full search */
+    uint32_t max_bucket;         /* largest level-1 bucket (records) */
+    uint32_t lsd_passes;         /* digit passes of the LSD path */
+    uint32_t widest_window;      /* widest learned search window (buckets) */
+    float model_loss;            /* final training loss of the learned model */
+    uint32_t reserved[4];
+} gbsort_stats;
+
+/* Sort nmemb records of elsize bytes from d_in into d_out (device memory;
+ * d_out may equal d_in).  `key` describes the radix; `method` a
+ * gbsort_method.  Requires nmemb < 2^32. */
+GBSORT_API int gbsort_sort_device(const void *d_in, void *d_out, size_t nmemb, size_t elsize,
+                       const gbsort_key_desc *key, int method, void *stream);
+
+/* Same, for host memory: in and out may be equal.  Blocks until done. */
+GBSORT_API int gbsort_sort_host(const void *in, void *out, size_t nmemb, size_t elsize,
+                     const gbsort_key_desc *key, int method);
+
+/* Sort host records in place by a host radix() callback producing rsize
+ * bytes per record (compared as a little-endian unsigned integer, which is
+ * what radixsort.c:47-194 does on a little-endian host).  The callback runs
+ * on the host, once per record; the sort runs on the GPU.  Blocks. */
+GBSORT_API int gbsort_sort_radix_host(void *base, size_t nmemb, size_t elsize,
+                           void (*radix)(const void *ptr, void *radix, void *arg),
+                           size_t rsize, void *arg);
+
+/* Batched sort of nseg independent segments in one pipeline: segment i is
+ * records [seg_offsets[i], seg_offsets[i+1]) of d_in (device memory; the
+ * offsets array is in host memory, nseg + 1 entries).  Each segment comes
+ * out sorted in place of its range in d_out. */
+GBSORT_API int gbsort_sort_segments_device(const void *d_in, void *d_out, const uint64_t *seg_offsets,
+                                size_t nseg, size_t elsize, const gbsort_key_desc *key,
+                                int method, void *stream);
+
+/* Join of two segments sorted by the same key (device memory): for every
+ * key present in both, the pair of record indices (ia into a, ib into b).
+ * Keys must be unique within each side.  *d_npairs (device memory) receives
+ * the pair count; d_pairs_a / d_pairs_b need min(na, nb) entries. */
+GBSORT_API int gbsort_merge_join_device(const void *d_a, size_t na, const void *d_b, size_t nb,
+                             size_t elsize, const gbsort_key_desc *key, uint64_t *d_pairs_a,
+                             uint64_t *d_pairs_b, uint64_t *d_npairs, void *stream);
+
+/* Learned-model pieces, exposed for checking: one forward and backward pass
+ * of the piecewise-linear CDF over sorted keys x (host arrays of s keys,
+ * knots y of (1 << lbits) + 1 floats).  Outputs the mean squared loss, the
+ * predictions (s floats) and the gradient (same size as y). */
+GBSORT_API int gbsort_cdf_forward_backward(const uint64_t *x, uint32_t s, uint64_t kmin, uint64_t kmax,
+                                int lbits, const float *y, float *loss, float *pred,
+                                float *grad);
+
+/* Learned-lookup probe (host arrays): trains the CDF model on the sample,
+ * derives its splitters (nbuckets - 1 of them, returned in `splitters`) and
+ * looks every key up twice -- with the model plus its search window, and
+ * with a full binary search over the same splitters.  The two bucket arrays
+ * must be identical; widest_window receives the widest window in buckets.
+ * Used by tests. */
+GBSORT_API int gbsort_debug_buckets(const uint64_t *sample, uint32_t s, int nbuckets, const uint64_t *keys,
+                         uint32_t nkeys, uint32_t *bucket_search, uint32_t *bucket_learned,
+                         uint64_t *splitters, uint32_t *widest_window);
+
+/* Plain splitter search alone (host arrays): the reference's bisection
+ * (internal-parallel.h:128-248) for nsplit splitters over a sorted run of
+ * s keys with targets C[i+1] = s*(i+1)/(nsplit+1).  Outputs the splitters
+ * before single-key bucket shaping, the per-splitter CLT/CLE counts and the
+ * number of rounds. */
+GBSORT_API int gbsort_debug_bisect(const uint64_t *sorted, uint32_t s, int nsplit, uint64_t *splitters,
+                        int64_t *clt, int64_t *cle, uint32_t *rounds);
+
+GBSORT_API int gbsort_last_stats(gbsort_stats *out);
+GBSORT_API const char *gbsort_status_string(int status);
+GBSORT_API const char *gbsort_last_error(void);
+GBSORT_API int gbsort_device_count(void);
+/* Frees the cached device workspace and pinned staging of the current device. */
+GBSORT_API int gbsort_release(void);
+/* Version string of this library. */
+GBSORT_API const char *gbsort_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBSORT_H */

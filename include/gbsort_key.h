@@ -28,6 +28,13 @@ extern "C" {
 
 #define GBSORT_MAX_KEY_WORDS 4
 
+/* Symbols of the public ABI (the library is built with hidden visibility). */
+#if defined(__GNUC__)
+#define GBSORT_API __attribute__((visibility("default")))
+#else
+#define GBSORT_API
+#endif
+
 typedef struct gbsort_key_word {
     uint32_t offset;     /* byte offset of the field inside the record */
     uint32_t width;      /* 4 or 8 bytes */

@@ -1,0 +1,380 @@
+// cdf.cu -- training and use of the learned CDF model (see cdf.cuh).
+//
+// Data: the sorted sample x_0 <= ... <= x_{s-1} with targets r_i = i / s,
+// i.e. (key, exact rank) pairs of the sample that the plain bisection also
+// works on.  Model: knots y_0 .. y_L (fp32) of a piecewise-linear F over L
+// uniform leaves of (key - kmin) >> lshift.  Loss: mean (F(x_i) - r_i)^2.
+//
+//   k_cdf_forward   -- F(x_i) and the loss
+//   k_cdf_backward  -- dLoss/dy_j (each sample feeds its two knots)
+//   k_cdf_curvature -- diagonal of the Gauss-Newton matrix (preconditioner)
+//   k_cdf_step      -- damped Jacobi-preconditioned gradient step
+//   k_cdf_project   -- non-decreasing knots in [0, 1] (cumulative max)
+//   k_cdf_splitters -- S_j = least key with predicted bucket >= j + 1
+//   k_cdf_heavy     -- keys covering a whole bucket of the sample get their
+//                      own single-key bucket [k, k + 1)
+//   k_cdf_windows   -- exact per-leaf [g - dlo, g + dhi] bracket of the true
+//                      bucket, evaluated at the points where either the
+//                      prediction or the true bucket can reach its extreme
+#include "cdf.cuh"
+#include "cdf_api.h"
+#include "common.cuh"
+
+namespace gb {
+
+namespace {
+
+__device__ __forceinline__ void features(uint64_t key, uint64_t kmin, int lshift, int lbits, uint32_t& leaf,
+                                         float& frac) {
+  const uint32_t nleaf = 1u << lbits;
+  if (key < kmin) {
+    leaf = 0;
+    frac = 0.f;
+    return;
+  }
+  uint64_t x = key - kmin;
+  uint64_t l = lshift >= 64 ? 0 : (x >> lshift);
+  if (l >= nleaf) {
+    leaf = nleaf - 1;
+    frac = 1.f;
+    return;
+  }
+  leaf = (uint32_t)l;
+  frac = leaf_frac(x, lshift);
+}
+
+__global__ void k_cdf_forward(const uint64_t* __restrict__ x, uint32_t s, CdfShape sh,
+                              const float* __restrict__ y, float* __restrict__ pred, float* __restrict__ loss) {
+  __shared__ float red[32];
+  float acc = 0.f;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s; i += gridDim.x * blockDim.x) {
+    uint32_t leaf;
+    float frac;
+    features(x[i], sh.kmin, sh.lshift, sh.lbits, leaf, frac);
+    float f = fmaf(frac, y[leaf + 1] - y[leaf], y[leaf]);
+    float r = (float)i / (float)s;
+    if (pred) pred[i] = f;
+    float e = f - r;
+    acc += e * e;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(GB_FULL_MASK, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float v = threadIdx.x < blockDim.x / 32 ? red[threadIdx.x] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(GB_FULL_MASK, v, o);
+    if (threadIdx.x == 0) atomicAdd(loss, v / (float)s);
+  }
+}
+
+// grad[j] += sum_i 2 (F(x_i) - r_i) * dF/dy_j / s, with dF/dy_leaf = 1 - frac,
+// dF/dy_{leaf+1} = frac.  Neighbouring samples share leaves (the sample is
+// sorted), so lanes with the same leaf combine before the atomic.
+__global__ void k_cdf_backward(const uint64_t* __restrict__ x, uint32_t s, CdfShape sh,
+                               const float* __restrict__ y, float* __restrict__ grad) {
+  for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < s; i0 += gridDim.x * blockDim.x) {
+    uint32_t i = i0 + threadIdx.x;
+    bool v = i < s;
+    uint32_t leaf = 0xffffffffu;
+    float g0 = 0.f, g1 = 0.f;
+    if (v) {
+      float frac;
+      features(x[i], sh.kmin, sh.lshift, sh.lbits, leaf, frac);
+      float f = fmaf(frac, y[leaf + 1] - y[leaf], y[leaf]);
+      float e = 2.f * (f - (float)i / (float)s) / (float)s;
+      g0 = e * (1.f - frac);
+      g1 = e * frac;
+    }
+    uint32_t peers = __match_any_sync(GB_FULL_MASK, leaf);
+    // reduce within the peer group (leader = lowest lane)
+    float a0 = 0.f, a1 = 0.f;
+    for (uint32_t m = peers; m; m &= m - 1) {
+      int l = __ffs(m) - 1;
+      a0 += __shfl_sync(peers, g0, l);
+      a1 += __shfl_sync(peers, g1, l);
+    }
+    if (v && (peers & lanemask_lt()) == 0) {
+      atomicAdd(&grad[leaf], a0);
+      atomicAdd(&grad[leaf + 1], a1);
+    }
+  }
+}
+
+__global__ void k_cdf_curvature(const uint64_t* __restrict__ x, uint32_t s, CdfShape sh, float* __restrict__ h) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s; i += gridDim.x * blockDim.x) {
+    uint32_t leaf;
+    float frac;
+    features(x[i], sh.kmin, sh.lshift, sh.lbits, leaf, frac);
+    atomicAdd(&h[leaf], 2.f * (1.f - frac) * (1.f - frac) / (float)s);
+    atomicAdd(&h[leaf + 1], 2.f * frac * frac / (float)s);
+  }
+}
+
+__global__ void k_cdf_step(float* __restrict__ y, const float* __restrict__ grad, const float* __restrict__ h,
+                           int nknots, float lr) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j <= 0 || j >= nknots - 1) return;  // F(kmin) = 0 and F(end) = 1 stay fixed
+  y[j] -= lr * grad[j] / (h[j] + 1e-12f);
+}
+
+// Initial knots: the empirical CDF of the sample at every knot.
+__global__ void k_cdf_init(const uint64_t* __restrict__ x, uint32_t s, CdfShape sh, float* __restrict__ y) {
+  const int nk = (1 << sh.lbits) + 1;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nk; j += gridDim.x * blockDim.x) {
+    // knot j sits at key kmin + (j << lshift): count samples below it
+    uint64_t kj;
+    bool beyond = false;
+    if (sh.lshift >= 64) beyond = j > 0;
+    else {
+      uint64_t off = (uint64_t)j << sh.lshift;
+      if (sh.lshift > 0 && (off >> sh.lshift) != (uint64_t)j) beyond = true;
+      kj = sh.kmin + off;
+      if (kj < sh.kmin) beyond = true;  // wrapped past 2^64
+    }
+    uint32_t c;
+    if (beyond) c = s;
+    else {
+      uint32_t lo = 0, hi = s;
+      while (lo < hi) {
+        uint32_t m = (lo + hi) >> 1;
+        if (x[m] < kj) lo = m + 1; else hi = m;
+      }
+      c = lo;
+    }
+    y[j] = (float)c / (float)s;
+  }
+}
+
+// Cumulative max, clamp to [0, 1], y_0 = 0, y_L = 1; knots[j] = (y_j, y_{j+1}).
+__global__ void __launch_bounds__(1024) k_cdf_project(float* __restrict__ y, int nknots, float2* __restrict__ knots) {
+  __shared__ float tmp[1024];
+  const int per = (nknots + 1023) / 1024;
+  const int b = threadIdx.x * per;
+  float m = 0.f;
+  for (int i = 0; i < per; ++i) {
+    int j = b + i;
+    if (j < nknots) {
+      float v = fminf(fmaxf(y[j], 0.f), 1.f);
+      if (j == 0) v = 0.f;
+      if (j == nknots - 1) v = 1.f;
+      y[j] = v;
+      m = fmaxf(m, v);
+    }
+  }
+  tmp[threadIdx.x] = m;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    float v = threadIdx.x >= (unsigned)o ? tmp[threadIdx.x - o] : 0.f;
+    __syncthreads();
+    tmp[threadIdx.x] = fmaxf(tmp[threadIdx.x], v);
+    __syncthreads();
+  }
+  float run = threadIdx.x ? tmp[threadIdx.x - 1] : 0.f;
+  for (int i = 0; i < per; ++i) {
+    int j = b + i;
+    if (j < nknots) {
+      run = fmaxf(run, y[j]);
+      y[j] = run;
+    }
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j + 1 < nknots; j += 1024) knots[j] = make_float2(y[j], y[j + 1]);
+}
+
+__device__ __forceinline__ uint32_t predict(uint64_t key, const CdfShape& sh, int nbuckets, const float2* knots) {
+  uint32_t leaf, g;
+  model_predict(key, sh.kmin, sh.lshift, sh.lbits, nbuckets, knots, leaf, g);
+  return g;
+}
+
+// S_j = least key with predicted bucket >= j + 1 (all keys above if none).
+__global__ void k_cdf_splitters(CdfShape sh, int nbuckets, const float2* __restrict__ knots,
+                                uint64_t* __restrict__ S) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nbuckets - 1) return;
+  uint64_t lo = 0, hi = ~0ull;
+  if (predict(hi, sh, nbuckets, knots) < (uint32_t)(j + 1)) {
+    S[j] = ~0ull;
+    return;
+  }
+  while (lo < hi) {  // smallest key with predict >= j + 1
+    uint64_t mid = lo + ((hi - lo) >> 1);
+    if (predict(mid, sh, nbuckets, knots) >= (uint32_t)(j + 1)) hi = mid;
+    else lo = mid + 1;
+  }
+  S[j] = lo;
+}
+
+// Keys whose run in the sorted sample is at least one bucket long get the
+// single-key bucket [k, k + 1): S at lower_bound(S, k) becomes k, the next
+// splitter k + 1 (a later cumulative max restores the order).
+__global__ void k_cdf_heavy(const uint64_t* __restrict__ x, uint32_t s, int nbuckets, uint64_t* __restrict__ S) {
+  const uint32_t need = (s + nbuckets - 1) / nbuckets;
+  const int nsplit = nbuckets - 1;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s; i += gridDim.x * blockDim.x) {
+    if (i > 0 && x[i - 1] == x[i]) continue;  // only run starts
+    if (i + need > s || x[i + need - 1] != x[i]) continue;
+    uint64_t k = x[i];
+    uint32_t lo = 0, hi = nsplit;
+    while (lo < hi) {
+      uint32_t m = (lo + hi) >> 1;
+      if (S[m] < k) lo = m + 1; else hi = m;
+    }
+    if (lo < (uint32_t)nsplit) S[lo] = k;
+    if (lo + 1 < (uint32_t)nsplit && k != ~0ull) S[lo + 1] = k + 1;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_cummax_u64(uint64_t* S, int n) {
+  // single block: per-thread segments, then a max-scan of the segment maxima
+  __shared__ uint64_t tmp[1024];
+  const int per = (n + 1023) / 1024;
+  const int b = threadIdx.x * per;
+  uint64_t m = 0;
+  for (int i = 0; i < per; ++i)
+    if (b + i < n) m = S[b + i] > m ? S[b + i] : m;
+  tmp[threadIdx.x] = m;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    uint64_t v = threadIdx.x >= o ? tmp[threadIdx.x - o] : 0;
+    __syncthreads();
+    if (v > tmp[threadIdx.x]) tmp[threadIdx.x] = v;
+    __syncthreads();
+  }
+  uint64_t run = threadIdx.x ? tmp[threadIdx.x - 1] : 0;
+  for (int i = 0; i < per; ++i)
+    if (b + i < n) {
+      run = S[b + i] > run ? S[b + i] : run;
+      S[b + i] = run;
+    }
+}
+
+__device__ __forceinline__ uint32_t true_bucket(const uint64_t* S, int nsplit, uint64_t key) {
+  return upper_bound_in(S, 0, (uint32_t)nsplit, key);
+}
+
+__device__ __forceinline__ void window_update(uint32_t* win_lo, uint32_t* win_hi, uint64_t key, const CdfShape& sh,
+                                              int nbuckets, const float2* knots, const uint64_t* S) {
+  uint32_t leaf, g;
+  model_predict(key, sh.kmin, sh.lshift, sh.lbits, nbuckets, knots, leaf, g);
+  uint32_t t = true_bucket(S, nbuckets - 1, key);
+  if (g > t) atomicMax(&win_lo[leaf], g - t);
+  if (t > g) atomicMax(&win_hi[leaf], t - g);
+}
+
+// Extremes of g - t sit at the last key before each true step (S_j - 1) and
+// at a leaf's last key; extremes of t - g at each S_j and at a leaf's first
+// key.  Both lists are evaluated; first/last keys of a leaf are clamped to
+// the key range.
+__global__ void k_cdf_windows(CdfShape sh, int nbuckets, const float2* __restrict__ knots,
+                              const uint64_t* __restrict__ S, uint32_t* __restrict__ win_lo,
+                              uint32_t* __restrict__ win_hi) {
+  const int nleaf = 1 << sh.lbits;
+  const int nsplit = nbuckets - 1;
+  const int total = nsplit + nleaf;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    if (i < nsplit) {
+      uint64_t k = S[i];
+      window_update(win_lo, win_hi, k, sh, nbuckets, knots, S);
+      if (k > 0) window_update(win_lo, win_hi, k - 1, sh, nbuckets, knots, S);
+    } else {
+      int l = i - nsplit;
+      uint64_t first, last;
+      if (l == 0) first = 0;
+      else first = sh.kmin + ((uint64_t)l << sh.lshift);
+      if (l == nleaf - 1) last = ~0ull;
+      else {
+        uint64_t nx = sh.kmin + ((uint64_t)(l + 1) << sh.lshift);
+        last = nx - 1;
+      }
+      if (sh.lshift >= 64) {  // a single leaf spans everything
+        first = 0;
+        last = ~0ull;
+      }
+      window_update(win_lo, win_hi, first, sh, nbuckets, knots, S);
+      window_update(win_lo, win_hi, last, sh, nbuckets, knots, S);
+      if (l == 0 && sh.kmin > 0) window_update(win_lo, win_hi, sh.kmin - 1, sh, nbuckets, knots, S);
+    }
+  }
+}
+
+__global__ void k_pack_windows(const uint32_t* __restrict__ lo, const uint32_t* __restrict__ hi, int nleaf,
+                               uint32_t* __restrict__ win, uint32_t* wide) {
+  int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nleaf) return;
+  uint32_t a = min(lo[l], 0xffffu), b = min(hi[l], 0xffffu);
+  win[l] = (a << 16) | b;
+  atomicMax(wide, max(lo[l], hi[l]));
+}
+
+unsigned grid_for(uint32_t n, int threads) {
+  uint32_t b = (n + threads - 1) / threads;
+  return b < 1 ? 1 : (b > 1184 ? 1184 : b);
+}
+
+}  // namespace
+
+CdfShape cdf_shape(uint64_t kmin, uint64_t kmax, int lbits) {
+  CdfShape sh{};
+  sh.kmin = kmin;
+  sh.lbits = lbits;
+  int bits = kmax > kmin ? 64 - __builtin_clzll(kmax - kmin) : 0;
+  sh.lshift = bits > lbits ? bits - lbits : 0;
+  return sh;
+}
+
+cudaError_t cdf_forward(const uint64_t* x, uint32_t s, const CdfShape& sh, const float* y, float* pred, float* loss,
+                        cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(loss, 0, sizeof(float), st);
+  if (e != cudaSuccess) return e;
+  k_cdf_forward<<<grid_for(s, 256), 256, 0, st>>>(x, s, sh, y, pred, loss);
+  return cudaGetLastError();
+}
+
+cudaError_t cdf_backward(const uint64_t* x, uint32_t s, const CdfShape& sh, const float* y, float* grad,
+                         cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(grad, 0, sizeof(float) * ((1u << sh.lbits) + 1), st);
+  if (e != cudaSuccess) return e;
+  k_cdf_backward<<<grid_for(s, 256), 256, 0, st>>>(x, s, sh, y, grad);
+  return cudaGetLastError();
+}
+
+cudaError_t cdf_train(const uint64_t* x, uint32_t s, const CdfShape& sh, int epochs, float lr, CdfWork& w,
+                      cudaStream_t st) {
+  const int nk = (1 << sh.lbits) + 1;
+  cudaError_t e;
+  k_cdf_init<<<grid_for(nk, 256), 256, 0, st>>>(x, s, sh, w.y);
+  if ((e = cudaMemsetAsync(w.h, 0, sizeof(float) * nk, st)) != cudaSuccess) return e;
+  k_cdf_curvature<<<grid_for(s, 256), 256, 0, st>>>(x, s, sh, w.h);
+  for (int it = 0; it < epochs; ++it) {
+    if ((e = cdf_backward(x, s, sh, w.y, w.grad, st)) != cudaSuccess) return e;
+    k_cdf_step<<<grid_for(nk, 256), 256, 0, st>>>(w.y, w.grad, w.h, nk, lr);
+  }
+  if (w.loss && (e = cdf_forward(x, s, sh, w.y, nullptr, w.loss, st)) != cudaSuccess) return e;
+  k_cdf_project<<<1, 1024, 0, st>>>(w.y, nk, w.knots);
+  return cudaGetLastError();
+}
+
+cudaError_t cdf_splitters(const uint64_t* x, uint32_t s, const CdfShape& sh, int nbuckets, const float2* knots,
+                          uint64_t* S, cudaStream_t st) {
+  const int nsplit = nbuckets - 1;
+  if (nsplit <= 0) return cudaSuccess;
+  k_cdf_splitters<<<grid_for(nsplit, 128), 128, 0, st>>>(sh, nbuckets, knots, S);
+  k_cdf_heavy<<<grid_for(s, 256), 256, 0, st>>>(x, s, nbuckets, S);
+  k_cummax_u64<<<1, 1024, 0, st>>>(S, nsplit);
+  return cudaGetLastError();
+}
+
+cudaError_t cdf_windows(const CdfShape& sh, int nbuckets, const float2* knots, const uint64_t* S, uint32_t* win,
+                        uint32_t* tmp_lo, uint32_t* tmp_hi, uint32_t* widest, cudaStream_t st) {
+  const int nleaf = 1 << sh.lbits;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(tmp_lo, 0, sizeof(uint32_t) * nleaf, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(tmp_hi, 0, sizeof(uint32_t) * nleaf, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(widest, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+  k_cdf_windows<<<grid_for(nbuckets + nleaf, 128), 128, 0, st>>>(sh, nbuckets, knots, S, tmp_lo, tmp_hi);
+  k_pack_windows<<<grid_for(nleaf, 256), 256, 0, st>>>(tmp_lo, tmp_hi, nleaf, win, widest);
+  return cudaGetLastError();
+}
+
+}  // namespace gb

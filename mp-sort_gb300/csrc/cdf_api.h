@@ -1,0 +1,36 @@
+// cdf_api.h -- host entry points of the learned CDF model (cdf.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gb {
+
+struct CdfShape {
+  uint64_t kmin;  // key of leaf 0's left edge
+  int lshift;     // leaf = (key - kmin) >> lshift
+  int lbits;      // 1 << lbits leaves, (1 << lbits) + 1 knots
+};
+
+struct CdfWork {   // device buffers of one training run
+  float* y;        // knots, (1 << lbits) + 1
+  float* grad;     // same size
+  float* h;        // same size
+  float2* knots;   // 1 << lbits pairs (y_j, y_{j+1}) after projection
+  float* loss;     // 1 float (may be null)
+};
+
+CdfShape cdf_shape(uint64_t kmin, uint64_t kmax, int lbits);
+cudaError_t cdf_forward(const uint64_t* x, uint32_t s, const CdfShape& sh, const float* y, float* pred,
+                        float* loss, cudaStream_t st);
+cudaError_t cdf_backward(const uint64_t* x, uint32_t s, const CdfShape& sh, const float* y, float* grad,
+                         cudaStream_t st);
+cudaError_t cdf_train(const uint64_t* x, uint32_t s, const CdfShape& sh, int epochs, float lr, CdfWork& w,
+                      cudaStream_t st);
+cudaError_t cdf_splitters(const uint64_t* x, uint32_t s, const CdfShape& sh, int nbuckets,
+                          const float2* knots, uint64_t* S, cudaStream_t st);
+cudaError_t cdf_windows(const CdfShape& sh, int nbuckets, const float2* knots, const uint64_t* S,
+                        uint32_t* win, uint32_t* tmp_lo, uint32_t* tmp_hi, uint32_t* widest,
+                        cudaStream_t st);
+
+}  // namespace gb

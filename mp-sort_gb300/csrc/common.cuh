@@ -1,0 +1,179 @@
+// common.cuh -- device helpers shared by every gbsort kernel (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gbsort_key.h"
+
+#define GB_FULL_MASK 0xffffffffu
+
+namespace gb {
+
+// Launch shape of the record-streaming kernels: one CTA of 512 threads per
+// SM slot, 16 warps.
+constexpr int kThreads = 512;
+constexpr int kWarps = kThreads / 32;
+
+// Device error word: kernels never trap; they record the first error here and
+// return.  The host reads it after the pipeline and maps it to a status code.
+enum DevError : uint32_t {
+  DEV_OK = 0,
+  DEV_ERR_TASK_OVERFLOW = 1,   // a task list ran out of room
+  DEV_ERR_LEVELS = 2,          // more split rounds than the key width allows
+  DEV_ERR_COUNT_MISMATCH = 3,  // a scatter wrote a different count than counted
+  DEV_ERR_WINDOW = 4,          // learned search window missed (never expected)
+  DEV_ERR_TIMEOUT = 5,         // a bounded spin-wait gave up
+};
+
+__device__ __forceinline__ void set_error(uint32_t* err, uint32_t code) {
+  if (err) atomicCAS(err, 0u, code);
+}
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
+__device__ __forceinline__ uint32_t warp_id() { return threadIdx.x >> 5; }
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Order-preserving 64-bit word of a key field held as raw bits (binding.pyx
+// radix_func_*: u8 as is, u4 zero-extended, i8/i4 sign-extended plus 2^63).
+__device__ __forceinline__ uint64_t map_key(uint64_t raw, uint32_t width, uint32_t is_signed) {
+  if (width == 8) return is_signed ? (raw ^ 0x8000000000000000ull) : raw;
+  uint32_t v = (uint32_t)raw;
+  if (is_signed) return (uint64_t)(int64_t)(int32_t)v ^ 0x8000000000000000ull;
+  return (uint64_t)v;
+}
+
+// Load one key word from a record whose address is 4-byte aligned.
+__device__ __forceinline__ uint64_t load_key_aligned4(const uint8_t* rec, const gbsort_key_word& w) {
+  const uint32_t* p = reinterpret_cast<const uint32_t*>(rec + w.offset);
+  uint64_t raw = p[0];
+  if (w.width == 8) raw |= (uint64_t)p[1] << 32;
+  return map_key(raw, w.width, w.is_signed);
+}
+
+// Load one key word from a record at any byte alignment.
+__device__ __forceinline__ uint64_t load_key_bytes(const uint8_t* rec, const gbsort_key_word& w) {
+  uint64_t raw = 0;
+  for (uint32_t b = 0; b < w.width; ++b) raw |= (uint64_t)rec[w.offset + b] << (8 * b);
+  return map_key(raw, w.width, w.is_signed);
+}
+
+// Select word `idx` of a register array without dynamic indexing.
+template <int N>
+__device__ __forceinline__ uint32_t reg_select(const uint32_t (&a)[N], uint32_t idx) {
+  uint32_t v = 0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) v = (i == (int)idx) ? a[i] : v;
+  return v;
+}
+
+// Key of a record held in registers as E_WORDS 32-bit words.
+template <int E_WORDS>
+__device__ __forceinline__ uint64_t key_from_regs(const uint32_t (&r)[E_WORDS], const gbsort_key_word& w) {
+  uint32_t k = w.offset >> 2;
+  uint64_t raw = reg_select<E_WORDS>(r, k);
+  if (w.width == 8) raw |= (uint64_t)reg_select<E_WORDS>(r, k + 1) << 32;
+  return map_key(raw, w.width, w.is_signed);
+}
+
+__device__ __forceinline__ int bitlen64(uint64_t x) { return x ? 64 - __clzll(x) : 0; }
+
+// Block-wide exclusive scan of one value per thread (kThreads threads).
+// `tmp` holds kWarps entries.  Returns the exclusive prefix; *total gets the sum.
+template <typename T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T* tmp, T* total) {
+  const uint32_t lane = lane_id(), w = warp_id();
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T y = __shfl_up_sync(GB_FULL_MASK, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) tmp[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    T s = lane < (uint32_t)kWarps ? tmp[lane] : T(0);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      T y = __shfl_up_sync(GB_FULL_MASK, s, o);
+      if (lane >= (uint32_t)o) s += y;
+    }
+    if (lane < (uint32_t)kWarps) tmp[lane] = s;
+  }
+  __syncthreads();
+  T warp_prefix = w ? tmp[w - 1] : T(0);
+  T result = warp_prefix + x - v;
+  if (total) *total = tmp[kWarps - 1];
+  __syncthreads();
+  return result;
+}
+
+// ---------------------------------------------------------------------------
+// Stable block ranking by a small digit (the warp match/ballot ranking).
+//
+// Items are in "warp-chunk" order: item r of lane l in warp w is tile element
+//   w * 32 * RPT + r * 32 + l,
+// so each warp owns a contiguous run of the tile.  Ranks are positions in the
+// tile stably sorted by digit.  `hist` is kWarps << DIGIT_BITS uint16
+// counters (digit-major).  Items with valid == false must carry the largest
+// digit; they then land after every valid item.
+// ---------------------------------------------------------------------------
+template <int RPT, int DIGIT_BITS>
+struct BlockRank {
+  static constexpr int kDigits = 1 << DIGIT_BITS;
+  static constexpr int kCounters = kDigits * kWarps;
+  static_assert(kCounters % kThreads == 0, "counter count must divide the block");
+  static constexpr int kPerThread = kCounters / kThreads;
+
+  // ranks[r] receives the position of item r; digit_start (optional, kDigits
+  // + 1 entries in shared memory) receives the start of every digit's run.
+  __device__ __forceinline__ static void rank(const uint32_t (&digit)[RPT], uint32_t (&ranks)[RPT],
+                                              uint16_t* hist, uint32_t* scan_tmp,
+                                              uint32_t* digit_start) {
+    const uint32_t lane = lane_id(), w = warp_id();
+    for (int i = threadIdx.x; i < kCounters; i += kThreads) hist[i] = 0;
+    __syncthreads();
+    const uint32_t lt = lanemask_lt();
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+      const uint32_t d = digit[r];
+      const uint32_t peers = __match_any_sync(GB_FULL_MASK, d);
+      const uint32_t before = hist[d * kWarps + w];
+      ranks[r] = before + __popc(peers & lt);
+      __syncwarp();
+      if ((peers & lt) == 0) hist[d * kWarps + w] = (uint16_t)(before + __popc(peers));
+      __syncwarp();
+    }
+    __syncthreads();
+    // exclusive scan over the digit-major counters
+    uint32_t local[kPerThread];
+    uint32_t sum = 0;
+    const int base = threadIdx.x * kPerThread;
+#pragma unroll
+    for (int i = 0; i < kPerThread; ++i) {
+      local[i] = hist[base + i];
+      sum += local[i];
+    }
+    uint32_t total;
+    uint32_t pre = block_exclusive_scan<uint32_t>(sum, scan_tmp, &total);
+#pragma unroll
+    for (int i = 0; i < kPerThread; ++i) {
+      hist[base + i] = (uint16_t)pre;
+      pre += local[i];
+    }
+    __syncthreads();
+    if (digit_start) {
+      for (int d = threadIdx.x; d < kDigits; d += kThreads) digit_start[d] = hist[d * kWarps];
+      if (threadIdx.x == 0) digit_start[kDigits] = total;
+    }
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) ranks[r] += hist[digit[r] * kWarps + w];
+    __syncthreads();
+  }
+};
+
+}  // namespace gb

@@ -1,0 +1,835 @@
+// gbsort.cu -- host side of libgbsort: device workspace, the sort pipelines
+// and every entry point of include/gbsort.h and include/mpsort.h.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "../../include/gbsort.h"
+#include "../../include/mpsort.h"
+#include "cdf.cuh"
+#include "cdf_api.h"
+#include "kernels.h"
+
+namespace gb {
+cudaError_t join_count(const uint8_t* a, uint32_t na, const uint8_t* b, uint32_t nb, uint32_t elsize,
+                       gbsort_key_word key, uint32_t* counts, int grid, cudaStream_t st);
+cudaError_t join_write(const uint8_t* a, uint32_t na, const uint8_t* b, uint32_t nb, uint32_t elsize,
+                       gbsort_key_word key, const uint32_t* offsets, int grid, uint64_t* pa, uint64_t* pb,
+                       uint64_t* npairs, cudaStream_t st);
+int join_grid(uint32_t na);
+cudaError_t segment_ranges(const uint8_t* rec, uint32_t elsize, gbsort_key_word key, const uint64_t* offsets,
+                           uint32_t nseg, SortTask* tasks, uint32_t* ntasks, uint32_t cap, uint32_t* err,
+                           cudaStream_t st);
+cudaError_t probe_buckets(const uint64_t* keys, uint32_t nkeys, const uint64_t* S, const void* model,
+                          uint32_t* learned, uint32_t* search, uint32_t* misses, cudaStream_t st);
+}  // namespace gb
+
+namespace {
+
+using namespace gb;
+
+thread_local char g_err[512] = "";
+thread_local int g_mpsort_status = GBSORT_OK;
+thread_local gbsort_stats g_stats = {};
+int g_mpi_options = 0;
+std::mutex g_opt_mu;
+
+void set_err(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+#define GB_CUDA(call)                                                                  \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      set_err("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_));      \
+      return e_ == cudaErrorMemoryAllocation ? GBSORT_ERR_OOM : GBSORT_ERR_CUDA;       \
+    }                                                                                  \
+  } while (0)
+
+// A grow-only device allocation.
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = bytes + bytes / 16;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      e = cudaMalloc(&p, bytes);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        p = nullptr;
+        return e;
+      }
+      want = bytes;
+    }
+    cap = want;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <typename T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+// Bump allocator over one device buffer for the small arrays of a run.
+struct Bump {
+  uint8_t* base;
+  size_t off = 0;
+  template <typename T>
+  T* take(size_t count) {
+    off = (off + 255) & ~(size_t)255;
+    T* r = reinterpret_cast<T*>(base + off);
+    off += sizeof(T) * count;
+    return r;
+  }
+};
+
+struct HostCounters {  // pinned, read back at the end of a run
+  uint32_t stats[STAT_SLOTS];
+  uint32_t err;
+  uint32_t iters;
+  uint32_t widest;
+  float loss;
+  uint32_t ntasks[2];
+  uint64_t kminmax[2];
+};
+
+struct Context {
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  DevBuf A, B;             // record scratch
+  DevBuf hin, hout;        // staging of the host entry points
+  DevBuf keysA, keysB;     // generic path key words
+  DevBuf idxA, idxB;       // generic path permutation
+  DevBuf small;            // splitters, counts, tasks, model, counters
+  DevBuf radix;            // host radix bytes (callback path)
+  HostCounters* hc = nullptr;
+  std::mutex mu;
+};
+
+std::mutex g_ctx_mu;
+Context* g_ctx[64] = {};
+
+int get_ctx(Context** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_err("no CUDA device: %s", cudaGetErrorString(e));
+    return GBSORT_ERR_NO_DEVICE;
+  }
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    set_err("no CUDA device visible");
+    return GBSORT_ERR_NO_DEVICE;
+  }
+  if (dev < 0 || dev >= 64) return GBSORT_ERR_BAD_ARG;
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  if (!g_ctx[dev]) {
+    Context* c = new Context();
+    c->device = dev;
+    GB_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    GB_CUDA(cudaMallocHost(&c->hc, sizeof(HostCounters)));
+    g_ctx[dev] = c;
+  }
+  *out = g_ctx[dev];
+  return GBSORT_OK;
+}
+
+bool key_ok(const gbsort_key_desc* key, size_t elsize) {
+  if (!key || key->nwords < 1 || key->nwords > GBSORT_MAX_KEY_WORDS) return false;
+  for (uint32_t w = 0; w < key->nwords; ++w) {
+    const gbsort_key_word& k = key->word[w];
+    if (k.width != 4 && k.width != 8) return false;
+    if (k.is_signed > 1) return false;
+    if ((size_t)k.offset + k.width > elsize) return false;
+  }
+  return true;
+}
+
+uint32_t pow2_ceil(uint64_t x) {
+  uint32_t p = 1;
+  while (p < x && p < (1u << 30)) p <<= 1;
+  return p;
+}
+
+// ------------------------------------------------------------ LSD path --
+// Sorts key words (and idx) in place in keys / idx, ping-ponging through
+// keys2 / idx2.  Digits whose histogram puts every key in one bin are
+// skipped.  Returns the number of passes run (the result is in the first
+// buffer either way).
+int lsd_sort_keys(Context& c, Bump& bump, uint64_t* keys, uint64_t* keys2, uint32_t* idx, uint32_t* idx2,
+                  uint32_t n, int nwords, bool skip_trivial, int* passes_out, cudaStream_t st) {
+  const int g = lsd_grid(n);
+  uint32_t* counts = bump.take<uint32_t>((size_t)256 * g);
+  uint32_t* scan_tmp = bump.take<uint32_t>(scan_tmp_words((size_t)256 * g));
+  std::vector<int> pass_word, pass_shift;
+  if (skip_trivial) {
+    uint32_t* hist = bump.take<uint32_t>((size_t)8 * 256 * nwords);
+    GB_CUDA(lsd_digit_histograms(keys, n, nwords, hist, st));
+    std::vector<uint32_t> h((size_t)8 * 256 * nwords);
+    GB_CUDA(cudaMemcpyAsync(h.data(), hist, h.size() * 4, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    for (int w = 0; w < nwords; ++w)
+      for (int d = 0; d < 8; ++d) {
+        bool trivial = false;
+        for (int b = 0; b < 256; ++b)
+          if (h[((size_t)w * 8 + d) * 256 + b] == n) trivial = true;
+        if (!trivial) {
+          pass_word.push_back(w);
+          pass_shift.push_back(8 * d);
+        }
+      }
+  } else {
+    for (int w = 0; w < nwords; ++w)
+      for (int d = 0; d < 8; ++d) {
+        pass_word.push_back(w);
+        pass_shift.push_back(8 * d);
+      }
+  }
+  uint64_t* kin = keys;
+  uint64_t* kout = keys2;
+  uint32_t* iin = idx;
+  uint32_t* iout = idx2;
+  for (size_t p = 0; p < pass_word.size(); ++p) {
+    GB_CUDA(lsd_count(kin + (size_t)pass_word[p] * n, n, pass_shift[p], counts, st));
+    GB_CUDA(exclusive_scan_u32(counts, counts, (size_t)256 * g, scan_tmp, st));
+    GB_CUDA(lsd_scatter(kin, iin, kout, iout, n, nwords, pass_word[p], pass_shift[p], counts, st));
+    std::swap(kin, kout);
+    std::swap(iin, iout);
+  }
+  if (kin != keys) {  // odd number of passes: move the result home
+    GB_CUDA(cudaMemcpyAsync(keys, kin, sizeof(uint64_t) * n * nwords, cudaMemcpyDeviceToDevice, st));
+    if (idx) GB_CUDA(cudaMemcpyAsync(idx, iin, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st));
+  }
+  if (passes_out) *passes_out = (int)pass_word.size();
+  return GBSORT_OK;
+}
+
+// Generic path over device records: keys from the descriptor (or from radix
+// bytes already on the device), LSD, then one gather into d_out.
+int run_lsd(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize, const gbsort_key_desc* key,
+            const uint8_t* d_radix, uint32_t rsize, cudaStream_t st) {
+  const int nwords = d_radix ? (int)((rsize + 7) / 8) : (int)key->nwords;
+  GB_CUDA(c.keysA.ensure(sizeof(uint64_t) * (size_t)n * nwords));
+  GB_CUDA(c.keysB.ensure(sizeof(uint64_t) * (size_t)n * nwords));
+  GB_CUDA(c.idxA.ensure(sizeof(uint32_t) * (size_t)n));
+  GB_CUDA(c.idxB.ensure(sizeof(uint32_t) * (size_t)n));
+  GB_CUDA(c.small.ensure((size_t)16 << 20));
+  Bump bump{c.small.as<uint8_t>()};
+  if (d_radix) GB_CUDA(radix_bytes_to_keys(d_radix, n, rsize, c.keysA.as<uint64_t>(), c.idxA.as<uint32_t>(), st));
+  else GB_CUDA(extract_keys(d_in, n, elsize, *key, c.keysA.as<uint64_t>(), c.idxA.as<uint32_t>(), st));
+  int passes = 0;
+  int rc = lsd_sort_keys(c, bump, c.keysA.as<uint64_t>(), c.keysB.as<uint64_t>(), c.idxA.as<uint32_t>(),
+                         c.idxB.as<uint32_t>(), n, nwords, true, &passes, st);
+  if (rc) return rc;
+  const void* src = d_in;
+  if (d_in == d_out) {  // the gather needs an untouched copy of the input
+    GB_CUDA(c.A.ensure((size_t)n * elsize));
+    GB_CUDA(cudaMemcpyAsync(c.A.p, d_in, (size_t)n * elsize, cudaMemcpyDeviceToDevice, st));
+    src = c.A.p;
+  }
+  GB_CUDA(gather_records(src, d_out, c.idxA.as<uint32_t>(), n, elsize, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  g_stats = gbsort_stats{};
+  g_stats.method = GBSORT_LSD;
+  g_stats.lsd_passes = (uint32_t)passes;
+  return GBSORT_OK;
+}
+
+// --------------------------------------------------------- hsort path ----
+bool hsort_layout_ok(const void* d_in, const void* d_out, uint32_t elsize, const gbsort_key_desc* key) {
+  if (key->nwords != 1 || !hsort_supported(elsize)) return false;
+  if (key->word[0].offset % 4) return false;
+  uintptr_t a = (uintptr_t)d_in | (uintptr_t)d_out;
+  uint32_t need = elsize % 16 == 0 ? 16 : (elsize % 8 == 0 ? 8 : 4);
+  return a % need == 0;
+}
+
+struct HsortRun {
+  uint32_t nbuckets = 1;
+  uint32_t sample = 0;
+};
+
+int choose_buckets(uint32_t n) {
+  if (n <= 4096) return 1;
+  uint64_t want = ((uint64_t)n + 2047) / 2048;
+  uint32_t nb = pow2_ceil(want);
+  return (int)std::min<uint32_t>(nb, 8192);
+}
+
+int run_tasks_rounds(Context& c, const HsortParams& p, SortTask* t0, SortTask* t1, uint32_t* nt, uint32_t cap,
+                     uint32_t* work, uint32_t* stats, uint32_t* err, cudaStream_t st) {
+  const int kRounds = 8;  // 64-bit keys lose >= 12 bits of range per round
+  SortTask* lists[2] = {t0, t1};
+  for (int r = 0; r < kRounds; ++r) {
+    uint32_t* nin = nt + (r & 1);
+    uint32_t* nout = nt + ((r + 1) & 1);
+    GB_CUDA(cudaMemsetAsync(nout, 0, sizeof(uint32_t), st));
+    GB_CUDA(run_tasks(p, lists[r & 1], nin, lists[(r + 1) & 1], nout, cap, work, stats, err, st));
+  }
+  return GBSORT_OK;
+}
+
+int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize, const gbsort_key_desc* key,
+              int method, cudaStream_t st) {
+  const bool learned = method == GBSORT_HISTOGRAM_LEARNED;
+  GB_CUDA(c.A.ensure((size_t)n * elsize));
+  GB_CUDA(c.B.ensure((size_t)n * elsize));
+  const int nb = choose_buckets(n);
+  const int grid = hsort_grid(n);
+  const uint32_t s = nb > 1 ? (uint32_t)std::min<uint64_t>(n, std::max<uint64_t>(4096, (uint64_t)nb * 128)) : 0;
+  const uint32_t cap = (uint32_t)nb + n / 2048 + 4096;
+  const int lbits = 11;
+  const int nleaf = 1 << lbits;
+  size_t small_bytes = (size_t)s * 16 + (size_t)nb * 8 + (size_t)nb * grid * 8 + (size_t)cap * 2 * sizeof(SortTask) +
+                       (size_t)256 * lsd_grid(std::max<uint32_t>(s, 1)) * 8 + (size_t)nleaf * 64 + (4 << 20);
+  GB_CUDA(c.small.ensure(small_bytes));
+  Bump bump{c.small.as<uint8_t>()};
+  uint32_t* counters = bump.take<uint32_t>(64);  // stats, err, ntasks x2, work, iters, widest
+  uint32_t* stats = counters;
+  uint32_t* err = counters + STAT_SLOTS;  // kernels given `stats` also find the error word here
+  uint32_t* nt = counters + 18;
+  uint32_t* work = counters + 20;
+  uint32_t* iters = counters + 21;
+  uint32_t* widest = counters + 22;
+  float* loss = reinterpret_cast<float*>(counters + 23);
+  GB_CUDA(cudaMemsetAsync(counters, 0, 64 * sizeof(uint32_t), st));
+  uint64_t* S = bump.take<uint64_t>((size_t)std::max(nb, 2));
+  uint32_t* counts = bump.take<uint32_t>((size_t)nb * grid);
+  uint32_t* scan_tmp = bump.take<uint32_t>(scan_tmp_words((size_t)nb * grid));
+  SortTask* t0 = bump.take<SortTask>(cap);
+  SortTask* t1 = bump.take<SortTask>(cap);
+
+  HsortParams p{};
+  p.in = (const uint8_t*)d_in;
+  p.out = (uint8_t*)d_out;
+  p.bufA = c.A.as<uint8_t>();
+  p.bufB = c.B.as<uint8_t>();
+  p.n = n;
+  p.elsize = elsize;
+  p.key = key->word[0];
+
+  ModelDev model{};
+  int lookup = LOOKUP_PLAIN;
+  if (nb > 1) {
+    uint64_t* sA = bump.take<uint64_t>(s);
+    uint64_t* sB = bump.take<uint64_t>(s);
+    GB_CUDA(sample_keys(p.in, n, elsize, p.key, s, sA, st));
+    int rc = lsd_sort_keys(c, bump, sA, sB, nullptr, nullptr, s, 1, false, nullptr, st);
+    if (rc) return rc;
+    if (!learned) {
+      GB_CUDA(plain_splitters(sA, s, nb - 1, S, iters, nullptr, nullptr, st));
+      GB_CUDA(finalize_splitters(S, nb - 1, st));
+    } else {
+      GB_CUDA(cudaMemcpyAsync(&c.hc->kminmax[0], sA, 8, cudaMemcpyDeviceToHost, st));
+      GB_CUDA(cudaMemcpyAsync(&c.hc->kminmax[1], sA + s - 1, 8, cudaMemcpyDeviceToHost, st));
+      GB_CUDA(cudaStreamSynchronize(st));
+      CdfShape sh = cdf_shape(c.hc->kminmax[0], c.hc->kminmax[1], lbits);
+      CdfWork w{};
+      w.y = bump.take<float>(nleaf + 1);
+      w.grad = bump.take<float>(nleaf + 1);
+      w.h = bump.take<float>(nleaf + 1);
+      w.knots = bump.take<float2>(nleaf);
+      w.loss = loss;
+      uint32_t* win = bump.take<uint32_t>(nleaf);
+      uint32_t* wlo = bump.take<uint32_t>(nleaf);
+      uint32_t* whi = bump.take<uint32_t>(nleaf);
+      const int epochs = 8;
+      GB_CUDA(cdf_train(sA, s, sh, epochs, 0.5f, w, st));
+      GB_CUDA(cdf_splitters(sA, s, sh, nb, w.knots, S, st));
+      GB_CUDA(finalize_splitters(S, nb - 1, st));
+      GB_CUDA(cdf_windows(sh, nb, w.knots, S, win, wlo, whi, widest, st));
+      model.kmin = sh.kmin;
+      model.lshift = sh.lshift;
+      model.lbits = sh.lbits;
+      model.nbuckets = nb;
+      model.knots = w.knots;
+      model.win = win;
+      lookup = LOOKUP_LEARNED;
+      GB_CUDA(cudaMemsetAsync(iters, 0, 4, st));
+      c.hc->iters = epochs;
+    }
+  }
+  GB_CUDA(l1_count(p, lookup, S, nb, lookup == LOOKUP_LEARNED ? &model : nullptr, counts, stats, st));
+  GB_CUDA(exclusive_scan_u32(counts, counts, (size_t)nb * grid, scan_tmp, st));
+  GB_CUDA(l1_scatter(p, lookup, S, nb, lookup == LOOKUP_LEARNED ? &model : nullptr, counts, stats, st));
+  GB_CUDA(build_tasks(counts, grid, S, nb, n, t0, nt, cap, err, stats, st));
+  int rc = run_tasks_rounds(c, p, t0, t1, nt, cap, work, stats, err, st);
+  if (rc) return rc;
+  uint32_t learned_iters = learned ? c.hc->iters : 0;
+  GB_CUDA(cudaMemcpyAsync(c.hc->stats, counters, sizeof(uint32_t) * STAT_SLOTS, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(&c.hc->err, err, 4, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(c.hc->ntasks, nt, 8, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(&c.hc->iters, iters, 4, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(&c.hc->widest, widest, 4, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(&c.hc->loss, loss, 4, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  if (c.hc->err) {
+    set_err("device check failed: code %u", c.hc->err);
+    return GBSORT_ERR_INTERNAL;
+  }
+  if (c.hc->ntasks[0] != 0) {  // after 8 rounds the last list (index 0) must be empty
+    set_err("split rounds did not finish: %u tasks left", c.hc->ntasks[0]);
+    return GBSORT_ERR_INTERNAL;
+  }
+  g_stats = gbsort_stats{};
+  g_stats.method = learned ? GBSORT_HISTOGRAM_LEARNED : GBSORT_HISTOGRAM_PLAIN;
+  g_stats.nbuckets = (uint32_t)nb;
+  g_stats.sample = s;
+  g_stats.splitter_rounds = learned ? learned_iters : c.hc->iters;
+  g_stats.local_sorts = c.hc->stats[STAT_LOCAL];
+  g_stats.splits = c.hc->stats[STAT_SPLIT];
+  g_stats.copies = c.hc->stats[STAT_COPY];
+  g_stats.resplits = c.hc->stats[STAT_PUSHED];
+  g_stats.bigbin_passes = c.hc->stats[STAT_BIGBIN];
+  g_stats.window_misses = c.hc->stats[STAT_WINDOW_MISS];
+  g_stats.max_bucket = c.hc->stats[STAT_MAX_BUCKET];
+  g_stats.widest_window = c.hc->widest;
+  g_stats.model_loss = learned ? c.hc->loss : 0.f;
+  return GBSORT_OK;
+}
+
+int sort_device_locked(Context& c, const void* d_in, void* d_out, size_t nmemb, size_t elsize,
+                       const gbsort_key_desc* key, int method, cudaStream_t st) {
+  if (nmemb == 0) return GBSORT_OK;
+  if (nmemb >= 0xffffffffull || elsize == 0 || elsize > (1u << 20)) {
+    set_err("nmemb must be < 2^32 and elsize in [1, 2^20]");
+    return GBSORT_ERR_BAD_ARG;
+  }
+  if (!key_ok(key, elsize)) {
+    set_err("bad key descriptor");
+    return GBSORT_ERR_BAD_ARG;
+  }
+  const uint32_t n = (uint32_t)nmemb, E = (uint32_t)elsize;
+  bool hs_ok = hsort_layout_ok(d_in, d_out, E, key);
+  if (method == GBSORT_AUTO) method = hs_ok ? GBSORT_HISTOGRAM_LEARNED : GBSORT_LSD;
+  if (method == GBSORT_HISTOGRAM_PLAIN || method == GBSORT_HISTOGRAM_LEARNED) {
+    if (!hs_ok) {
+      set_err("histogram sort needs a one-word key at a 4-byte offset and a record size of 8-64 bytes");
+      return GBSORT_ERR_UNSUPPORTED;
+    }
+    return run_hsort(c, d_in, d_out, n, E, key, method, st);
+  }
+  if (method == GBSORT_LSD) return run_lsd(c, d_in, d_out, n, E, key, nullptr, 0, st);
+  set_err("unknown method %d", method);
+  return GBSORT_ERR_BAD_ARG;
+}
+
+}  // namespace
+
+// ============================================================== C ABI ====
+extern "C" {
+
+int gbsort_sort_device(const void* d_in, void* d_out, size_t nmemb, size_t elsize, const gbsort_key_desc* key,
+                       int method, void* stream) {
+  if (nmemb && (!d_in || !d_out)) return GBSORT_ERR_BAD_ARG;
+  Context* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  return sort_device_locked(*c, d_in, d_out, nmemb, elsize, key, method, st);
+}
+
+int gbsort_sort_host(const void* in, void* out, size_t nmemb, size_t elsize, const gbsort_key_desc* key,
+                     int method) {
+  if (nmemb == 0) return GBSORT_OK;
+  if (!in || !out) return GBSORT_ERR_BAD_ARG;
+  if (!key_ok(key, elsize)) {
+    set_err("bad key descriptor");
+    return GBSORT_ERR_BAD_ARG;
+  }
+  Context* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  const size_t bytes = nmemb * elsize;
+  GB_CUDA(c->hin.ensure(bytes));
+  GB_CUDA(c->hout.ensure(bytes));
+  GB_CUDA(cudaMemcpyAsync(c->hin.p, in, bytes, cudaMemcpyHostToDevice, c->stream));
+  rc = sort_device_locked(*c, c->hin.p, c->hout.p, nmemb, elsize, key, method, c->stream);
+  if (rc) return rc;
+  GB_CUDA(cudaMemcpyAsync(out, c->hout.p, bytes, cudaMemcpyDeviceToHost, c->stream));
+  GB_CUDA(cudaStreamSynchronize(c->stream));
+  return GBSORT_OK;
+}
+
+int gbsort_sort_radix_host(void* base, size_t nmemb, size_t elsize,
+                           void (*radix)(const void* ptr, void* radix, void* arg), size_t rsize, void* arg) {
+  if (nmemb <= 1) return GBSORT_OK;
+  if (!base || !radix || rsize == 0 || rsize > 8 * GBSORT_MAX_KEY_WORDS || elsize == 0) {
+    set_err("bad arguments");
+    return GBSORT_ERR_BAD_ARG;
+  }
+  if (nmemb >= 0xffffffffull) return GBSORT_ERR_BAD_ARG;
+  Context* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  // radix bytes on the host, in parallel slices (radix() must be re-entrant,
+  // as the reference's mpsort_omp also calls it from every thread)
+  std::vector<uint8_t> rb(nmemb * rsize);
+  unsigned nth = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  if (nmemb < 65536) nth = 1;
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < nth; ++t) {
+    th.emplace_back([&, t]() {
+      size_t lo = nmemb * t / nth, hi = nmemb * (t + 1) / nth;
+      for (size_t i = lo; i < hi; ++i) radix((const uint8_t*)base + i * elsize, rb.data() + i * rsize, arg);
+    });
+  }
+  for (auto& x : th) x.join();
+  const size_t bytes = nmemb * elsize;
+  GB_CUDA(c->hin.ensure(bytes));
+  GB_CUDA(c->hout.ensure(bytes));
+  GB_CUDA(c->radix.ensure(rb.size()));
+  GB_CUDA(cudaMemcpyAsync(c->hin.p, base, bytes, cudaMemcpyHostToDevice, c->stream));
+  GB_CUDA(cudaMemcpyAsync(c->radix.p, rb.data(), rb.size(), cudaMemcpyHostToDevice, c->stream));
+  rc = run_lsd(*c, c->hin.p, c->hout.p, (uint32_t)nmemb, (uint32_t)elsize, nullptr, c->radix.as<uint8_t>(),
+               (uint32_t)rsize, c->stream);
+  if (rc) return rc;
+  GB_CUDA(cudaMemcpyAsync(base, c->hout.p, bytes, cudaMemcpyDeviceToHost, c->stream));
+  GB_CUDA(cudaStreamSynchronize(c->stream));
+  return GBSORT_OK;
+}
+
+int gbsort_sort_segments_device(const void* d_in, void* d_out, const uint64_t* seg_offsets, size_t nseg,
+                                size_t elsize, const gbsort_key_desc* key, int method, void* stream) {
+  if (nseg == 0) return GBSORT_OK;
+  if (!seg_offsets || !d_in || !d_out) return GBSORT_ERR_BAD_ARG;
+  const uint64_t n = seg_offsets[nseg];
+  if (n == 0) return GBSORT_OK;
+  if (n >= 0xffffffffull || seg_offsets[0] != 0) return GBSORT_ERR_BAD_ARG;
+  for (size_t i = 0; i < nseg; ++i)
+    if (seg_offsets[i + 1] < seg_offsets[i]) return GBSORT_ERR_BAD_ARG;
+  if (!key_ok(key, elsize)) return GBSORT_ERR_BAD_ARG;
+  Context* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  const uint32_t E = (uint32_t)elsize, N = (uint32_t)n;
+  if (!hsort_layout_ok(d_in, d_out, E, key) || method == GBSORT_LSD) {
+    // generic path: one LSD sort per segment
+    for (size_t i = 0; i < nseg; ++i) {
+      uint64_t a = seg_offsets[i], b = seg_offsets[i + 1];
+      if (b == a) continue;
+      rc = sort_device_locked(*c, (const uint8_t*)d_in + a * E, (uint8_t*)d_out + a * E, b - a, E, key,
+                              GBSORT_LSD, st);
+      if (rc) return rc;
+    }
+    return GBSORT_OK;
+  }
+  GB_CUDA(c->A.ensure((size_t)N * E));
+  GB_CUDA(c->B.ensure((size_t)N * E));
+  const uint32_t cap = (uint32_t)nseg + N / 2048 + 4096;
+  GB_CUDA(c->small.ensure((size_t)cap * 2 * sizeof(SortTask) + (nseg + 1) * 8 + (1 << 20)));
+  Bump bump{c->small.as<uint8_t>()};
+  uint32_t* counters = bump.take<uint32_t>(64);
+  uint32_t* stats = counters;
+  uint32_t* err = counters + 16;
+  uint32_t* nt = counters + 18;
+  uint32_t* work = counters + 20;
+  uint64_t* offs = bump.take<uint64_t>(nseg + 1);
+  SortTask* t0 = bump.take<SortTask>(cap);
+  SortTask* t1 = bump.take<SortTask>(cap);
+  GB_CUDA(cudaMemsetAsync(counters, 0, 64 * sizeof(uint32_t), st));
+  GB_CUDA(cudaMemcpyAsync(offs, seg_offsets, (nseg + 1) * 8, cudaMemcpyHostToDevice, st));
+  GB_CUDA(cudaMemcpyAsync(c->A.p, d_in, (size_t)N * E, cudaMemcpyDeviceToDevice, st));
+  GB_CUDA(segment_ranges(c->A.as<uint8_t>(), E, key->word[0], offs, (uint32_t)nseg, t0, nt, cap, err, st));
+  HsortParams p{};
+  p.in = (const uint8_t*)d_in;
+  p.out = (uint8_t*)d_out;
+  p.bufA = c->A.as<uint8_t>();
+  p.bufB = c->B.as<uint8_t>();
+  p.n = N;
+  p.elsize = E;
+  p.key = key->word[0];
+  rc = run_tasks_rounds(*c, p, t0, t1, nt, cap, work, stats, err, st);
+  if (rc) return rc;
+  GB_CUDA(cudaMemcpyAsync(c->hc->stats, counters, sizeof(uint32_t) * STAT_SLOTS, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(&c->hc->err, err, 4, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(c->hc->ntasks, nt, 8, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  if (c->hc->err || c->hc->ntasks[0]) {
+    set_err("segmented sort device check failed: code %u, %u tasks left", c->hc->err, c->hc->ntasks[0]);
+    return GBSORT_ERR_INTERNAL;
+  }
+  g_stats = gbsort_stats{};
+  g_stats.method = GBSORT_HISTOGRAM_PLAIN;
+  g_stats.nbuckets = (uint32_t)nseg;
+  g_stats.local_sorts = c->hc->stats[STAT_LOCAL];
+  g_stats.splits = c->hc->stats[STAT_SPLIT];
+  g_stats.copies = c->hc->stats[STAT_COPY];
+  g_stats.resplits = c->hc->stats[STAT_PUSHED];
+  g_stats.bigbin_passes = c->hc->stats[STAT_BIGBIN];
+  return GBSORT_OK;
+}
+
+int gbsort_merge_join_device(const void* d_a, size_t na, const void* d_b, size_t nb, size_t elsize,
+                             const gbsort_key_desc* key, uint64_t* d_pairs_a, uint64_t* d_pairs_b, uint64_t* d_npairs,
+                             void* stream) {
+  if (!d_npairs || !key_ok(key, elsize) || key->nwords != 1 || key->word[0].offset % 4 || elsize % 4)
+    return GBSORT_ERR_BAD_ARG;
+  if (na >= 0xffffffffull || nb >= 0xffffffffull) return GBSORT_ERR_BAD_ARG;
+  Context* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  if (na == 0 || nb == 0) {
+    GB_CUDA(cudaMemsetAsync(d_npairs, 0, 8, st));
+    return GBSORT_OK;
+  }
+  const int g = join_grid((uint32_t)na);
+  GB_CUDA(c->small.ensure((size_t)g * 8 + (1 << 20)));
+  Bump bump{c->small.as<uint8_t>()};
+  uint32_t* counts = bump.take<uint32_t>(g + 1);
+  uint32_t* tmp = bump.take<uint32_t>(scan_tmp_words(g + 1));
+  GB_CUDA(join_count((const uint8_t*)d_a, (uint32_t)na, (const uint8_t*)d_b, (uint32_t)nb, (uint32_t)elsize,
+                     key->word[0], counts, g, st));
+  GB_CUDA(exclusive_scan_u32(counts, counts, (size_t)g + 1, tmp, st));
+  GB_CUDA(join_write((const uint8_t*)d_a, (uint32_t)na, (const uint8_t*)d_b, (uint32_t)nb, (uint32_t)elsize,
+                     key->word[0], counts, g, d_pairs_a, d_pairs_b, d_npairs, st));
+  return GBSORT_OK;
+}
+
+int gbsort_cdf_forward_backward(const uint64_t* x, uint32_t s, uint64_t kmin, uint64_t kmax, int lbits,
+                                const float* y, float* loss, float* pred, float* grad) {
+  if (!x || !y || s == 0 || lbits < 0 || lbits > 16) return GBSORT_ERR_BAD_ARG;
+  Context* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  const int nk = (1 << lbits) + 1;
+  GB_CUDA(c->small.ensure((size_t)s * 12 + (size_t)nk * 8 + (1 << 16)));
+  Bump bump{c->small.as<uint8_t>()};
+  uint64_t* dx = bump.take<uint64_t>(s);
+  float* dy = bump.take<float>(nk);
+  float* dg = bump.take<float>(nk);
+  float* dp = bump.take<float>(s);
+  float* dl = bump.take<float>(1);
+  cudaStream_t st = c->stream;
+  GB_CUDA(cudaMemcpyAsync(dx, x, (size_t)s * 8, cudaMemcpyHostToDevice, st));
+  GB_CUDA(cudaMemcpyAsync(dy, y, (size_t)nk * 4, cudaMemcpyHostToDevice, st));
+  CdfShape sh = cdf_shape(kmin, kmax, lbits);
+  GB_CUDA(cdf_forward(dx, s, sh, dy, dp, dl, st));
+  GB_CUDA(cdf_backward(dx, s, sh, dy, dg, st));
+  if (loss) GB_CUDA(cudaMemcpyAsync(loss, dl, 4, cudaMemcpyDeviceToHost, st));
+  if (pred) GB_CUDA(cudaMemcpyAsync(pred, dp, (size_t)s * 4, cudaMemcpyDeviceToHost, st));
+  if (grad) GB_CUDA(cudaMemcpyAsync(grad, dg, (size_t)nk * 4, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  return GBSORT_OK;
+}
+
+int gbsort_debug_bisect(const uint64_t* sorted, uint32_t s, int nsplit, uint64_t* splitters, int64_t* clt,
+                        int64_t* cle, uint32_t* rounds) {
+  if (!sorted || s == 0 || nsplit <= 0) return GBSORT_ERR_BAD_ARG;
+  Context* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  GB_CUDA(c->small.ensure((size_t)s * 8 + (size_t)nsplit * 24 + (1 << 16)));
+  Bump bump{c->small.as<uint8_t>()};
+  uint64_t* dx = bump.take<uint64_t>(s);
+  uint64_t* dS = bump.take<uint64_t>(nsplit);
+  int64_t* dlt = bump.take<int64_t>(nsplit);
+  int64_t* dle = bump.take<int64_t>(nsplit);
+  uint32_t* dit = bump.take<uint32_t>(1);
+  cudaStream_t st = c->stream;
+  GB_CUDA(cudaMemcpyAsync(dx, sorted, (size_t)s * 8, cudaMemcpyHostToDevice, st));
+  GB_CUDA(plain_splitters(dx, s, nsplit, dS, dit, dlt, dle, st));
+  GB_CUDA(cudaMemcpyAsync(splitters, dS, (size_t)nsplit * 8, cudaMemcpyDeviceToHost, st));
+  if (clt) GB_CUDA(cudaMemcpyAsync(clt, dlt, (size_t)nsplit * 8, cudaMemcpyDeviceToHost, st));
+  if (cle) GB_CUDA(cudaMemcpyAsync(cle, dle, (size_t)nsplit * 8, cudaMemcpyDeviceToHost, st));
+  if (rounds) GB_CUDA(cudaMemcpyAsync(rounds, dit, 4, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  return GBSORT_OK;
+}
+
+int gbsort_debug_buckets(const uint64_t* sample, uint32_t s, int nbuckets, const uint64_t* keys, uint32_t nkeys,
+                         uint32_t* bucket_search, uint32_t* bucket_learned, uint64_t* splitters,
+                         uint32_t* widest_window) {
+  if (!sample || s == 0 || nbuckets < 2 || nbuckets > 8192 || !keys) return GBSORT_ERR_BAD_ARG;
+  Context* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  const int lbits = 11, nleaf = 1 << lbits;
+  GB_CUDA(c->small.ensure((size_t)s * 8 + (size_t)nkeys * 16 + (size_t)nbuckets * 8 + (size_t)nleaf * 64 +
+                          (1 << 20)));
+  Bump bump{c->small.as<uint8_t>()};
+  uint64_t* dx = bump.take<uint64_t>(s);
+  uint64_t* dk = bump.take<uint64_t>(nkeys);
+  uint32_t* dl = bump.take<uint32_t>(nkeys);
+  uint32_t* ds = bump.take<uint32_t>(nkeys);
+  uint64_t* S = bump.take<uint64_t>(nbuckets);
+  uint32_t* misc = bump.take<uint32_t>(4);
+  CdfWork w{};
+  w.y = bump.take<float>(nleaf + 1);
+  w.grad = bump.take<float>(nleaf + 1);
+  w.h = bump.take<float>(nleaf + 1);
+  w.knots = bump.take<float2>(nleaf);
+  uint32_t* win = bump.take<uint32_t>(nleaf);
+  uint32_t* wlo = bump.take<uint32_t>(nleaf);
+  uint32_t* whi = bump.take<uint32_t>(nleaf);
+  cudaStream_t st = c->stream;
+  std::vector<uint64_t> hs(sample, sample + s);
+  std::sort(hs.begin(), hs.end());
+  GB_CUDA(cudaMemcpyAsync(dx, hs.data(), (size_t)s * 8, cudaMemcpyHostToDevice, st));
+  GB_CUDA(cudaMemcpyAsync(dk, keys, (size_t)nkeys * 8, cudaMemcpyHostToDevice, st));
+  GB_CUDA(cudaMemsetAsync(misc, 0, 16, st));
+  CdfShape sh = cdf_shape(hs.front(), hs.back(), lbits);
+  GB_CUDA(cdf_train(dx, s, sh, 8, 0.5f, w, st));
+  GB_CUDA(cdf_splitters(dx, s, sh, nbuckets, w.knots, S, st));
+  GB_CUDA(finalize_splitters(S, nbuckets - 1, st));
+  GB_CUDA(cdf_windows(sh, nbuckets, w.knots, S, win, wlo, whi, misc, st));
+  ModelDev m{};
+  m.kmin = sh.kmin;
+  m.lshift = sh.lshift;
+  m.lbits = sh.lbits;
+  m.nbuckets = nbuckets;
+  m.knots = w.knots;
+  m.win = win;
+  GB_CUDA(probe_buckets(dk, nkeys, S, &m, dl, ds, misc + 1, st));
+  if (bucket_learned) GB_CUDA(cudaMemcpyAsync(bucket_learned, dl, (size_t)nkeys * 4, cudaMemcpyDeviceToHost, st));
+  if (bucket_search) GB_CUDA(cudaMemcpyAsync(bucket_search, ds, (size_t)nkeys * 4, cudaMemcpyDeviceToHost, st));
+  if (splitters) GB_CUDA(cudaMemcpyAsync(splitters, S, (size_t)(nbuckets - 1) * 8, cudaMemcpyDeviceToHost, st));
+  uint32_t hm[2] = {0, 0};
+  GB_CUDA(cudaMemcpyAsync(hm, misc, 8, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  if (widest_window) *widest_window = hm[0];
+  g_stats.window_misses = hm[1];
+  return GBSORT_OK;
+}
+
+int gbsort_last_stats(gbsort_stats* out) {
+  if (!out) return GBSORT_ERR_BAD_ARG;
+  *out = g_stats;
+  return GBSORT_OK;
+}
+
+const char* gbsort_status_string(int status) {
+  switch (status) {
+    case GBSORT_OK: return "ok";
+    case GBSORT_ERR_BAD_ARG: return "bad argument";
+    case GBSORT_ERR_OOM: return "out of memory";
+    case GBSORT_ERR_CUDA: return "CUDA error";
+    case GBSORT_ERR_NO_DEVICE: return "no CUDA device";
+    case GBSORT_ERR_INTERNAL: return "device consistency check failed";
+    case GBSORT_ERR_UNSUPPORTED: return "unsupported layout for this method";
+    default: return "unknown status";
+  }
+}
+
+const char* gbsort_last_error(void) { return g_err; }
+
+int gbsort_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int gbsort_release(void) {
+  Context* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaStreamSynchronize(c->stream);
+  DevBuf* bufs[] = {&c->A, &c->B, &c->hin, &c->hout, &c->keysA, &c->keysB, &c->idxA, &c->idxB, &c->small, &c->radix};
+  for (DevBuf* b : bufs) b->release();
+  return GBSORT_OK;
+}
+
+const char* gbsort_version(void) { return "gbsort 0.1.0 (sm_103a)"; }
+
+// ---------------------------------------------------------- drop-ins ----
+void mpsort_radix_desc(const void* ptr, void* radix, void* arg) {
+  const gbsort_key_desc* d = (const gbsort_key_desc*)arg;
+  const uint8_t* rec = (const uint8_t*)ptr;
+  uint8_t* out = (uint8_t*)radix;
+  for (uint32_t i = 0; i < d->nwords; ++i) {
+    const gbsort_key_word& w = d->word[i];
+    uint64_t v;
+    if (w.width == 8) {
+      memcpy(&v, rec + w.offset, 8);
+      if (w.is_signed) v += 0x8000000000000000ull;
+    } else {
+      uint32_t u;
+      memcpy(&u, rec + w.offset, 4);
+      v = w.is_signed ? (uint64_t)(int64_t)(int32_t)u + 0x8000000000000000ull : (uint64_t)u;
+    }
+    memcpy(out + 8 * i, &v, 8);
+  }
+}
+
+static void dropin_sort(void* base, size_t nmemb, size_t size, void (*radix)(const void*, void*, void*),
+                        size_t rsize, void* arg, const char* who) {
+  int rc;
+  if (nmemb == 0) {
+    g_mpsort_status = GBSORT_OK;
+    return;
+  }
+  if (radix == mpsort_radix_desc) {
+    const gbsort_key_desc* d = (const gbsort_key_desc*)arg;
+    if (!d || rsize != 8u * d->nwords) rc = GBSORT_ERR_BAD_ARG;
+    else rc = gbsort_sort_host(base, base, nmemb, size, d, GBSORT_AUTO);
+  } else {
+    rc = gbsort_sort_radix_host(base, nmemb, size, radix, rsize, arg);
+  }
+  g_mpsort_status = rc;
+  if (rc != GBSORT_OK)
+    fprintf(stderr, "%s: GPU sort failed (%s): %s; data left unsorted\n", who, gbsort_status_string(rc), g_err);
+}
+
+void radix_sort(void* base, size_t nmemb, size_t size, void (*radix)(const void* ptr, void* radix, void* arg),
+                size_t rsize, void* arg) {
+  dropin_sort(base, nmemb, size, radix, rsize, arg, "radix_sort");
+}
+
+void mpsort_omp(void* base, size_t nmemb, size_t size, void (*radix)(const void* ptr, void* radix, void* arg),
+                size_t rsize, void* arg) {
+  dropin_sort(base, nmemb, size, radix, rsize, arg, "mpsort_omp");
+}
+
+int mpsort_last_status(void) { return g_mpsort_status; }
+
+void mpsort_mpi_set_options(int options) {
+  std::lock_guard<std::mutex> lk(g_opt_mu);
+  g_mpi_options |= options;
+}
+int mpsort_mpi_has_options(int options) {
+  std::lock_guard<std::mutex> lk(g_opt_mu);
+  return (g_mpi_options & options) == options;
+}
+void mpsort_mpi_unset_options(int options) {
+  std::lock_guard<std::mutex> lk(g_opt_mu);
+  g_mpi_options &= ~options;
+}
+
+}  // extern "C"

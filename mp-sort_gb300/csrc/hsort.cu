@@ -1,0 +1,916 @@
+// hsort.cu -- the histogram sort: the GB300 form of mpsort_omp's
+// sample / split / exchange / local-sort pipeline for single-word keys.
+//
+//   reference stage (mpsort-omp.c)          device stage (this file)
+//   ------------------------------------    ----------------------------------
+//   radix_sort of each chunk (:247)          sample_keys + LSD sort of a sample
+//   Pmin/Pmax, piter bisection (:251-295)    k_plain_splitters / learned model
+//   _histogram + _reduce_sum (:286-289)      k_l1_count: (bucket x chunk) counts
+//   _solve_for_layout (:331)                 scan of the count matrix
+//   memcpy exchange (:338-369)               k_l1_scatter: stable bucket scatter
+//   radix_sort of each chunk again (:389)    k_tasks: split + shared-memory sort
+//
+// Records stay whole (any size that is a multiple of 4 bytes, up to 64) and
+// the result is the stable order by key, record for record.  The buffers:
+// input -> scratch A (level 1), A -> scratch B (bucket splits), and every
+// final local sort writes the output, so the output may alias the input.
+#include "cdf.cuh"
+#include "common.cuh"
+#include "kernels.h"
+
+namespace gb {
+
+int num_sms();
+
+namespace {
+
+constexpr int kLocalMax = 4096;        // records a local sort holds in shared memory
+constexpr int kLocalRpt = kLocalMax / kThreads;
+constexpr int kLocalBits = 10;         // digit of the local MSD pass
+constexpr int kInsertMax = 24;         // bins up to this size use insertion sort
+constexpr int kSplitBits = 12;         // bins of a bucket split
+constexpr int kSplitBins = 1 << kSplitBits;
+constexpr int kMaxGroups = 256;        // sub-buckets per split
+constexpr uint32_t kCopyPiece = 1u << 16;
+
+__host__ __device__ __forceinline__ uint32_t chunk_begin(uint32_t n, uint32_t c, uint32_t g) {
+  return (uint32_t)(((uint64_t)n * c / g) & ~(uint64_t)31);
+}
+__host__ __device__ __forceinline__ uint32_t chunk_end(uint32_t n, uint32_t c, uint32_t g) {
+  return c + 1 == g ? n : chunk_begin(n, c + 1, g);
+}
+
+// ------------------------------------------------------------ record I/O --
+// A record of EW 32-bit words moved with the widest vector that divides it.
+template <int EW>
+struct RecIO {
+  __device__ __forceinline__ static void load(const uint8_t* p, uint32_t (&r)[EW]) {
+    if constexpr (EW % 4 == 0) {
+#pragma unroll
+      for (int i = 0; i < EW / 4; ++i) {
+        uint4 v = reinterpret_cast<const uint4*>(p)[i];
+        r[4 * i] = v.x; r[4 * i + 1] = v.y; r[4 * i + 2] = v.z; r[4 * i + 3] = v.w;
+      }
+    } else if constexpr (EW % 2 == 0) {
+#pragma unroll
+      for (int i = 0; i < EW / 2; ++i) {
+        uint2 v = reinterpret_cast<const uint2*>(p)[i];
+        r[2 * i] = v.x; r[2 * i + 1] = v.y;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < EW; ++i) r[i] = reinterpret_cast<const uint32_t*>(p)[i];
+    }
+  }
+  __device__ __forceinline__ static void store(uint8_t* p, const uint32_t (&r)[EW]) {
+    if constexpr (EW % 4 == 0) {
+#pragma unroll
+      for (int i = 0; i < EW / 4; ++i)
+        reinterpret_cast<uint4*>(p)[i] = make_uint4(r[4 * i], r[4 * i + 1], r[4 * i + 2], r[4 * i + 3]);
+    } else if constexpr (EW % 2 == 0) {
+#pragma unroll
+      for (int i = 0; i < EW / 2; ++i) reinterpret_cast<uint2*>(p)[i] = make_uint2(r[2 * i], r[2 * i + 1]);
+    } else {
+#pragma unroll
+      for (int i = 0; i < EW; ++i) reinterpret_cast<uint32_t*>(p)[i] = r[i];
+    }
+  }
+};
+
+// Block copy of `count` records of EW words from src to dst (distinct).
+template <int EW>
+__device__ __forceinline__ void block_copy(const uint8_t* src, uint8_t* dst, uint32_t count) {
+  constexpr int E = EW * 4;
+  if constexpr (EW % 4 == 0) {
+    const uint64_t nv = (uint64_t)count * (E / 16);
+    for (uint64_t f = threadIdx.x; f < nv; f += kThreads)
+      reinterpret_cast<uint4*>(dst)[f] = reinterpret_cast<const uint4*>(src)[f];
+  } else if constexpr (EW % 2 == 0) {
+    const uint64_t nv = (uint64_t)count * (E / 8);
+    for (uint64_t f = threadIdx.x; f < nv; f += kThreads)
+      reinterpret_cast<uint2*>(dst)[f] = reinterpret_cast<const uint2*>(src)[f];
+  } else {
+    const uint64_t nv = (uint64_t)count * EW;
+    for (uint64_t f = threadIdx.x; f < nv; f += kThreads)
+      reinterpret_cast<uint32_t*>(dst)[f] = reinterpret_cast<const uint32_t*>(src)[f];
+  }
+}
+
+__device__ __forceinline__ uint64_t key_at(const uint8_t* base, uint32_t i, uint32_t elsize,
+                                           const gbsort_key_word& kw) {
+  return load_key_aligned4(base + (size_t)i * elsize, kw);
+}
+
+// --------------------------------------------------------------- sample --
+__global__ void k_sample(const uint8_t* __restrict__ rec, uint32_t n, uint32_t elsize,
+                         gbsort_key_word kw, uint32_t s, uint64_t* __restrict__ out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s; i += gridDim.x * blockDim.x) {
+    uint32_t j = (uint32_t)((uint64_t)i * n / s);
+    out[i] = key_at(rec, j, elsize, kw);
+  }
+}
+
+// ----------------------------------------------------- plain splitters --
+// One thread per splitter runs the reference's bisection for that splitter
+// (piter_bisect / _histogram / piter_accept, internal-parallel.h:150-248)
+// against the sorted sample, which plays the role of the locally sorted
+// chunks.  The splitters never interact, so running each one's rounds to
+// completion independently gives the same values as the reference's
+// lock-step rounds; `iters` receives the number of rounds of the slowest.
+__device__ __forceinline__ uint32_t count_lt(const uint64_t* a, uint32_t n, uint64_t p) {
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    uint32_t m = (lo + hi) >> 1;
+    if (a[m] < p) lo = m + 1; else hi = m;
+  }
+  return lo;
+}
+__device__ __forceinline__ uint32_t count_le(const uint64_t* a, uint32_t n, uint64_t p) {
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    uint32_t m = (lo + hi) >> 1;
+    if (a[m] <= p) lo = m + 1; else hi = m;
+  }
+  return lo;
+}
+
+__global__ void k_plain_splitters(const uint64_t* __restrict__ sample, uint32_t s, int nsplit,
+                                  uint64_t* __restrict__ P, uint32_t* iters, int64_t* clt,
+                                  int64_t* cle) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsplit) return;
+  const int64_t C = (int64_t)((uint64_t)s * (uint64_t)(i + 1) / (uint64_t)(nsplit + 1));
+  uint64_t left = sample[0], right = sample[s - 1], p = left;
+  bool narrow = false;
+  uint32_t it = 0;
+  for (;;) {
+    ++it;
+    if (narrow) {           // last round: test right itself, then stop
+      p = right;
+      break;
+    }
+    p = left + ((right - left) >> 1);
+    if (p <= left) narrow = true;
+    int64_t lt = count_lt(sample, s, p), le = count_le(sample, s, p);
+    if (lt < C && C <= le) break;
+    if (lt >= C) right = p; else left = p;
+    if (it > 200) break;    // cannot happen for 64-bit keys; keeps the loop bounded
+  }
+  P[i] = p;
+  atomicMax(iters, it);
+  if (clt) clt[i] = count_lt(sample, s, p);
+  if (cle) cle[i] = count_le(sample, s, p);
+}
+
+// Runs of equal splitters become single-key buckets: [.., k, k, k, ..] ->
+// [.., k, k+1, k+1, ..], so every record of a heavy key k lands in the bucket
+// [k, k+1) and needs no sort at all.
+__global__ void __launch_bounds__(1024) k_finalize_splitters(uint64_t* S, int nsplit) {
+  constexpr int PER = 8;  // nsplit <= 8192
+  uint64_t cur[PER], prev[PER];
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    int i = threadIdx.x + j * 1024;
+    cur[j] = i < nsplit ? S[i] : 0;
+    prev[j] = (i > 0 && i < nsplit) ? S[i - 1] : 0;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    int i = threadIdx.x + j * 1024;
+    if (i > 0 && i < nsplit && cur[j] == prev[j] && cur[j] != ~0ull) S[i] = cur[j] + 1;
+  }
+}
+
+// ---------------------------------------------------------- lookups ------
+struct LookupSmem {
+  uint64_t* S;
+  float2* knots;
+  uint32_t* win;
+};
+
+template <int LK>
+__device__ __forceinline__ uint32_t lookup(const LookupSmem& L, const ModelDev& m, int nbuckets,
+                                           uint64_t key, uint32_t* misses) {
+  if constexpr (LK == LOOKUP_PLAIN) return bucket_plain(L.S, nbuckets, key);
+  else return bucket_learned(L.S, m, L.knots, L.win, key, misses);
+}
+
+// Loads splitters (and the model tables) into shared memory at `smem`;
+// returns the first free byte.
+template <int LK>
+__device__ __forceinline__ uint8_t* load_lookup(uint8_t* smem, const uint64_t* S, int nbuckets,
+                                                const ModelDev& m, LookupSmem& L) {
+  L.S = reinterpret_cast<uint64_t*>(smem);
+  for (int i = threadIdx.x; i < nbuckets - 1; i += blockDim.x) L.S[i] = S[i];
+  smem += 8 * (size_t)((nbuckets + 1) & ~1);
+  if constexpr (LK == LOOKUP_LEARNED) {
+    const int nl = 1 << m.lbits;
+    L.knots = reinterpret_cast<float2*>(smem);
+    for (int i = threadIdx.x; i < nl; i += blockDim.x) L.knots[i] = m.knots[i];
+    smem += 8 * (size_t)nl;
+    L.win = reinterpret_cast<uint32_t*>(smem);
+    for (int i = threadIdx.x; i < nl; i += blockDim.x) L.win[i] = m.win[i];
+    smem += 4 * (size_t)nl;
+  }
+  return smem;
+}
+
+template <int LK>
+size_t lookup_smem_bytes(int nbuckets, const ModelDev* m) {
+  size_t b = 8 * (size_t)((nbuckets + 1) & ~1);
+  if (LK == LOOKUP_LEARNED) b += 12 * ((size_t)1 << m->lbits);
+  return b;
+}
+
+// ----------------------------------------------------- level-1 count ------
+template <int LK>
+__global__ void __launch_bounds__(kThreads) k_l1_count(HsortParams p, const uint64_t* __restrict__ S,
+                                                        int nbuckets, ModelDev model,
+                                                        uint32_t* __restrict__ counts,
+                                                        uint32_t* __restrict__ stats) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  LookupSmem L;
+  uint32_t* hist = reinterpret_cast<uint32_t*>(load_lookup<LK>(smem, S, nbuckets, model, L));
+  for (int i = threadIdx.x; i < nbuckets; i += kThreads) hist[i] = 0;
+  __syncthreads();
+  const uint32_t c = blockIdx.x, g = gridDim.x;
+  const uint32_t cb = chunk_begin(p.n, c, g), ce = chunk_end(p.n, c, g);
+  constexpr int U = 8;
+  for (uint32_t base = cb; base < ce; base += kThreads * U) {
+    uint64_t k[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      uint32_t i = base + u * kThreads + threadIdx.x;
+      k[u] = i < ce ? key_at(p.in, i, p.elsize, p.key) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      uint32_t i = base + u * kThreads + threadIdx.x;
+      bool v = i < ce;
+      uint32_t b = v ? lookup<LK>(L, model, nbuckets, k[u], stats + STAT_WINDOW_MISS) : 0xffffffffu;
+      uint32_t peers = __match_any_sync(GB_FULL_MASK, b);
+      if (v && (peers & lanemask_lt()) == 0) atomicAdd(&hist[b], (uint32_t)__popc(peers));
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nbuckets; b += kThreads) counts[(size_t)b * g + c] = hist[b];
+}
+
+// --------------------------------------------------- level-1 scatter ------
+template <int EW>
+struct Tile {
+  static constexpr int kRpt = (32 / EW) < 1 ? 1 : (32 / EW);
+  static constexpr int kSize = kThreads * kRpt;
+};
+
+// Stable scatter of each chunk into its buckets.  Per tile: records in
+// registers, bucket ids ranked stably in two 7-bit passes (low bits, then
+// high bits), then each record goes to cursor[bucket] + its rank in the
+// bucket's run of the tile; cursors start at the scanned (bucket, chunk)
+// offsets, so chunk order and tile order are both preserved.
+template <int EW, int LK>
+__global__ void __launch_bounds__(kThreads, 1) k_l1_scatter(HsortParams p, const uint64_t* __restrict__ S,
+                                                             int nbuckets, ModelDev model,
+                                                             const uint32_t* __restrict__ offsets,
+                                                             uint32_t* __restrict__ stats) {
+  uint32_t* err = stats + STAT_SLOTS;  // the error word follows the statistics
+  constexpr int RPT = Tile<EW>::kRpt, T = Tile<EW>::kSize;
+  using Rank = BlockRank<RPT, 7>;
+  extern __shared__ __align__(16) uint8_t smem[];
+  LookupSmem L;
+  uint8_t* q = load_lookup<LK>(smem, S, nbuckets, model, L);
+  uint32_t* cursor = reinterpret_cast<uint32_t*>(q);
+  q += 4 * (size_t)((nbuckets + 3) & ~3);
+  uint16_t* hist = reinterpret_cast<uint16_t*>(q);
+  q += 2 * Rank::kCounters;
+  uint16_t* bsorted = reinterpret_cast<uint16_t*>(q);
+  q += 2 * T;
+  uint16_t* fpos = reinterpret_cast<uint16_t*>(q);
+  q += 2 * T;
+  uint16_t* bfinal = reinterpret_cast<uint16_t*>(q);
+  q += 2 * T;
+  __shared__ uint32_t scan_tmp[kWarps];
+
+  const uint32_t c = blockIdx.x, g = gridDim.x;
+  const uint32_t cb = chunk_begin(p.n, c, g), ce = chunk_end(p.n, c, g);
+  for (int b = threadIdx.x; b < nbuckets; b += kThreads) cursor[b] = offsets[(size_t)b * g + c];
+  __syncthreads();
+  const uint32_t w = warp_id(), lane = lane_id();
+  const uint32_t E = EW * 4;
+  const bool two_pass = nbuckets > 128;
+
+  for (uint32_t t0 = cb; t0 < ce; t0 += T) {
+    const uint32_t nvalid = min((uint32_t)T, ce - t0);
+    uint32_t rec[RPT][EW];
+    uint32_t bkt[RPT], dig[RPT], pos[RPT];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+      uint32_t e = w * 32 * RPT + r * 32 + lane;
+      if (e < nvalid) RecIO<EW>::load(p.in + (size_t)(t0 + e) * E, rec[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+      uint32_t e = w * 32 * RPT + r * 32 + lane;
+      if (e < nvalid) {
+        uint64_t k = key_from_regs<EW>(rec[r], p.key);
+        bkt[r] = lookup<LK>(L, model, nbuckets, k, stats + STAT_WINDOW_MISS);
+      } else {
+        bkt[r] = 0x3fffu;  // sorts after every real bucket in both passes
+      }
+      dig[r] = bkt[r] & 127u;
+    }
+    Rank::rank(dig, pos, hist, scan_tmp, nullptr);
+    if (two_pass) {
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) bsorted[pos[r]] = (uint16_t)bkt[r];
+      __syncthreads();
+      uint32_t kb[RPT], pos2[RPT];
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) {
+        uint32_t k = w * 32 * RPT + r * 32 + lane;
+        kb[r] = bsorted[k];
+        dig[r] = kb[r] >> 7;
+      }
+      Rank::rank(dig, pos2, hist, scan_tmp, nullptr);
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) {
+        uint32_t k = w * 32 * RPT + r * 32 + lane;
+        fpos[k] = (uint16_t)pos2[r];
+        bfinal[pos2[r]] = (uint16_t)kb[r];
+      }
+      __syncthreads();
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) pos[r] = fpos[pos[r]];
+    } else {
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) bfinal[pos[r]] = (uint16_t)bkt[r];
+      __syncthreads();
+    }
+    // run heads turn cursor[b] into cursor[b] - head_position
+    for (uint32_t i = threadIdx.x; i < nvalid; i += kThreads) {
+      uint32_t b = bfinal[i];
+      if (i == 0 || bfinal[i - 1] != b) cursor[b] -= i;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+      uint32_t e = w * 32 * RPT + r * 32 + lane;
+      if (e < nvalid) {
+        uint32_t dest = cursor[bkt[r]] + pos[r];
+        if (dest < p.n) RecIO<EW>::store(p.bufA + (size_t)dest * E, rec[r]);
+        else set_error(err, DEV_ERR_COUNT_MISMATCH);
+      }
+    }
+    __syncthreads();
+    // run tails advance the cursors past the tile's records
+    for (uint32_t i = threadIdx.x; i < nvalid; i += kThreads) {
+      uint32_t b = bfinal[i];
+      if (i + 1 == nvalid || bfinal[i + 1] != b) cursor[b] += i + 1;
+    }
+    __syncthreads();
+  }
+}
+
+template <int EW, int LK>
+size_t l1_scatter_smem(int nbuckets, const ModelDev* m) {
+  using Rank = BlockRank<Tile<EW>::kRpt, 7>;
+  return lookup_smem_bytes<LK>(nbuckets, m) + 4 * (size_t)((nbuckets + 3) & ~3) +
+         2 * Rank::kCounters + 3 * 2 * (size_t)Tile<EW>::kSize;
+}
+
+// ------------------------------------------------------------- tasks -----
+__global__ void k_build_tasks(const uint32_t* __restrict__ offsets, int grid,
+                              const uint64_t* __restrict__ S, int nbuckets, uint32_t n,
+                              SortTask* __restrict__ tasks, uint32_t* ntasks, uint32_t cap,
+                              uint32_t* err, uint32_t* stats) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbuckets) return;
+  uint32_t start = offsets[(size_t)b * grid];
+  uint32_t end = b + 1 < nbuckets ? offsets[(size_t)(b + 1) * grid] : n;
+  uint32_t cnt = end - start;
+  if (cnt == 0) return;
+  atomicMax(stats + STAT_MAX_BUCKET, cnt);
+  uint64_t lo = b == 0 ? 0ull : S[b - 1];
+  uint64_t hi = b == nbuckets - 1 ? ~0ull : S[b] - 1;
+  if (lo == hi || cnt == 1) {
+    uint32_t pieces = (cnt + kCopyPiece - 1) / kCopyPiece;
+    uint32_t at = atomicAdd(ntasks, pieces);
+    if (at + pieces > cap) { set_error(err, DEV_ERR_TASK_OVERFLOW); return; }
+    for (uint32_t i = 0; i < pieces; ++i) {
+      uint32_t s0 = start + i * kCopyPiece;
+      tasks[at + i] = SortTask{s0, min(kCopyPiece, end - s0), lo, hi, 0u, TASK_COPY};
+    }
+  } else {
+    uint32_t at = atomicAdd(ntasks, 1u);
+    if (at >= cap) { set_error(err, DEV_ERR_TASK_OVERFLOW); return; }
+    tasks[at] = SortTask{start, cnt, lo, hi, 0u, TASK_SORT};
+  }
+}
+
+// Shared memory of the task engine (a union of the split and local phases).
+struct LocalSmem {
+  uint64_t key[kLocalMax];
+  uint16_t idx[kLocalMax];
+  uint16_t hist[kWarps << kLocalBits];
+  uint32_t start[(1 << kLocalBits) + 1];
+  uint16_t big[kLocalMax / (kInsertMax + 1) + 2];  // start of pending bins
+  uint16_t bigsz[kLocalMax / (kInsertMax + 1) + 2];
+  uint32_t nbig;
+  uint64_t red[2 * kWarps];
+};
+struct SplitSmem {
+  uint32_t hist[kSplitBins];
+  uint8_t gmap[kSplitBins];
+  uint32_t cursor[kMaxGroups];
+  uint32_t dstart[kMaxGroups + 1];
+  uint16_t rhist[kWarps * kMaxGroups];
+};
+struct EngineSmem {
+  union {
+    LocalSmem loc;
+    SplitSmem spl;
+  };
+  uint32_t gstart[kMaxGroups + 1];  // split groups: kept while local sorts reuse the union
+  uint32_t gfirst[kMaxGroups + 1];
+  uint32_t scan_tmp[kWarps];
+  uint32_t task_id;
+};
+
+__device__ __forceinline__ void block_minmax(uint64_t& mn, uint64_t& mx, uint64_t* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    uint64_t a = __shfl_xor_sync(GB_FULL_MASK, mn, o), b = __shfl_xor_sync(GB_FULL_MASK, mx, o);
+    mn = a < mn ? a : mn;
+    mx = b > mx ? b : mx;
+  }
+  if (lane_id() == 0) {
+    red[warp_id()] = mn;
+    red[kWarps + warp_id()] = mx;
+  }
+  __syncthreads();
+  mn = red[0];
+  mx = red[kWarps];
+#pragma unroll
+  for (int i = 1; i < kWarps; ++i) {
+    mn = red[i] < mn ? red[i] : mn;
+    mx = red[kWarps + i] > mx ? red[kWarps + i] : mx;
+  }
+  __syncthreads();
+}
+
+// One MSD counting pass over positions [a, a+s) whose keys and indices are in
+// registers (warp-chunk order): stable by (key - mn) >> shift, written to
+// sm.key / sm.idx at [a, a+s); small bins are then insertion-sorted and large
+// bins queued for another pass.
+__device__ void local_msd_pass(LocalSmem& sm, uint32_t* scan_tmp, const uint64_t (&k)[kLocalRpt],
+                               const uint32_t (&ix)[kLocalRpt], uint32_t a, uint32_t s, uint64_t mn,
+                               uint64_t mx, uint32_t* stats) {
+  using Rank = BlockRank<kLocalRpt, kLocalBits>;
+  const uint32_t w = warp_id(), lane = lane_id();
+  const int bits = bitlen64(mx - mn);
+  const int shift = bits > kLocalBits ? bits - kLocalBits : 0;
+  uint32_t dig[kLocalRpt], pos[kLocalRpt];
+#pragma unroll
+  for (int r = 0; r < kLocalRpt; ++r) {
+    uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
+    dig[r] = e < s ? (uint32_t)((k[r] - mn) >> shift) : ((1u << kLocalBits) - 1);
+  }
+  Rank::rank(dig, pos, sm.hist, scan_tmp, sm.start);
+#pragma unroll
+  for (int r = 0; r < kLocalRpt; ++r) {
+    uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
+    if (e < s) {
+      sm.key[a + pos[r]] = k[r];
+      sm.idx[a + pos[r]] = (uint16_t)ix[r];
+    }
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < (1 << kLocalBits); d += kThreads) {
+    uint32_t b0 = sm.start[d], b1 = min(sm.start[d + 1], s);
+    if (b1 <= b0 + 1) continue;
+    uint32_t sz = b1 - b0;
+    if (sz <= (uint32_t)kInsertMax) {
+      uint64_t* key = sm.key + a + b0;
+      uint16_t* idx = sm.idx + a + b0;
+      for (uint32_t i = 1; i < sz; ++i) {
+        uint64_t kv = key[i];
+        uint16_t iv = idx[i];
+        uint32_t j = i;
+        while (j > 0 && key[j - 1] > kv) {
+          key[j] = key[j - 1];
+          idx[j] = idx[j - 1];
+          --j;
+        }
+        key[j] = kv;
+        idx[j] = iv;
+      }
+    } else {
+      uint32_t at = atomicAdd(&sm.nbig, 1u);
+      sm.big[at] = (uint16_t)(a + b0);
+      sm.bigsz[at] = (uint16_t)sz;
+    }
+  }
+  __syncthreads();
+}
+
+// Stable sort of `m` <= kLocalMax records of src by key into dst.
+template <int EW>
+__device__ void local_sort(EngineSmem& es, const uint8_t* src, uint8_t* dst, uint32_t m,
+                           const gbsort_key_word& kw, uint32_t* stats) {
+  LocalSmem& sm = es.loc;
+  constexpr uint32_t E = EW * 4;
+  const uint32_t w = warp_id(), lane = lane_id();
+  uint64_t k[kLocalRpt];
+  uint32_t ix[kLocalRpt];
+  uint64_t mn = ~0ull, mx = 0;
+#pragma unroll
+  for (int r = 0; r < kLocalRpt; ++r) {
+    uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
+    ix[r] = e;
+    if (e < m) {
+      k[r] = key_at(src, e, E, kw);
+      mn = k[r] < mn ? k[r] : mn;
+      mx = k[r] > mx ? k[r] : mx;
+    } else {
+      k[r] = 0;
+    }
+  }
+  if (threadIdx.x == 0) sm.nbig = 0;
+  block_minmax(mn, mx, sm.red);
+  if (mn == mx) {  // one key: the input order is the stable order
+    block_copy<EW>(src, dst, m);
+    return;
+  }
+  local_msd_pass(sm, es.scan_tmp, k, ix, 0, m, mn, mx, stats);
+  // further passes over bins too large for insertion sort
+  for (;;) {
+    uint32_t nb = sm.nbig;
+    __syncthreads();
+    if (nb == 0) break;
+    uint32_t a = sm.big[nb - 1], s = sm.bigsz[nb - 1];
+    __syncthreads();
+    if (threadIdx.x == 0) sm.nbig = nb - 1;
+    uint64_t bmn = ~0ull, bmx = 0;
+#pragma unroll
+    for (int r = 0; r < kLocalRpt; ++r) {
+      uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
+      if (e < s) {
+        k[r] = sm.key[a + e];
+        ix[r] = sm.idx[a + e];
+        bmn = k[r] < bmn ? k[r] : bmn;
+        bmx = k[r] > bmx ? k[r] : bmx;
+      }
+    }
+    block_minmax(bmn, bmx, sm.red);
+    if (bmn == bmx) continue;  // equal keys are already in input order
+    if (threadIdx.x == 0) atomicAdd(stats + STAT_BIGBIN, 1u);
+    local_msd_pass(sm, es.scan_tmp, k, ix, a, s, bmn, bmx, stats);
+  }
+  // gather the records into dst in sorted order
+  if constexpr (EW % 4 == 0) {
+    constexpr int V = EW / 4;
+    for (uint32_t f = threadIdx.x; f < m * V; f += kThreads) {
+      uint32_t i = f / V, v = f % V;
+      reinterpret_cast<uint4*>(dst + (size_t)i * E)[v] =
+          reinterpret_cast<const uint4*>(src + (size_t)sm.idx[i] * E)[v];
+    }
+  } else if constexpr (EW % 2 == 0) {
+    constexpr int V = EW / 2;
+    for (uint32_t f = threadIdx.x; f < m * V; f += kThreads) {
+      uint32_t i = f / V, v = f % V;
+      reinterpret_cast<uint2*>(dst + (size_t)i * E)[v] =
+          reinterpret_cast<const uint2*>(src + (size_t)sm.idx[i] * E)[v];
+    }
+  } else {
+    for (uint32_t f = threadIdx.x; f < m * EW; f += kThreads) {
+      uint32_t i = f / EW, v = f % EW;
+      reinterpret_cast<uint32_t*>(dst + (size_t)i * E)[v] =
+          reinterpret_cast<const uint32_t*>(src + (size_t)sm.idx[i] * E)[v];
+    }
+  }
+  __syncthreads();
+}
+
+// Split of one large bucket: 4096 bins of its key range, grouped into at most
+// 256 runs of consecutive bins, a stable scatter src -> other by group, then
+// a local sort (or a new task) per group.
+template <int EW>
+__device__ void split_task(EngineSmem& es, const HsortParams& p, const SortTask& task,
+                           SortTask* tasks_out, uint32_t* ntasks_out, uint32_t cap, uint32_t* stats,
+                           uint32_t* err) {
+  SplitSmem& sm = es.spl;
+  constexpr uint32_t E = EW * 4;
+  constexpr int RPT = Tile<EW>::kRpt, T = Tile<EW>::kSize;
+  using Rank = BlockRank<RPT, 8>;
+  const uint8_t* src = (task.src ? p.bufB : p.bufA) + (size_t)task.start * E;
+  uint8_t* oth = (task.src ? p.bufA : p.bufB) + (size_t)task.start * E;
+  uint8_t* out = p.out + (size_t)task.start * E;
+  const uint32_t m = task.count;
+  const int bits = bitlen64(task.hi - task.lo);
+  const int shift = bits > kSplitBits ? bits - kSplitBits : 0;
+  const uint32_t nbins = (uint32_t)((task.hi - task.lo) >> shift) + 1;
+  const uint32_t w = warp_id(), lane = lane_id();
+
+  for (int i = threadIdx.x; i < kSplitBins; i += kThreads) sm.hist[i] = 0;
+  __syncthreads();
+  for (uint32_t i0 = 0; i0 < m; i0 += kThreads) {
+    uint32_t i = i0 + threadIdx.x;
+    bool v = i < m;
+    uint32_t bin = 0xffffffffu;
+    if (v) {
+      uint64_t key = key_at(src, i, E, p.key);
+      uint64_t x = key > task.lo ? key - task.lo : 0;
+      bin = (uint32_t)min(x >> shift, (uint64_t)(nbins - 1));
+    }
+    uint32_t peers = __match_any_sync(GB_FULL_MASK, bin);
+    if (v && (peers & lanemask_lt()) == 0) atomicAdd(&sm.hist[bin], (uint32_t)__popc(peers));
+  }
+  __syncthreads();
+  // exclusive scan of the bins, then the group of every bin
+  {
+    constexpr int PER = kSplitBins / kThreads;
+    uint32_t loc[PER], s = 0;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      loc[i] = sm.hist[threadIdx.x * PER + i];
+      s += loc[i];
+    }
+    uint32_t pre = block_exclusive_scan<uint32_t>(s, es.scan_tmp, nullptr);
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      sm.hist[threadIdx.x * PER + i] = pre;
+      pre += loc[i];
+    }
+  }
+  __syncthreads();
+  uint32_t target = max((uint32_t)(kLocalMax / 2), (m + kMaxGroups - 1) / kMaxGroups);
+  for (uint32_t b = threadIdx.x; b < (uint32_t)kSplitBins; b += kThreads) {
+    uint32_t gb_ = b < nbins ? min(sm.hist[b] / target, (uint32_t)(kMaxGroups - 1)) : kMaxGroups - 1;
+    sm.gmap[b] = (uint8_t)gb_;
+  }
+  __syncthreads();
+  for (uint32_t b = threadIdx.x; b < nbins; b += kThreads) {
+    int gcur = sm.gmap[b];
+    int gprev = b ? (int)sm.gmap[b - 1] : -1;
+    for (int g = gprev + 1; g <= gcur; ++g) {
+      es.gstart[g] = sm.hist[b];
+      es.gfirst[g] = b;
+    }
+    if (b == nbins - 1) {
+      for (int g = gcur + 1; g <= kMaxGroups; ++g) {
+        es.gstart[g] = m;
+        es.gfirst[g] = nbins;
+      }
+    }
+  }
+  __syncthreads();
+  for (int g = threadIdx.x; g < kMaxGroups; g += kThreads) sm.cursor[g] = es.gstart[g];
+  __syncthreads();
+  // stable scatter src -> other by group
+  for (uint32_t t0 = 0; t0 < m; t0 += T) {
+    const uint32_t nvalid = min((uint32_t)T, m - t0);
+    uint32_t rec[RPT][EW];
+    uint32_t dig[RPT], pos[RPT];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+      uint32_t e = w * 32 * RPT + r * 32 + lane;
+      if (e < nvalid) {
+        RecIO<EW>::load(src + (size_t)(t0 + e) * E, rec[r]);
+        uint64_t key = key_from_regs<EW>(rec[r], p.key);
+        uint64_t x = key > task.lo ? key - task.lo : 0;
+        uint32_t bin = (uint32_t)min(x >> shift, (uint64_t)(nbins - 1));
+        dig[r] = sm.gmap[bin];
+      } else {
+        dig[r] = kMaxGroups - 1;
+      }
+    }
+    Rank::rank(dig, pos, sm.rhist, es.scan_tmp, sm.dstart);
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+      uint32_t e = w * 32 * RPT + r * 32 + lane;
+      if (e < nvalid) {
+        uint32_t d = dig[r];
+        uint32_t dest = sm.cursor[d] + pos[r] - sm.dstart[d];
+        if (dest < m) RecIO<EW>::store(oth + (size_t)dest * E, rec[r]);
+        else set_error(err, DEV_ERR_COUNT_MISMATCH);
+      }
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kMaxGroups; d += kThreads) {
+      uint32_t cnt = sm.dstart[d + 1] - sm.dstart[d];
+      if (d == kMaxGroups - 1) cnt -= (uint32_t)T - nvalid;
+      sm.cursor[d] += cnt;
+    }
+    __syncthreads();
+  }
+  __threadfence_block();
+  // per group: local sort, copy, or a new task for the next round
+  for (int g = 0; g < kMaxGroups; ++g) {
+    const uint32_t g0 = es.gstart[g], g1 = es.gstart[g + 1];
+    const uint32_t b0 = es.gfirst[g], b1 = es.gfirst[g + 1];
+    __syncthreads();
+    if (g1 == g0) continue;
+    const uint32_t s = g1 - g0;
+    uint64_t glo = task.lo + ((uint64_t)b0 << shift);
+    uint64_t ghi = b1 >= nbins ? task.hi : task.lo + ((uint64_t)b1 << shift) - 1;
+    if (glo == ghi || s == 1) {
+      if (s <= kCopyPiece) {
+        block_copy<EW>(oth + (size_t)g0 * E, out + (size_t)g0 * E, s);
+        __syncthreads();
+      } else if (threadIdx.x == 0) {
+        uint32_t pieces = (s + kCopyPiece - 1) / kCopyPiece;
+        uint32_t at = atomicAdd(ntasks_out, pieces);
+        if (at + pieces > cap) set_error(err, DEV_ERR_TASK_OVERFLOW);
+        else
+          for (uint32_t i = 0; i < pieces; ++i) {
+            uint32_t s0 = i * kCopyPiece;
+            tasks_out[at + i] = SortTask{task.start + g0 + s0, min(kCopyPiece, s - s0), glo, ghi,
+                                         task.src ^ 1u, TASK_COPY};
+          }
+      }
+    } else if (s <= (uint32_t)kLocalMax) {
+      local_sort<EW>(es, oth + (size_t)g0 * E, out + (size_t)g0 * E, s, p.key, stats);
+      if (threadIdx.x == 0) atomicAdd(stats + STAT_LOCAL, 1u);
+    } else if (threadIdx.x == 0) {
+      uint32_t at = atomicAdd(ntasks_out, 1u);
+      atomicAdd(stats + STAT_PUSHED, 1u);
+      if (at >= cap) set_error(err, DEV_ERR_TASK_OVERFLOW);
+      else tasks_out[at] = SortTask{task.start + g0, s, glo, ghi, task.src ^ 1u, TASK_SORT};
+    }
+  }
+  __syncthreads();
+}
+
+template <int EW>
+__global__ void __launch_bounds__(kThreads, 1) k_tasks(HsortParams p, const SortTask* __restrict__ tasks_in,
+                                                        const uint32_t* __restrict__ ntasks_in,
+                                                        SortTask* __restrict__ tasks_out,
+                                                        uint32_t* __restrict__ ntasks_out, uint32_t cap,
+                                                        uint32_t* __restrict__ work,
+                                                        uint32_t* __restrict__ stats,
+                                                        uint32_t* __restrict__ err) {
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  EngineSmem& es = *reinterpret_cast<EngineSmem*>(smem_raw);
+  constexpr uint32_t E = EW * 4;
+  const uint32_t nt = min(*ntasks_in, cap);
+  for (;;) {
+    if (threadIdx.x == 0) es.task_id = atomicAdd(work, 1u);
+    __syncthreads();
+    const uint32_t t = es.task_id;
+    __syncthreads();
+    if (t >= nt) break;
+    const SortTask task = tasks_in[t];
+    const uint8_t* src = (task.src ? p.bufB : p.bufA) + (size_t)task.start * E;
+    uint8_t* out = p.out + (size_t)task.start * E;
+    if (task.kind == TASK_COPY || task.count == 1) {
+      block_copy<EW>(src, out, task.count);
+      if (threadIdx.x == 0) atomicAdd(stats + STAT_COPY, 1u);
+    } else if (task.count <= (uint32_t)kLocalMax) {
+      local_sort<EW>(es, src, out, task.count, p.key, stats);
+      if (threadIdx.x == 0) atomicAdd(stats + STAT_LOCAL, 1u);
+    } else {
+      if (threadIdx.x == 0) atomicAdd(stats + STAT_SPLIT, 1u);
+      split_task<EW>(es, p, task, tasks_out, ntasks_out, cap, stats, err);
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ dispatch --
+template <typename F>
+bool dispatch_ew(uint32_t elsize, F&& f) {
+  switch (elsize / 4) {
+    case 2: f(std::integral_constant<int, 2>()); return true;
+    case 3: f(std::integral_constant<int, 3>()); return true;
+    case 4: f(std::integral_constant<int, 4>()); return true;
+    case 6: f(std::integral_constant<int, 6>()); return true;
+    case 8: f(std::integral_constant<int, 8>()); return true;
+    case 10: f(std::integral_constant<int, 10>()); return true;
+    case 12: f(std::integral_constant<int, 12>()); return true;
+    case 16: f(std::integral_constant<int, 16>()); return true;
+    default: return false;
+  }
+}
+
+}  // namespace
+
+bool hsort_supported(uint32_t elsize) {
+  if (elsize % 4) return false;
+  switch (elsize / 4) {
+    case 2: case 3: case 4: case 6: case 8: case 10: case 12: case 16: return true;
+    default: return false;
+  }
+}
+
+int hsort_grid(uint32_t n) {
+  int g = num_sms();
+  uint64_t maxg = ((uint64_t)n + 4095) / 4096;
+  if ((uint64_t)g > maxg) g = (int)(maxg < 1 ? 1 : maxg);
+  return g;
+}
+
+int task_engine_grid() { return num_sms(); }
+
+cudaError_t sample_keys(const uint8_t* rec, uint32_t n, uint32_t elsize, gbsort_key_word key, uint32_t s,
+                        uint64_t* out, cudaStream_t stream) {
+  if (s == 0) return cudaSuccess;
+  unsigned blocks = (s + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  k_sample<<<blocks, 256, 0, stream>>>(rec, n, elsize, key, s, out);
+  return cudaGetLastError();
+}
+
+cudaError_t plain_splitters(const uint64_t* sorted_sample, uint32_t s, int nsplit, uint64_t* splitters,
+                            uint32_t* iters, int64_t* clt, int64_t* cle, cudaStream_t stream) {
+  if (nsplit <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(iters, 0, sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return e;
+  k_plain_splitters<<<(nsplit + 127) / 128, 128, 0, stream>>>(sorted_sample, s, nsplit, splitters, iters,
+                                                               clt, cle);
+  return cudaGetLastError();
+}
+
+cudaError_t finalize_splitters(uint64_t* splitters, int nsplit, cudaStream_t stream) {
+  if (nsplit <= 1) return cudaSuccess;
+  if (nsplit > 8192) return cudaErrorInvalidValue;
+  k_finalize_splitters<<<1, 1024, 0, stream>>>(splitters, nsplit);
+  return cudaGetLastError();
+}
+
+static cudaError_t set_smem(const void* fn, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+cudaError_t l1_count(const HsortParams& p, int lookup_kind, const uint64_t* splitters, int nbuckets,
+                     const void* model, uint32_t* counts, uint32_t* stats, cudaStream_t stream) {
+  const ModelDev m = model ? *(const ModelDev*)model : ModelDev{};
+  const int g = hsort_grid(p.n);
+  cudaError_t e;
+  if (lookup_kind == LOOKUP_LEARNED) {
+    size_t sm = lookup_smem_bytes<LOOKUP_LEARNED>(nbuckets, &m) + 4 * (size_t)nbuckets;
+    if ((e = set_smem((const void*)k_l1_count<LOOKUP_LEARNED>, sm)) != cudaSuccess) return e;
+    k_l1_count<LOOKUP_LEARNED><<<g, kThreads, sm, stream>>>(p, splitters, nbuckets, m, counts, stats);
+  } else {
+    size_t sm = lookup_smem_bytes<LOOKUP_PLAIN>(nbuckets, &m) + 4 * (size_t)nbuckets;
+    if ((e = set_smem((const void*)k_l1_count<LOOKUP_PLAIN>, sm)) != cudaSuccess) return e;
+    k_l1_count<LOOKUP_PLAIN><<<g, kThreads, sm, stream>>>(p, splitters, nbuckets, m, counts, stats);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t l1_scatter(const HsortParams& p, int lookup_kind, const uint64_t* splitters, int nbuckets,
+                       const void* model, const uint32_t* offsets, uint32_t* stats, cudaStream_t stream) {
+  const ModelDev m = model ? *(const ModelDev*)model : ModelDev{};
+  const int g = hsort_grid(p.n);
+  cudaError_t e = cudaSuccess;
+  bool ok = dispatch_ew(p.elsize, [&](auto ewc) {
+    constexpr int EW = decltype(ewc)::value;
+    if (lookup_kind == LOOKUP_LEARNED) {
+      size_t sm = l1_scatter_smem<EW, LOOKUP_LEARNED>(nbuckets, &m);
+      e = set_smem((const void*)k_l1_scatter<EW, LOOKUP_LEARNED>, sm);
+      if (e == cudaSuccess)
+        k_l1_scatter<EW, LOOKUP_LEARNED><<<g, kThreads, sm, stream>>>(p, splitters, nbuckets, m, offsets,
+                                                                       stats);
+    } else {
+      size_t sm = l1_scatter_smem<EW, LOOKUP_PLAIN>(nbuckets, &m);
+      e = set_smem((const void*)k_l1_scatter<EW, LOOKUP_PLAIN>, sm);
+      if (e == cudaSuccess)
+        k_l1_scatter<EW, LOOKUP_PLAIN><<<g, kThreads, sm, stream>>>(p, splitters, nbuckets, m, offsets,
+                                                                     stats);
+    }
+  });
+  if (!ok) return cudaErrorInvalidValue;
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+cudaError_t build_tasks(const uint32_t* offsets, int grid, const uint64_t* splitters, int nbuckets,
+                        uint32_t n, SortTask* tasks, uint32_t* ntasks, uint32_t cap, uint32_t* err,
+                        uint32_t* stats, cudaStream_t stream) {
+  k_build_tasks<<<(nbuckets + 255) / 256, 256, 0, stream>>>(offsets, grid, splitters, nbuckets, n, tasks,
+                                                            ntasks, cap, err, stats);
+  return cudaGetLastError();
+}
+
+
+cudaError_t run_tasks(const HsortParams& p, const SortTask* tasks_in, const uint32_t* ntasks_in,
+                      SortTask* tasks_out, uint32_t* ntasks_out, uint32_t cap, uint32_t* work_counter,
+                      uint32_t* stats, uint32_t* err, cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return e;
+  bool ok = dispatch_ew(p.elsize, [&](auto ewc) {
+    constexpr int EW = decltype(ewc)::value;
+    size_t sm = sizeof(EngineSmem);
+    e = set_smem((const void*)k_tasks<EW>, sm);
+    if (e == cudaSuccess)
+      k_tasks<EW><<<task_engine_grid(), kThreads, sm, stream>>>(p, tasks_in, ntasks_in, tasks_out, ntasks_out,
+                                                                 cap, work_counter, stats, err);
+  });
+  if (!ok) return cudaErrorInvalidValue;
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+}  // namespace gb

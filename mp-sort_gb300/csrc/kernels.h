@@ -1,0 +1,111 @@
+// kernels.h -- host-side launch wrappers for the gbsort kernels.
+//
+// Every wrapper enqueues work on `stream` and returns the launch's
+// cudaError_t; none of them synchronises.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/gbsort_key.h"
+
+namespace gb {
+
+// ---- scan.cu --------------------------------------------------------------
+// Exclusive prefix sum of n uint32 values (n <= 2^24); `tmp` needs
+// scan_tmp_words(n) words.  out may alias in.
+size_t scan_tmp_words(size_t n);
+cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n, uint32_t* tmp,
+                               cudaStream_t stream);
+
+// ---- lsd.cu: the generic path (any key width, any record size) -------------
+// Key words of every record into word-major arrays keys[w * n + i], and the
+// identity permutation into idx (if not null).
+cudaError_t extract_keys(const void* rec, uint32_t n, uint32_t elsize, const gbsort_key_desc& key,
+                         uint64_t* keys, uint32_t* idx, cudaStream_t stream);
+// rsize little-endian radix bytes per record (from a host radix() callback)
+// into nwords = ceil(rsize / 8) key words.
+cudaError_t radix_bytes_to_keys(const uint8_t* radix, uint32_t n, uint32_t rsize, uint64_t* keys,
+                                uint32_t* idx, cudaStream_t stream);
+// 256-bin histograms of all 8 * nwords digits in one read ([digit][256]).
+cudaError_t lsd_digit_histograms(const uint64_t* keys, uint32_t n, int nwords, uint32_t* hist,
+                                 cudaStream_t stream);
+// Grid size used by lsd_count / lsd_scatter.
+int lsd_grid(uint32_t n);
+// One LSD pass on digit (word, shift): per-chunk counts, then stable scatter
+// of all key words (and idx, if not null) using offsets = exclusive scan of
+// counts ([256][grid]).
+cudaError_t lsd_count(const uint64_t* keys_word, uint32_t n, int shift, uint32_t* counts,
+                      cudaStream_t stream);
+cudaError_t lsd_scatter(const uint64_t* keys_in, const uint32_t* idx_in, uint64_t* keys_out,
+                        uint32_t* idx_out, uint32_t n, int nwords, int word, int shift,
+                        const uint32_t* offsets, cudaStream_t stream);
+// out[i] = in[idx[i]] for records of elsize bytes.
+cudaError_t gather_records(const void* in, void* out, const uint32_t* idx, uint32_t n,
+                           uint32_t elsize, cudaStream_t stream);
+
+// ---- hsort.cu: the histogram sort ----------------------------------------
+// Device statistics slots filled by the histogram sort.
+enum StatSlot : int {
+  STAT_LOCAL = 0,        // shared-memory local sorts
+  STAT_SPLIT = 1,        // bucket splits
+  STAT_COPY = 2,         // single-key copy tasks
+  STAT_PUSHED = 3,       // sub-buckets re-split in a further round
+  STAT_BIGBIN = 4,       // extra local MSD passes on clustered bins
+  STAT_WINDOW_MISS = 5,  // learned lookups whose window missed (full search ran)
+  STAT_MAX_BUCKET = 6,   // largest level-1 bucket
+  STAT_SLOTS = 8
+};
+
+enum Lookup : int { LOOKUP_PLAIN = 0, LOOKUP_LEARNED = 1 };
+
+struct SortTask {        // one bucket or sub-bucket of the level-2 task engine
+  uint32_t start;        // first record (same index in every buffer)
+  uint32_t count;        // records
+  uint64_t lo, hi;       // key range [lo, hi] of the records
+  uint32_t src;          // 0: scratch A, 1: scratch B
+  uint32_t kind;         // TASK_* below
+};
+enum TaskKind : uint32_t { TASK_SORT = 0, TASK_COPY = 1 };
+
+struct HsortParams {
+  const uint8_t* in;
+  uint8_t* out;
+  uint8_t* bufA;
+  uint8_t* bufB;
+  uint32_t n;
+  uint32_t elsize;
+  gbsort_key_word key;
+};
+
+bool hsort_supported(uint32_t elsize);
+int hsort_grid(uint32_t n);
+cudaError_t sample_keys(const uint8_t* rec, uint32_t n, uint32_t elsize, gbsort_key_word key,
+                        uint32_t s, uint64_t* out, cudaStream_t stream);
+// Plain splitter search: for every splitter, the reference's bisection over
+// the sorted sample (internal-parallel.h piter_* with CLT < C <= CLE), then
+// equal runs turned into single-key buckets.
+cudaError_t plain_splitters(const uint64_t* sorted_sample, uint32_t s, int nsplit,
+                            uint64_t* splitters, uint32_t* iters, int64_t* clt, int64_t* cle,
+                            cudaStream_t stream);
+cudaError_t finalize_splitters(uint64_t* splitters, int nsplit, cudaStream_t stream);
+// Level-1 bucket counts per chunk ([nbuckets][grid]) and the stable scatter.
+// `model` points to a host copy of the ModelDev (cdf.cuh) for the learned
+// lookup, else null.  `stats` is the device statistics array (Stat indices).
+cudaError_t l1_count(const HsortParams& p, int lookup, const uint64_t* splitters, int nbuckets,
+                     const void* model, uint32_t* counts, uint32_t* stats, cudaStream_t stream);
+cudaError_t l1_scatter(const HsortParams& p, int lookup, const uint64_t* splitters, int nbuckets,
+                       const void* model, const uint32_t* offsets, uint32_t* stats, cudaStream_t stream);
+// Level-2 tasks from the level-1 buckets.
+cudaError_t build_tasks(const uint32_t* offsets, int grid, const uint64_t* splitters, int nbuckets,
+                        uint32_t n, SortTask* tasks, uint32_t* ntasks, uint32_t cap,
+                        uint32_t* err, uint32_t* stats, cudaStream_t stream);
+// One round of the persistent task engine: consumes tasks_in, appends
+// oversize sub-buckets to tasks_out.
+int task_engine_grid();
+cudaError_t run_tasks(const HsortParams& p, const SortTask* tasks_in, const uint32_t* ntasks_in,
+                      SortTask* tasks_out, uint32_t* ntasks_out, uint32_t cap, uint32_t* work_counter,
+                      uint32_t* stats, uint32_t* err, cudaStream_t stream);
+
+}  // namespace gb

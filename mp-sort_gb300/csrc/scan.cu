@@ -1,0 +1,85 @@
+// scan.cu -- exclusive prefix sum of uint32 counts (reduce, then scan).
+//
+// Used for the (bucket x chunk) count matrices of the histogram sort and the
+// (digit x chunk) matrices of the LSD passes: the device counterpart of the
+// reference's count reductions (mpsort-omp.c:110-121) and displacement
+// arithmetic (mpsort-mpi.c:483-510).
+#include "common.cuh"
+#include "kernels.h"
+
+namespace gb {
+
+namespace {
+
+constexpr int kSeg = 4096;  // elements per segment (8 per thread)
+constexpr int kPer = kSeg / kThreads;
+
+__global__ void __launch_bounds__(kThreads) k_segment_sums(const uint32_t* __restrict__ in, size_t n,
+                                                            uint32_t* __restrict__ sums) {
+  __shared__ uint32_t tmp[kWarps];
+  size_t base = (size_t)blockIdx.x * kSeg;
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < kPer; ++i) {
+    size_t j = base + (size_t)i * kThreads + threadIdx.x;
+    if (j < n) s += in[j];
+  }
+  uint32_t total;
+  block_exclusive_scan<uint32_t>(s, tmp, &total);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// Scans the segment sums in place (one block; nseg <= kSeg).
+__global__ void __launch_bounds__(kThreads) k_scan_sums(uint32_t* sums, int nseg) {
+  __shared__ uint32_t tmp[kWarps];
+  uint32_t v[kPer];
+  uint32_t s = 0;
+  const int base = threadIdx.x * kPer;
+#pragma unroll
+  for (int i = 0; i < kPer; ++i) {
+    v[i] = (base + i < nseg) ? sums[base + i] : 0u;
+    s += v[i];
+  }
+  uint32_t pre = block_exclusive_scan<uint32_t>(s, tmp, nullptr);
+#pragma unroll
+  for (int i = 0; i < kPer; ++i) {
+    if (base + i < nseg) sums[base + i] = pre;
+    pre += v[i];
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_segment_scan(const uint32_t* in, uint32_t* out, size_t n,
+                                                            const uint32_t* __restrict__ seg_base) {
+  __shared__ uint32_t tmp[kWarps];
+  size_t base = (size_t)blockIdx.x * kSeg + (size_t)threadIdx.x * kPer;
+  uint32_t v[kPer];
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < kPer; ++i) {
+    v[i] = (base + i < n) ? in[base + i] : 0u;
+    s += v[i];
+  }
+  uint32_t pre = block_exclusive_scan<uint32_t>(s, tmp, nullptr) + seg_base[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < kPer; ++i) {
+    if (base + i < n) out[base + i] = pre;
+    pre += v[i];
+  }
+}
+
+}  // namespace
+
+size_t scan_tmp_words(size_t n) { return (n + kSeg - 1) / kSeg + 1; }
+
+cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n, uint32_t* tmp,
+                               cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  size_t nseg = (n + kSeg - 1) / kSeg;
+  if (nseg > (size_t)kSeg) return cudaErrorInvalidValue;
+  k_segment_sums<<<(unsigned)nseg, kThreads, 0, stream>>>(in, n, tmp);
+  k_scan_sums<<<1, kThreads, 0, stream>>>(tmp, (int)nseg);
+  k_segment_scan<<<(unsigned)nseg, kThreads, 0, stream>>>(in, out, n, tmp);
+  return cudaGetLastError();
+}
+
+}  // namespace gb

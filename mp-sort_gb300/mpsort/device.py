@@ -1,0 +1,93 @@
+"""Device-memory entry points for records already in GPU memory.
+
+Pointers are plain integers (e.g. ``torch.Tensor.data_ptr()``) and streams
+are ``cudaStream_t`` values as integers (e.g. ``torch.cuda.Stream.cuda_stream``);
+0 selects the library's own stream.  Every call returns once the work is
+enqueued on that stream.
+"""
+import ctypes
+
+import numpy
+
+from . import _lib
+
+
+def _desc(dtype, orderby):
+    return _lib.key_desc(dtype, orderby)
+
+
+def sort(d_in, d_out, n, dtype, orderby, method="auto", stream=0):
+    """Sort n records of `dtype` from d_in into d_out by field `orderby`."""
+    dtype = numpy.dtype(dtype)
+    desc = _desc(dtype, orderby)
+    _lib.check(_lib.lib().gbsort_sort_device(d_in, d_out, n, dtype.itemsize, ctypes.byref(desc),
+                                             _lib.METHODS[method], stream or None))
+
+
+def sort_segments(d_in, d_out, offsets, dtype, orderby, method="auto", stream=0):
+    """Sort every segment [offsets[i], offsets[i+1]) of d_in independently."""
+    dtype = numpy.dtype(dtype)
+    desc = _desc(dtype, orderby)
+    offs = numpy.ascontiguousarray(offsets, dtype=numpy.uint64)
+    _lib.check(_lib.lib().gbsort_sort_segments_device(d_in, d_out, offs.ctypes.data, len(offs) - 1,
+                                                      dtype.itemsize, ctypes.byref(desc),
+                                                      _lib.METHODS[method], stream or None))
+
+
+def merge_join(d_a, na, d_b, nb, dtype, orderby, d_pairs_a, d_pairs_b, d_npairs, stream=0):
+    """Index pairs of equal keys of two key-sorted arrays (unique keys per side)."""
+    dtype = numpy.dtype(dtype)
+    desc = _desc(dtype, orderby)
+    _lib.check(_lib.lib().gbsort_merge_join_device(d_a, na, d_b, nb, dtype.itemsize, ctypes.byref(desc),
+                                                   d_pairs_a, d_pairs_b, d_npairs, stream or None))
+
+
+def sort_host(a, orderby, out=None, method="auto"):
+    """Host-array sort through the device pipeline (numpy in, numpy out)."""
+    a = numpy.ascontiguousarray(a)
+    if out is None:
+        out = numpy.empty_like(a)
+    desc = _desc(a.dtype, orderby)
+    if len(a):
+        _lib.check(_lib.lib().gbsort_sort_host(a.ctypes.data, out.ctypes.data, len(a), a.dtype.itemsize,
+                                               ctypes.byref(desc), _lib.METHODS[method]))
+    return out
+
+
+def cdf_forward_backward(x, kmin, kmax, lbits, y):
+    """Loss, predictions and knot gradient of the learned CDF on sorted keys x."""
+    x = numpy.ascontiguousarray(x, dtype=numpy.uint64)
+    y = numpy.ascontiguousarray(y, dtype=numpy.float32)
+    loss = numpy.zeros(1, numpy.float32)
+    pred = numpy.zeros(len(x), numpy.float32)
+    grad = numpy.zeros(len(y), numpy.float32)
+    _lib.check(_lib.lib().gbsort_cdf_forward_backward(x.ctypes.data, len(x), int(kmin), int(kmax), int(lbits),
+                                                      y.ctypes.data, loss.ctypes.data, pred.ctypes.data,
+                                                      grad.ctypes.data))
+    return float(loss[0]), pred, grad
+
+
+def debug_buckets(sample, nbuckets, keys):
+    """(full-search buckets, learned buckets, splitters, widest window)."""
+    sample = numpy.ascontiguousarray(sample, dtype=numpy.uint64)
+    keys = numpy.ascontiguousarray(keys, dtype=numpy.uint64)
+    bs = numpy.zeros(len(keys), numpy.uint32)
+    bl = numpy.zeros(len(keys), numpy.uint32)
+    S = numpy.zeros(nbuckets - 1, numpy.uint64)
+    w = ctypes.c_uint32(0)
+    _lib.check(_lib.lib().gbsort_debug_buckets(sample.ctypes.data, len(sample), nbuckets, keys.ctypes.data,
+                                               len(keys), bs.ctypes.data, bl.ctypes.data, S.ctypes.data,
+                                               ctypes.byref(w)))
+    return bs, bl, S, w.value
+
+
+def debug_bisect(sorted_keys, nsplit):
+    """(splitters, CLT, CLE, rounds) of the device bisection splitter search."""
+    x = numpy.ascontiguousarray(sorted_keys, dtype=numpy.uint64)
+    S = numpy.zeros(nsplit, numpy.uint64)
+    clt = numpy.zeros(nsplit, numpy.int64)
+    cle = numpy.zeros(nsplit, numpy.int64)
+    r = ctypes.c_uint32(0)
+    _lib.check(_lib.lib().gbsort_debug_bisect(x.ctypes.data, len(x), nsplit, S.ctypes.data, clt.ctypes.data,
+                                              cle.ctypes.data, ctypes.byref(r)))
+    return S, clt, cle, r.value

@@ -1,0 +1,416 @@
+"""GPU parity: the CUDA sort against the oracle and the reference's vectors.
+
+Every comparison is bit-exact on whole records: the reference's output is
+the stable order by radix (stdlib/msort.c keeps ties in input order), so
+the expected result is unique.
+"""
+import ctypes
+
+import numpy
+import pytest
+
+import oracle as O
+from conftest import golden_cases
+
+pytestmark = pytest.mark.gpu
+
+METHODS = ["plain", "learned", "lsd"]
+
+
+@pytest.fixture(scope="module")
+def mp():
+    import __graft_entry__ as g
+    g.build()
+    import mpsort
+    if mpsort._lib.lib().gbsort_device_count() < 1:
+        pytest.fail("no CUDA device visible to libgbsort")
+    return mpsort
+
+
+def check(mp, arr, orderby, method):
+    out = numpy.empty_like(arr)
+    mp.sort(arr, orderby, out=out, method=method)
+    exp = O.numpy_sorted(arr, orderby)
+    assert out.tobytes() == exp.tobytes(), (arr.dtype, len(arr), method)
+    return out
+
+
+# ------------------------------------------------------------- golden --
+@pytest.mark.parametrize("method", ["auto"] + METHODS)
+def test_golden_vectors(mp, golden, method):
+    for name, arr, out, orderby in golden_cases(golden):
+        res = numpy.empty_like(arr)
+        try:
+            mp.sort(arr, orderby, out=res, method=method)
+        except mp.GBSortError as e:
+            assert e.status == 6 and method in ("plain", "learned"), (name, e)  # unsupported layout
+            continue
+        assert res.tobytes() == out.tobytes(), (name, method)
+
+
+def test_golden_callbacks_through_dropin_symbols(mp, golden):
+    """radix_sort / mpsort_omp with the reference tests' own radix() callbacks."""
+    L = mp._lib.lib()
+    olib = O.oracle_lib()
+    for fn, sym in ((L.radix_sort, "radix_sort"), (L.mpsort_omp, "mpsort_omp")):
+        ints = golden["cb_int__in"].copy()
+        fn(ints.ctypes.data, len(ints), 4, ctypes.cast(olib.ref_radix_int, ctypes.c_void_p), 4, None)
+        assert L.mpsort_last_status() == 0, sym
+        assert ints.tobytes() == golden["cb_int__out"].tobytes(), sym
+        recs = golden["cb_issue7__in"].copy()
+        fn(recs.ctypes.data, len(recs), 40, ctypes.cast(olib.ref_radix_issue7, ctypes.c_void_p), 16, None)
+        assert recs.tobytes() == golden["cb_issue7__out"].tobytes(), sym
+
+
+def test_dropin_with_key_descriptor(mp, golden):
+    L = mp._lib.lib()
+    arr = golden["cfg1_4096__in"].copy()
+    d = mp._lib.key_desc(arr.dtype, 'key')
+    L.mpsort_omp(arr.ctypes.data, len(arr), arr.dtype.itemsize,
+                 ctypes.cast(L.mpsort_radix_desc, ctypes.c_void_p), 8, ctypes.byref(d))
+    assert L.mpsort_last_status() == 0
+    assert arr.tobytes() == golden["cfg1_4096__out"].tobytes()
+
+
+def test_reference_build_live(mp):
+    """Against the unmodified reference mpsort_omp where it was built."""
+    if O.ref_lib() is None:
+        pytest.skip("reference build absent")
+    rng = numpy.random.default_rng(0)
+    a = numpy.empty(300_000, dtype=[('key', 'u8'), ('value', 'f4')])
+    a['key'] = rng.integers(0, 2**64, len(a), dtype=numpy.uint64, endpoint=False)
+    a['value'] = numpy.arange(len(a), dtype=numpy.float32)
+    exp = O.ref_sort(a, 'key', 'omp')
+    for m in METHODS:
+        out = numpy.empty_like(a)
+        mp.sort(a, 'key', out=out, method=m)
+        assert out.tobytes() == exp.tobytes(), m
+
+
+# --------------------------------------------------- edges and layouts --
+SIZES = [1, 2, 3, 31, 32, 33, 511, 4095, 4096, 4097, 8193, 65537, 300_001]
+
+
+def make(dtype, key, n, dist, rng):
+    a = numpy.zeros(n, dtype=dtype)
+    kd = a[key].dtype
+    info = numpy.iinfo(kd)
+    if dist == "uniform":
+        k = rng.integers(info.min, info.max, n, dtype=kd, endpoint=True)
+    elif dist == "dups":
+        k = rng.integers(-3, 4, n).astype(kd) if info.min < 0 else rng.integers(0, 7, n).astype(kd)
+    elif dist == "equal":
+        k = numpy.full(n, 5, dtype=kd)
+    elif dist == "sorted":
+        k = numpy.arange(n).astype(kd)
+    elif dist == "reversed":
+        k = numpy.arange(n)[::-1].astype(kd)
+    elif dist == "zipf":
+        vals = rng.integers(info.min, info.max, 1000, dtype=kd, endpoint=True)
+        k = vals[numpy.minimum(rng.zipf(1.2, n) - 1, 999)]
+    elif dist == "extremes":
+        k = rng.choice(numpy.array([info.min, info.max, 0, 1, info.max - 1], dtype=kd), n)
+    a[key] = k
+    for f in a.dtype.names:
+        if f != key and a[f].dtype.kind in "iu" and a[f].ndim == 1:
+            a[f] = numpy.arange(n) % numpy.iinfo(a[f].dtype).max
+    return a
+
+
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("n", SIZES)
+def test_sizes_u8_16B(mp, n, method):
+    rng = numpy.random.default_rng(n)
+    for dist in ("uniform", "dups", "sorted", "reversed"):
+        check(mp, make([('key', 'u8'), ('val', 'i8')], 'key', n, dist, rng), 'key', method)
+
+
+LAYOUTS = [
+    ([('key', 'i4'), ('payload', 'u4')], 'key'),                    # 8 B, signed 32-bit
+    ([('key', 'u8'), ('value', 'f4')], 'key'),                      # 12 B packed
+    ([('id', 'i8'), ('mass', 'f4'), ('halo', 'i4')], 'id'),         # 16 B, signed 64-bit
+    ([('a', 'u4'), ('key', 'u4'), ('b', 'u8'), ('c', 'u8')], 'key'),  # 24 B, key at offset 4
+    ([('pos', ('f4', 3)), ('vel', ('f4', 3)), ('id', 'u8'), ('key', 'u8')], 'key'),  # 40 B
+    ([('k', 'i8'), ('pad', ('u8', 7))], 'k'),                       # 64 B
+    ([('key', 'u8'), ('x', 'u4'), ('y', 'u4'), ('z', 'u4'), ('w', 'u4')], 'key'),  # 24 B
+]
+
+
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("layout", range(len(LAYOUTS)))
+def test_layouts_and_distributions(mp, layout, method):
+    dtype, key = LAYOUTS[layout]
+    rng = numpy.random.default_rng(layout)
+    for n in (5000, 200_003):
+        for dist in ("uniform", "dups", "equal", "zipf", "extremes", "sorted"):
+            check(mp, make(dtype, key, n, dist, rng), key, method)
+
+
+@pytest.mark.parametrize("n", [17, 5000, 70_001])
+def test_generic_path_layouts(mp, n):
+    """Records the histogram sort does not take: odd sizes, unaligned keys,
+    multi-word keys.  AUTO routes them to the LSD path."""
+    rng = numpy.random.default_rng(n)
+    cases = [
+        (numpy.dtype([('c', 'u1'), ('key', 'i4')]), 'key'),         # 5 B, key at offset 1
+        (numpy.dtype([('key', 'u8'), ('c', 'u1')]), 'key'),         # 9 B
+        (numpy.dtype([('v', ('u8', 3)), ('w', 'u4')]), 'v'),        # 3-word key
+        (numpy.dtype([('v', ('i4', 2)), ('w', 'u1')]), 'v'),        # 2 x i4, 9 B
+        (numpy.dtype([('v', ('i8', 4))]), 'v'),                     # 4-word key
+    ]
+    for dt, key in cases:
+        a = numpy.zeros(n, dt)
+        f = a[key]
+        info = numpy.iinfo(f.dtype)
+        a[key] = rng.integers(max(info.min, -20), min(info.max, 20), f.shape)
+        check(mp, a, key, "auto")
+
+
+def test_in_place_and_aliasing(mp):
+    rng = numpy.random.default_rng(9)
+    for m in METHODS:
+        a = make([('key', 'i8'), ('v', 'i8')], 'key', 100_000, "dups", rng)
+        exp = O.numpy_sorted(a, 'key')
+        mp.sort(a, 'key', method=m)
+        assert a.tobytes() == exp.tobytes(), m
+
+
+# ------------------------------------------- ports of test_mpsort.py --
+def test_sort_i4_i8_u8_u4(mp):
+    s = numpy.int32(numpy.random.random(size=1000) * 1000 - 400)
+    r = s.copy()
+    mp.sort(r, orderby=None, out=None)
+    assert (r == numpy.sort(s)).all()
+    s = numpy.int64(numpy.random.random(size=1000) * 1000 - 400)
+    r = s.copy()
+    mp.sort(r)
+    assert (r == numpy.sort(s)).all()
+    s = numpy.uint64(numpy.random.uniform(size=1000, low=-1000000, high=1000000) * 1000 - 400)
+    r = s.copy()
+    mp.sort(r)
+    assert (r == numpy.sort(s)).all()
+    s = numpy.uint32(numpy.random.random(size=1000) * 1000 - 400)
+    r = s.copy()
+    mp.sort(r)
+    assert (r == numpy.sort(s)).all()
+
+
+@pytest.mark.parametrize("tuning", [[], ['DISABLE_SPARSE_ALLTOALLV'], ['REQUIRE_SPARSE_ALLTOALLV'],
+                                    ['REQUIRE_GATHER_SORT'], ['DISABLE_GATHER_SORT']])
+def test_sort_tunings(mp, tuning):
+    s = numpy.int32(numpy.random.random(size=1000) * 1000)
+    r = s.copy()
+    mp.sort(r, orderby=None, out=None, tuning=tuning)
+    assert (r == numpy.sort(s)).all()
+
+
+def test_sort_inplace_outplace_flatiter(mp):
+    s = numpy.int32(numpy.random.random(size=1000) * 1000)
+    local = s.copy()
+    mp.sort(local, local, out=None)
+    assert (local == numpy.sort(s)).all()
+    local = s.copy()
+    res = numpy.zeros(local.size, dtype=local.dtype)
+    mp.sort(local, local, out=res)
+    assert (res == numpy.sort(s)).all()
+    local = s.copy()
+    res = numpy.zeros(local.size, dtype=local.dtype)
+    mp.sort(local.flat, local.flat, out=res.flat)
+    assert (res == numpy.sort(s)).all()
+
+
+def test_sort_struct_and_vectors(mp):
+    s = numpy.empty(10, dtype=[('value', 'i8'), ('key', 'i8')])
+    numpy.random.seed(1234)
+    s['value'] = numpy.int32(numpy.random.random(size=10) * 1000 - 400)
+    s['key'] = s['value']
+    backup = s.copy()
+    res = numpy.zeros_like(s)
+    mp.sort(s, 'key', out=res)
+    backup.sort(order='key')
+    assert (backup['value'] == res['value']).all()
+
+    s = numpy.empty(10, dtype=[('value', 'i8'), ('key', 'i8'), ('vkey', ('i8', 2))])
+    s['value'] = numpy.int32(numpy.random.random(size=len(s)) * 1000)
+    s['key'][:][...] = s['value']
+    s['vkey'][:, 0][...] = s['value']
+    s['vkey'][:, 1][...] = s['value']
+    res = numpy.zeros_like(s)
+    mp.sort(s, 'vkey', out=res)
+    s.sort(order='key')
+    assert (s['value'] == res['value']).all()
+
+    s = numpy.empty(10, dtype=[('value', 'i8')])
+    s['value'] = numpy.int32(numpy.random.random(size=len(s)) * 1000)
+    k = numpy.empty(len(s), ('i8', 2))
+    k[:, 0][...] = s['value']
+    k[:, 1][...] = s['value']
+    res = numpy.zeros_like(s)
+    mp.sort(s, k, out=res)
+    s.sort(order='value')
+    assert (s['value'] == res['value']).all()
+
+
+def test_permute_take(mp):
+    s = numpy.arange(10)
+    i = numpy.arange(9, -1, -1)
+    assert (mp.permute(s, i, None) == s[i]).all()
+    res = numpy.empty(10, s.dtype)
+    mp.permute(s, i, None, out=res)
+    assert (res == s[i]).all()
+    assert (mp.take(s, i, None) == s[i]).all()
+    res = numpy.empty(10, s.dtype)
+    mp.take(s, i, None, out=res)
+    assert (res == s[i]).all()
+    rng = numpy.random.default_rng(4)
+    src = rng.integers(0, 1 << 40, 50_000)
+    idx = rng.integers(0, 50_000, 50_000)      # not a permutation, repeats
+    assert (mp.take(src, idx, None) == src[idx]).all()
+    perm = rng.permutation(50_000)
+    assert (mp.permute(src, perm, None) == src[perm]).all()
+
+
+def test_few_items_exhaustive(mp):
+    from itertools import product
+    for sizes in product(*([[0, 1, 2]] * 4)):
+        A = [numpy.arange(sizes[i], dtype='u8') for i in range(4)]
+        s = numpy.empty(sum(sizes), dtype=[('vkey', ('u8', 3)), ('vector', ('u4', 3))])
+        s['vkey'] = numpy.concatenate(A)[:, None]
+        s['vector'] = 1
+        S = s.copy()
+        S.sort()
+        r = numpy.empty(len(s), dtype=s.dtype)
+        mp.sort(s, 'vkey', out=r)
+        assert (r['vkey'] == S['vkey']).all()
+
+
+# ------------------------------------------ splitters and the model --
+def test_device_bisection_matches_oracle(mp):
+    from mpsort import device
+    lib = O.oracle_lib()
+    rng = numpy.random.default_rng(2)
+    for s, nsplit, dist in ((10_000, 63, "u"), (50_000, 1023, "dup"), (4096, 4095, "u"), (777, 8, "dup")):
+        if dist == "u":
+            x = numpy.sort(rng.integers(0, 2**64, s, dtype=numpy.uint64, endpoint=False))
+        else:
+            x = numpy.sort(rng.integers(0, 50, s).astype(numpy.uint64) * numpy.uint64(1 << 40))
+        S, clt, cle, rounds = device.debug_bisect(x, nsplit)
+        P = numpy.zeros(nsplit, numpy.uint64)
+        CLT = numpy.zeros(nsplit + 2, numpy.int64)
+        CLE = numpy.zeros(nsplit + 2, numpy.int64)
+        it = lib.oracle_bisect_splitters(x.ctypes.data, s, 8, nsplit, P.ctypes.data, CLT.ctypes.data,
+                                         CLE.ctypes.data)
+        assert (S == P).all()
+        assert (clt == CLT[1:nsplit + 1]).all() and (cle == CLE[1:nsplit + 1]).all()
+        assert rounds == it
+        C = numpy.array([s * (i + 1) // (nsplit + 1) for i in range(nsplit)])
+        assert ((clt < C) & (C <= cle)).all()
+
+
+def test_cdf_forward_backward_matches_numpy(mp):
+    """Gradient check of the hand-written forward/backward kernels."""
+    from mpsort import device
+    import cdf_oracle
+    rng = numpy.random.default_rng(7)
+    for lbits, gen in ((6, lambda: rng.integers(0, 2**64, 20000, dtype=numpy.uint64, endpoint=False)),
+                       (8, lambda: rng.integers(10**6, 10**6 + 5000, 20000).astype(numpy.uint64)),
+                       (4, lambda: (rng.normal(0, 1e9, 20000) + 2**62).astype(numpy.uint64))):
+        x = numpy.sort(gen())
+        y = numpy.sort(rng.random((1 << lbits) + 1)).astype(numpy.float32)
+        y[0], y[-1] = 0, 1
+        loss, pred, grad = device.cdf_forward_backward(x, x[0], x[-1], lbits, y)
+        l2, p2, g2 = cdf_oracle.forward_backward(x, int(x[0]), int(x[-1]), lbits, y)
+        assert abs(loss - l2) <= 1e-4 * max(1e-6, l2) + 1e-7
+        numpy.testing.assert_allclose(pred, p2, rtol=1e-5, atol=1e-6)
+        numpy.testing.assert_allclose(grad, g2, rtol=2e-3, atol=1e-7)
+        # finite-difference check of the numpy gradient itself
+        j = len(y) // 2
+        h = 1e-3
+        yp = y.astype(numpy.float64).copy(); yp[j] += h
+        ym = y.astype(numpy.float64).copy(); ym[j] -= h
+        fd = (cdf_oracle.forward_backward(x, int(x[0]), int(x[-1]), lbits, yp)[0] -
+              cdf_oracle.forward_backward(x, int(x[0]), int(x[-1]), lbits, ym)[0]) / (2 * h)
+        assert abs(fd - g2[j]) <= 1e-3 * max(abs(fd), 1e-4) + 1e-6
+
+
+@pytest.mark.parametrize("dist", ["uniform", "zipf", "clustered", "narrow"])
+def test_learned_lookup_equals_search(mp, dist):
+    from mpsort import device
+    rng = numpy.random.default_rng(11)
+    n = 400_000
+    if dist == "uniform":
+        keys = rng.integers(0, 2**64, n, dtype=numpy.uint64, endpoint=False)
+    elif dist == "zipf":
+        vals = rng.integers(0, 2**64, 10000, dtype=numpy.uint64, endpoint=False)
+        keys = vals[numpy.minimum(rng.zipf(1.2, n) - 1, 9999)]
+    elif dist == "clustered":
+        c = rng.integers(0, 2**60, 50, dtype=numpy.uint64)
+        keys = c[rng.integers(0, 50, n)] + rng.integers(0, 1 << 20, n).astype(numpy.uint64)
+    else:
+        keys = rng.integers(1000, 3000, n).astype(numpy.uint64)
+    sample = keys[:: 8]
+    for nb in (16, 1024, 8192):
+        probe = numpy.concatenate([keys[:100_000], numpy.array([0, 2**64 - 1, 1], dtype=numpy.uint64)])
+        bs, bl, S, widest = device.debug_buckets(sample, nb, probe)
+        assert (bs == bl).all(), (dist, nb)
+        assert (numpy.diff(S.astype(object)) >= 0).all()
+
+
+# --------------------------------------------- batched and join paths --
+def test_segments(mp):
+    import torch
+    from mpsort import device
+    rng = numpy.random.default_rng(5)
+    sizes = numpy.concatenate([[0, 1, 2, 4096, 4097, 70_000], rng.integers(0, 3000, 200)])
+    offs = numpy.concatenate([[0], numpy.cumsum(sizes)]).astype(numpy.uint64)
+    n = int(offs[-1])
+    dt = numpy.dtype([('key', 'i4'), ('payload', 'u4')])
+    a = numpy.zeros(n, dt)
+    a['key'] = rng.integers(-2**31, 2**31 - 1, n)
+    a['key'][::10] = -2**31 + rng.integers(0, 5, len(a['key'][::10]))
+    a['payload'] = numpy.arange(n)
+    din = torch.from_numpy(a.view(numpy.uint8).copy()).cuda()
+    dout = torch.empty_like(din)
+    device.sort_segments(din.data_ptr(), dout.data_ptr(), offs, dt, 'key')
+    torch.cuda.synchronize()
+    got = dout.cpu().numpy().view(dt)
+    for i in range(len(sizes)):
+        lo, hi = int(offs[i]), int(offs[i + 1])
+        assert got[lo:hi].tobytes() == O.numpy_sorted(a[lo:hi], 'key').tobytes(), i
+
+
+def test_merge_join(mp):
+    import torch
+    from mpsort import device
+    rng = numpy.random.default_rng(6)
+    dt = numpy.dtype([('id', 'i8'), ('mass', 'f4'), ('halo', 'i4')])
+    ids = rng.choice(numpy.arange(-10**7, 10**7), 300_000, replace=False)
+    a = numpy.zeros(200_000, dt)
+    a['id'] = ids[:200_000]
+    b = numpy.zeros(200_000, dt)
+    b['id'] = numpy.concatenate([ids[4000:196_000], ids[200_000:208_000]])
+    a = O.numpy_sorted(a, 'id')
+    b = O.numpy_sorted(b, 'id')
+    da = torch.from_numpy(a.view(numpy.uint8).copy()).cuda()
+    db = torch.from_numpy(b.view(numpy.uint8).copy()).cuda()
+    pa = torch.empty(200_000, dtype=torch.int64, device='cuda')
+    pb = torch.empty_like(pa)
+    npairs = torch.zeros(1, dtype=torch.int64, device='cuda')
+    device.merge_join(da.data_ptr(), len(a), db.data_ptr(), len(b), dt, 'id', pa.data_ptr(), pb.data_ptr(),
+                      npairs.data_ptr())
+    torch.cuda.synchronize()
+    k = int(npairs.item())
+    common, ia, ib = numpy.intersect1d(a['id'], b['id'], assume_unique=True, return_indices=True)
+    assert k == len(common)
+    assert (pa[:k].cpu().numpy() == ia).all() and (pb[:k].cpu().numpy() == ib).all()
+
+
+def test_stats_report_method(mp):
+    rng = numpy.random.default_rng(8)
+    a = make([('key', 'u8'), ('val', 'i8')], 'key', 1_000_000, "uniform", rng)
+    for m in METHODS:
+        check(mp, a, 'key', m)
+        st = mp.last_stats()
+        assert st["method"] == m
+        if m != "lsd":
+            assert st["nbuckets"] > 1 and st["window_misses"] == 0
