@@ -1,0 +1,386 @@
+"""Benchmark of the GB300 histogram sort (one JSON line on rank 0).
+
+Workload (default): 1e9 records of [('key','u8'),('val','i8')] (16 B, 16 GB),
+key uniform uint64 from a seeded generator, val = index -- the large plain
+sort on one GB300.  A step is one sort of the whole array, input resident in
+HBM, output to a second buffer (the inputs are far larger than L2, so no L2
+flush is needed between steps).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--method learned|plain|lsd] [--n N] [--dist uniform|sorted1pct|zipf]
+
+`value` is the device-resident throughput (records/s); `e2e` is the same
+metric through the public host API (mpsort.sort on pinned host arrays, host
+to device and back inside the timed region).  The reference arm times the
+CPU implementation of the same path on this machine's cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "mp-sort_gb300"))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+METRIC = "sorted records/s (1e9 x 16 B u64-keyed records)"
+UNIT = "records/s"
+DTYPE_DESC = [('key', 'u8'), ('val', 'i8')]
+
+# Algorithmic bytes per record of the dominant kernel (the level-1 bucket
+# scatter reads and writes every record once) and of the whole pipeline
+# (two passes, each a read and a write of every record).
+E = 16
+SCATTER_BYTES_PER_RECORD = 2 * E
+PIPELINE_BYTES_PER_RECORD = 2 * 2 * E
+
+# DRAM bytes per record of the scatter kernel measured by ncu
+# (profiles/l1_scatter_16B.md: dram__bytes_read.sum + dram__bytes_write.sum
+# of one launch on 1e8 records, divided by 1e8; traffic grows in proportion
+# to the records processed).
+SCATTER_NCU_BYTES_PER_RECORD = None
+
+
+def load_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def scatter_traffic_per_record():
+    """Per-record DRAM traffic of the scatter kernel from the committed ncu
+    summary (a `bytes_per_record:` line), or None."""
+    path = os.path.join(REPO, "profiles", "l1_scatter_16B.md")
+    try:
+        for line in open(path):
+            if line.strip().startswith("bytes_per_record:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_keys(torch, n, dist, device, seed):
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    if dist == "uniform":
+        return torch.randint(-2**63, 2**63 - 1, (n,), dtype=torch.int64, device=device, generator=g)
+    if dist == "sorted1pct":
+        k = torch.arange(n, dtype=torch.int64, device=device)
+        m = n // 100
+        i = torch.randint(0, n, (m,), device=device, generator=g)
+        j = torch.randint(0, n, (m,), device=device, generator=g)
+        ki, kj = k[i].clone(), k[j].clone()
+        k[i] = kj
+        k[j] = ki
+        return k
+    if dist == "zipf":
+        # rank r in [1, 1e6] with P(r) ~ r^-1.2 by inverse transform on a
+        # tabulated CDF, mapped through a seeded permutation of random values
+        import numpy as np
+        rng = np.random.default_rng(seed)
+        ranks = np.arange(1, 10**6 + 1, dtype=np.float64)
+        cdf = np.cumsum(ranks ** -1.2)
+        cdf /= cdf[-1]
+        vals = torch.from_numpy(rng.integers(-2**63, 2**63 - 1, 10**6, dtype=np.int64)).to(device)
+        cdf_t = torch.from_numpy(cdf).to(device)
+        u = torch.rand(n, dtype=torch.float64, device=device, generator=g)
+        r = torch.searchsorted(cdf_t, u).clamp_(max=10**6 - 1)
+        return vals[r]
+    raise ValueError(dist)
+
+
+def run_ours(args):
+    import numpy
+    import torch
+    import mpsort
+    from mpsort import device as dev
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dt = numpy.dtype(DTYPE_DESC)
+    n = args.n
+    rec = torch.empty((n, 2), dtype=torch.int64, device="cuda")
+    rec[:, 0] = make_keys(torch, n, args.dist, "cuda", 1234 + rank)
+    rec[:, 1] = torch.arange(n, device="cuda")
+    out = torch.empty_like(rec)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    def step():
+        dev.sort(rec.data_ptr(), out.data_ptr(), n, dt, 'key', args.method, sp)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # parity of the last warm-up output: sorted keys, permutation of the input
+    ks = out[:, 0] ^ (-2**63)
+    ok_sorted = bool((ks[1:] >= ks[:-1]).all().item())
+    vs = out[:, 1]
+    ok_perm = bool((torch.bincount(vs, minlength=n) == 1).all().item())
+    eq = ks[1:] == ks[:-1]
+    ok_stable = bool((~eq | (vs[1:] > vs[:-1])).all().item())
+    del ks, vs, eq
+
+    stats_steps = []
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+            stats_steps.append(mpsort.last_stats())
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    ms_per_step = ms / args.steps
+    value = world * n / (ms_per_step / 1e3)
+
+    # the plain form on the same data, for the learned-vs-plain comparison
+    plain_rps = None
+    if args.method == "learned" and not args.no_compare:
+        for _ in range(2):
+            dev.sort(rec.data_ptr(), out.data_ptr(), n, dt, 'key', 'plain', sp)
+        torch.cuda.synchronize()
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        for _ in range(max(1, args.steps // 2)):
+            dev.sort(rec.data_ptr(), out.data_ptr(), n, dt, 'key', 'plain', sp)
+        p1.record(stream)
+        torch.cuda.synchronize()
+        plain_rps = n / (p0.elapsed_time(p1) / max(1, args.steps // 2) / 1e3)
+
+    st = stats_steps[-1]
+    stage_ms = {k: round(sum(s["stage_ms"][k] for s in stats_steps) / len(stats_steps), 4)
+                for k in st["stage_ms"]}
+
+    # e2e through the host API: pinned host arrays, H2D + sort + D2H per step
+    e2e = None
+    if not args.no_e2e:
+        del out
+        torch.cuda.empty_cache()
+        hin = torch.empty((n, 2), dtype=torch.int64, pin_memory=True)
+        hin.copy_(rec)
+        del rec
+        torch.cuda.empty_cache()
+        hout = torch.empty_like(hin, pin_memory=True)
+        a_in = hin.numpy().view(dt).reshape(n)
+        a_out = hout.numpy().view(dt).reshape(n)
+        mpsort.sort(a_in, 'key', out=a_out, method=args.method)  # warm-up (allocates staging)
+        steps_e2e = max(1, min(args.steps, 3))
+        t0 = time.perf_counter()
+        for _ in range(steps_e2e):
+            mpsort.sort(a_in, 'key', out=a_out, method=args.method)
+        t1 = time.perf_counter()
+        e2e = {"value": n / ((t1 - t0) / steps_e2e), "unit": UNIT,
+               "h2d_bytes_per_step": n * dt.itemsize, "d2h_bytes_per_step": n * dt.itemsize,
+               "steps": steps_e2e}
+        mpsort._lib.lib().gbsort_release()
+
+    peak, peak_kind = load_peaks()
+    scat_ms = stage_ms["scatter"]
+    achieved = n * SCATTER_BYTES_PER_RECORD / (scat_ms / 1e3) / 1e9 if scat_ms > 0 else None
+    tpr = scatter_traffic_per_record()
+    roofline = {"bound": "hbm", "kernel": "k_l1_scatter (level-1 bucket scatter)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if achieved else None, "peak_kind": peak_kind,
+                "traffic": tpr * n if tpr else None,
+                "algorithmic_bytes_per_launch": n * SCATTER_BYTES_PER_RECORD,
+                "pipeline_frac": n * PIPELINE_BYTES_PER_RECORD / (ms_per_step / 1e3) / 1e9 / peak}
+
+    launches = st.get("launches")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64 keys, 16 B records",
+        "data": "synthetic (seeded %s uint64 keys, val = index)" % args.dist,
+        "config": {"workload": "1e9 x 16 B [('key','u8'),('val','i8')] sort by key, %s keys" % args.dist,
+                   "n": n, "elsize": E, "method": args.method, "l2": "inputs (16 GB) larger than L2",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": roofline,
+        "e2e": e2e,
+        "gpu_launches": launches * args.steps if launches else None,
+        "learned_vs_plain": {"learned_records_per_s": value / world if args.method == "learned" else None,
+                             "plain_records_per_s": plain_rps},
+        "stage_ms": stage_ms,
+        "sort_stats": {k: v for k, v in st.items() if k != "stage_ms"},
+        "parity": {"sorted": ok_sorted, "permutation": ok_perm, "stable": ok_stable},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        line["cpu_baseline"] = cpu_baseline(args)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(args, seconds=None):
+    """The CPU port of mpsort_omp (oracle/oracle.c, OpenMP over all host
+    cores) on a bounded sample of the same workload."""
+    import numpy
+    import oracle as O
+    threads = os.cpu_count() or 1
+    n = args.cpu_sample
+    rng = numpy.random.default_rng(0)
+    a = numpy.empty(n, dtype=DTYPE_DESC)
+    if args.dist == "uniform":
+        a['key'] = rng.integers(0, 2**64, n, dtype=numpy.uint64, endpoint=False)
+    else:
+        a['key'] = numpy.arange(n, dtype=numpy.uint64)
+    a['val'] = numpy.arange(n)
+    kind = "reference" if O.ref_lib() is not None else "port"
+    if kind == "reference":
+        O.set_ref_threads(threads)
+        t = O.time_ref_sort(a, 'key', 'omp', repeat=3)
+    else:
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            O.oracle_mpsort(a, 'key', threads)
+            ts.append(time.perf_counter() - t0)
+        ts.sort()
+        t = ts[1]
+    return {"value": n / t, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": "%d records of the same 16 B layout, median of 3 sorts" % n}
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy
+    import oracle as O
+    threads = os.cpu_count() or 1
+    n = args.cpu_sample
+    rng = numpy.random.default_rng(0)
+    a = numpy.empty(n, dtype=DTYPE_DESC)
+    a['key'] = rng.integers(0, 2**64, n, dtype=numpy.uint64, endpoint=False)
+    a['val'] = numpy.arange(n)
+    kind = "reference" if O.ref_lib() is not None else "port"
+    O.set_ref_threads(threads) if kind == "reference" else None
+
+    def one():
+        t0 = time.perf_counter()
+        if kind == "reference":
+            O.ref_sort(a, 'key', 'omp')
+        else:
+            O.oracle_mpsort(a, 'key', threads)
+        return time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        one()
+    t = sum(one() for _ in range(args.steps))
+    ms_per_step = t / args.steps * 1e3
+    value = n / (ms_per_step / 1e3)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64 keys, 16 B records",
+        "data": "synthetic (seeded uniform uint64 keys, val = index)",
+        "config": {"workload": "1e9 x 16 B [('key','u8'),('val','i8')] sort by key, uniform keys",
+                   "n": args.n, "elsize": E, "parallelism": "CPU threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": "each step sorts %d records of the workload's layout" % n},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--method", choices=["learned", "plain", "lsd"], default="learned")
+    ap.add_argument("--n", type=int, default=10**9)
+    ap.add_argument("--dist", choices=["uniform", "sorted1pct", "zipf"], default="uniform")
+    ap.add_argument("--cpu-sample", type=int, default=20_000_000)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-compare", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -60,7 +60,12 @@ typedef struct gbsort_stats {
     uint32_t lsd_passes;         /* digit passes of the LSD path */
     uint32_t widest_window;      /* widest learned search window (buckets) */
     float model_loss;            /* final training loss of the learned model */
-    uint32_t reserved[4];
+    /* device time (ms, CUDA events) of the histogram sort's stages: splitter
+     * search (sample, sort, bisection or training), bucket counts, count
+     * scan, bucket scatter, bucket splits, local sorts */
+    float stage_ms[6];
+    uint32_t launches;           /* kernels this sort enqueued */
+    uint32_t reserved[3];
 } gbsort_stats;
 
 /* Sort nmemb records of elsize bytes from d_in into d_out (device memory;

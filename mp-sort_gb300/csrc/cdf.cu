@@ -19,6 +19,7 @@
 #include "cdf.cuh"
 #include "cdf_api.h"
 #include "common.cuh"
+#include "kernels.h"
 
 namespace gb {
 
@@ -328,6 +329,7 @@ cudaError_t cdf_forward(const uint64_t* x, uint32_t s, const CdfShape& sh, const
   cudaError_t e = cudaMemsetAsync(loss, 0, sizeof(float), st);
   if (e != cudaSuccess) return e;
   k_cdf_forward<<<grid_for(s, 256), 256, 0, st>>>(x, s, sh, y, pred, loss);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -336,6 +338,7 @@ cudaError_t cdf_backward(const uint64_t* x, uint32_t s, const CdfShape& sh, cons
   cudaError_t e = cudaMemsetAsync(grad, 0, sizeof(float) * ((1u << sh.lbits) + 1), st);
   if (e != cudaSuccess) return e;
   k_cdf_backward<<<grid_for(s, 256), 256, 0, st>>>(x, s, sh, y, grad);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -344,14 +347,18 @@ cudaError_t cdf_train(const uint64_t* x, uint32_t s, const CdfShape& sh, int epo
   const int nk = (1 << sh.lbits) + 1;
   cudaError_t e;
   k_cdf_init<<<grid_for(nk, 256), 256, 0, st>>>(x, s, sh, w.y);
+  note_launches(1);
   if ((e = cudaMemsetAsync(w.h, 0, sizeof(float) * nk, st)) != cudaSuccess) return e;
   k_cdf_curvature<<<grid_for(s, 256), 256, 0, st>>>(x, s, sh, w.h);
+  note_launches(1);
   for (int it = 0; it < epochs; ++it) {
     if ((e = cdf_backward(x, s, sh, w.y, w.grad, st)) != cudaSuccess) return e;
     k_cdf_step<<<grid_for(nk, 256), 256, 0, st>>>(w.y, w.grad, w.h, nk, lr);
+    note_launches(1);
   }
   if (w.loss && (e = cdf_forward(x, s, sh, w.y, nullptr, w.loss, st)) != cudaSuccess) return e;
   k_cdf_project<<<1, 1024, 0, st>>>(w.y, nk, w.knots);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -362,6 +369,7 @@ cudaError_t cdf_splitters(const uint64_t* x, uint32_t s, const CdfShape& sh, int
   k_cdf_splitters<<<grid_for(nsplit, 128), 128, 0, st>>>(sh, nbuckets, knots, S);
   k_cdf_heavy<<<grid_for(s, 256), 256, 0, st>>>(x, s, nbuckets, S);
   k_cummax_u64<<<1, 1024, 0, st>>>(S, nsplit);
+  note_launches(3);
   return cudaGetLastError();
 }
 
@@ -374,6 +382,7 @@ cudaError_t cdf_windows(const CdfShape& sh, int nbuckets, const float2* knots, c
   if ((e = cudaMemsetAsync(widest, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
   k_cdf_windows<<<grid_for(nbuckets + nleaf, 128), 128, 0, st>>>(sh, nbuckets, knots, S, tmp_lo, tmp_hi);
   k_pack_windows<<<grid_for(nleaf, 256), 256, 0, st>>>(tmp_lo, tmp_hi, nleaf, win, widest);
+  note_launches(2);
   return cudaGetLastError();
 }
 

@@ -118,16 +118,16 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T* tmp, T* total) {
 // Items are in "warp-chunk" order: item r of lane l in warp w is tile element
 //   w * 32 * RPT + r * 32 + l,
 // so each warp owns a contiguous run of the tile.  Ranks are positions in the
-// tile stably sorted by digit.  `hist` is kWarps << DIGIT_BITS uint16
-// counters (digit-major).  Items with valid == false must carry the largest
-// digit; they then land after every valid item.
+// tile stably sorted by digit.  `hist` holds kWarps << DIGIT_BITS uint16
+// counters, warp-major (hist[w][d]), so the lanes of a warp touching
+// different digits touch different banks.  Items with valid == false must
+// carry the largest digit; they then land after every valid item.
 // ---------------------------------------------------------------------------
 template <int RPT, int DIGIT_BITS>
 struct BlockRank {
   static constexpr int kDigits = 1 << DIGIT_BITS;
   static constexpr int kCounters = kDigits * kWarps;
-  static_assert(kCounters % kThreads == 0, "counter count must divide the block");
-  static constexpr int kPerThread = kCounters / kThreads;
+  static constexpr int kDigitsPerThread = (kDigits + kThreads - 1) / kThreads;
 
   // ranks[r] receives the position of item r; digit_start (optional, kDigits
   // + 1 entries in shared memory) receives the start of every digit's run.
@@ -138,40 +138,52 @@ struct BlockRank {
     for (int i = threadIdx.x; i < kCounters; i += kThreads) hist[i] = 0;
     __syncthreads();
     const uint32_t lt = lanemask_lt();
+    uint16_t* wh = hist + w * kDigits;
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
       const uint32_t d = digit[r];
       const uint32_t peers = __match_any_sync(GB_FULL_MASK, d);
-      const uint32_t before = hist[d * kWarps + w];
+      const uint32_t before = wh[d];
       ranks[r] = before + __popc(peers & lt);
       __syncwarp();
-      if ((peers & lt) == 0) hist[d * kWarps + w] = (uint16_t)(before + __popc(peers));
+      if ((peers & lt) == 0) wh[d] = (uint16_t)(before + __popc(peers));
       __syncwarp();
     }
     __syncthreads();
-    // exclusive scan over the digit-major counters
-    uint32_t local[kPerThread];
+    // per digit: exclusive prefix over the warps, then over the digits
+    uint32_t tot[kDigitsPerThread];
     uint32_t sum = 0;
-    const int base = threadIdx.x * kPerThread;
 #pragma unroll
-    for (int i = 0; i < kPerThread; ++i) {
-      local[i] = hist[base + i];
-      sum += local[i];
+    for (int j = 0; j < kDigitsPerThread; ++j) {
+      const int d = threadIdx.x * kDigitsPerThread + j;
+      uint32_t run = 0;
+      if (d < kDigits) {
+#pragma unroll
+        for (int q = 0; q < kWarps; ++q) {
+          uint32_t c = hist[q * kDigits + d];
+          hist[q * kDigits + d] = (uint16_t)run;
+          run += c;
+        }
+      }
+      tot[j] = run;
+      sum += run;
     }
     uint32_t total;
-    uint32_t pre = block_exclusive_scan<uint32_t>(sum, scan_tmp, &total);
+    uint32_t base = block_exclusive_scan<uint32_t>(sum, scan_tmp, &total);
 #pragma unroll
-    for (int i = 0; i < kPerThread; ++i) {
-      hist[base + i] = (uint16_t)pre;
-      pre += local[i];
+    for (int j = 0; j < kDigitsPerThread; ++j) {
+      const int d = threadIdx.x * kDigitsPerThread + j;
+      if (d < kDigits) {
+#pragma unroll
+        for (int q = 0; q < kWarps; ++q) hist[q * kDigits + d] = (uint16_t)(hist[q * kDigits + d] + base);
+        if (digit_start) digit_start[d] = base;
+      }
+      base += tot[j];
     }
+    if (digit_start && threadIdx.x == 0) digit_start[kDigits] = total;
     __syncthreads();
-    if (digit_start) {
-      for (int d = threadIdx.x; d < kDigits; d += kThreads) digit_start[d] = hist[d * kWarps];
-      if (threadIdx.x == 0) digit_start[kDigits] = total;
-    }
 #pragma unroll
-    for (int r = 0; r < RPT; ++r) ranks[r] += hist[digit[r] * kWarps + w];
+    for (int r = 0; r < RPT; ++r) ranks[r] += wh[digit[r]];
     __syncthreads();
   }
 };

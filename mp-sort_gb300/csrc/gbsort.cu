@@ -124,6 +124,7 @@ struct Context {
   DevBuf small;            // splitters, counts, tasks, model, counters
   DevBuf radix;            // host radix bytes (callback path)
   HostCounters* hc = nullptr;
+  cudaEvent_t ev[8] = {};  // stage boundaries of the histogram sort
   std::mutex mu;
 };
 
@@ -151,6 +152,7 @@ int get_ctx(Context** out) {
     c->device = dev;
     GB_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     GB_CUDA(cudaMallocHost(&c->hc, sizeof(HostCounters)));
+    for (cudaEvent_t& e : c->ev) GB_CUDA(cudaEventCreate(&e));
     g_ctx[dev] = c;
   }
   *out = g_ctx[dev];
@@ -279,16 +281,52 @@ int choose_buckets(uint32_t n) {
   return (int)std::min<uint32_t>(nb, 8192);
 }
 
-int run_tasks_rounds(Context& c, const HsortParams& p, SortTask* t0, SortTask* t1, uint32_t* nt, uint32_t cap,
-                     uint32_t* work, uint32_t* stats, uint32_t* err, cudaStream_t st) {
-  const int kRounds = 8;  // 64-bit keys lose >= 12 bits of range per round
-  SortTask* lists[2] = {t0, t1};
-  for (int r = 0; r < kRounds; ++r) {
-    uint32_t* nin = nt + (r & 1);
-    uint32_t* nout = nt + ((r + 1) & 1);
-    GB_CUDA(cudaMemsetAsync(nout, 0, sizeof(uint32_t), st));
-    GB_CUDA(run_tasks(p, lists[r & 1], nin, lists[(r + 1) & 1], nout, cap, work, stats, err, st));
+// Device task lists of level 2 and their counters.
+struct Level2 {
+  SortTask* split[2];
+  SortTask* local;
+  uint32_t* nsplit;  // [2]
+  uint32_t* nlocal;
+  uint32_t* work;
+  uint32_t cap_split, cap_local;
+  static size_t bytes(uint32_t cap_split, uint32_t cap_local) {
+    return ((size_t)cap_split * 2 + cap_local) * sizeof(SortTask) + 4096;
   }
+  void carve(Bump& bump, uint32_t* counters, uint32_t cs, uint32_t cl) {
+    cap_split = cs;
+    cap_local = cl;
+    split[0] = bump.take<SortTask>(cs);
+    split[1] = bump.take<SortTask>(cs);
+    local = bump.take<SortTask>(cl);
+    nsplit = counters;
+    nlocal = counters + 2;
+    work = counters + 3;
+  }
+  TaskListsHost round(int r) const {  // round r reads split[r&1], appends to split[(r+1)&1]
+    TaskListsHost L;
+    L.split_in = split[r & 1];
+    L.nsplit_in = nsplit + (r & 1);
+    L.split_out = split[(r + 1) & 1];
+    L.nsplit_out = nsplit + ((r + 1) & 1);
+    L.local = local;
+    L.nlocal = nlocal;
+    L.cap_split = cap_split;
+    L.cap_local = cap_local;
+    return L;
+  }
+};
+
+constexpr int kSplitRounds = 16;  // every round narrows each re-split range; 64-bit keys need few
+
+// The split rounds, then one pass over every local task.  The initial tasks
+// must already be in split[0] (count in nsplit[0]).
+int run_level2(const HsortParams& p, const Level2& l2, uint32_t* stats, uint32_t* err, cudaStream_t st) {
+  for (int r = 0; r < kSplitRounds; ++r) {
+    TaskListsHost L = l2.round(r);
+    GB_CUDA(cudaMemsetAsync(L.nsplit_out, 0, sizeof(uint32_t), st));
+    GB_CUDA(run_split_round(p, L, l2.work, stats, err, st));
+  }
+  GB_CUDA(run_local(p, l2.local, l2.nlocal, l2.cap_local, l2.work, stats, st));
   return GBSORT_OK;
 }
 
@@ -300,18 +338,17 @@ int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t el
   const int nb = choose_buckets(n);
   const int grid = hsort_grid(n);
   const uint32_t s = nb > 1 ? (uint32_t)std::min<uint64_t>(n, std::max<uint64_t>(4096, (uint64_t)nb * 128)) : 0;
-  const uint32_t cap = (uint32_t)nb + n / 2048 + 4096;
+  const uint32_t cap_split = (uint32_t)nb + n / 4096 + 4096;
+  const uint32_t cap_local = 4u * (uint32_t)nb + n / 512 + 65536;
   const int lbits = 11;
   const int nleaf = 1 << lbits;
-  size_t small_bytes = (size_t)s * 16 + (size_t)nb * 8 + (size_t)nb * grid * 8 + (size_t)cap * 2 * sizeof(SortTask) +
+  size_t small_bytes = (size_t)s * 16 + (size_t)nb * 8 + (size_t)nb * grid * 8 + Level2::bytes(cap_split, cap_local) +
                        (size_t)256 * lsd_grid(std::max<uint32_t>(s, 1)) * 8 + (size_t)nleaf * 64 + (4 << 20);
   GB_CUDA(c.small.ensure(small_bytes));
   Bump bump{c.small.as<uint8_t>()};
   uint32_t* counters = bump.take<uint32_t>(64);  // stats, err, ntasks x2, work, iters, widest
   uint32_t* stats = counters;
   uint32_t* err = counters + STAT_SLOTS;  // kernels given `stats` also find the error word here
-  uint32_t* nt = counters + 18;
-  uint32_t* work = counters + 20;
   uint32_t* iters = counters + 21;
   uint32_t* widest = counters + 22;
   float* loss = reinterpret_cast<float*>(counters + 23);
@@ -319,8 +356,8 @@ int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t el
   uint64_t* S = bump.take<uint64_t>((size_t)std::max(nb, 2));
   uint32_t* counts = bump.take<uint32_t>((size_t)nb * grid);
   uint32_t* scan_tmp = bump.take<uint32_t>(scan_tmp_words((size_t)nb * grid));
-  SortTask* t0 = bump.take<SortTask>(cap);
-  SortTask* t1 = bump.take<SortTask>(cap);
+  Level2 l2;
+  l2.carve(bump, counters + 24, cap_split, cap_local);
 
   HsortParams p{};
   p.in = (const uint8_t*)d_in;
@@ -333,6 +370,7 @@ int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t el
 
   ModelDev model{};
   int lookup = LOOKUP_PLAIN;
+  GB_CUDA(cudaEventRecord(c.ev[0], st));
   if (nb > 1) {
     uint64_t* sA = bump.take<uint64_t>(s);
     uint64_t* sB = bump.take<uint64_t>(s);
@@ -372,16 +410,29 @@ int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t el
       c.hc->iters = epochs;
     }
   }
+  GB_CUDA(cudaEventRecord(c.ev[1], st));
   GB_CUDA(l1_count(p, lookup, S, nb, lookup == LOOKUP_LEARNED ? &model : nullptr, counts, stats, st));
+  GB_CUDA(cudaEventRecord(c.ev[2], st));
   GB_CUDA(exclusive_scan_u32(counts, counts, (size_t)nb * grid, scan_tmp, st));
+  GB_CUDA(cudaEventRecord(c.ev[3], st));
   GB_CUDA(l1_scatter(p, lookup, S, nb, lookup == LOOKUP_LEARNED ? &model : nullptr, counts, stats, st));
-  GB_CUDA(build_tasks(counts, grid, S, nb, n, t0, nt, cap, err, stats, st));
-  int rc = run_tasks_rounds(c, p, t0, t1, nt, cap, work, stats, err, st);
-  if (rc) return rc;
+  GB_CUDA(cudaEventRecord(c.ev[4], st));
+  {
+    TaskListsHost L = l2.round(-1);  // appends to split[0]
+    GB_CUDA(build_tasks(counts, grid, S, nb, n, L, err, stats, st));
+  }
+  for (int r = 0; r < kSplitRounds; ++r) {
+    TaskListsHost L = l2.round(r);
+    GB_CUDA(cudaMemsetAsync(L.nsplit_out, 0, sizeof(uint32_t), st));
+    GB_CUDA(run_split_round(p, L, l2.work, stats, err, st));
+  }
+  GB_CUDA(cudaEventRecord(c.ev[5], st));
+  GB_CUDA(run_local(p, l2.local, l2.nlocal, l2.cap_local, l2.work, stats, st));
+  GB_CUDA(cudaEventRecord(c.ev[6], st));
   uint32_t learned_iters = learned ? c.hc->iters : 0;
   GB_CUDA(cudaMemcpyAsync(c.hc->stats, counters, sizeof(uint32_t) * STAT_SLOTS, cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaMemcpyAsync(&c.hc->err, err, 4, cudaMemcpyDeviceToHost, st));
-  GB_CUDA(cudaMemcpyAsync(c.hc->ntasks, nt, 8, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(c.hc->ntasks, l2.nsplit, 8, cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaMemcpyAsync(&c.hc->iters, iters, 4, cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaMemcpyAsync(&c.hc->widest, widest, 4, cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaMemcpyAsync(&c.hc->loss, loss, 4, cudaMemcpyDeviceToHost, st));
@@ -390,8 +441,8 @@ int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t el
     set_err("device check failed: code %u", c.hc->err);
     return GBSORT_ERR_INTERNAL;
   }
-  if (c.hc->ntasks[0] != 0) {  // after 8 rounds the last list (index 0) must be empty
-    set_err("split rounds did not finish: %u tasks left", c.hc->ntasks[0]);
+  if (c.hc->ntasks[kSplitRounds & 1] != 0) {  // the last round's output list must be empty
+    set_err("split rounds did not finish: %u tasks left", c.hc->ntasks[kSplitRounds & 1]);
     return GBSORT_ERR_INTERNAL;
   }
   g_stats = gbsort_stats{};
@@ -408,12 +459,31 @@ int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t el
   g_stats.max_bucket = c.hc->stats[STAT_MAX_BUCKET];
   g_stats.widest_window = c.hc->widest;
   g_stats.model_loss = learned ? c.hc->loss : 0.f;
+  for (int i = 0; i < 6; ++i) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c.ev[i], c.ev[i + 1]);
+    g_stats.stage_ms[i] = ms;
+  }
   return GBSORT_OK;
 }
 
+int sort_device_dispatch(Context& c, const void* d_in, void* d_out, size_t nmemb, size_t elsize,
+                         const gbsort_key_desc* key, int method, cudaStream_t st);
+
 int sort_device_locked(Context& c, const void* d_in, void* d_out, size_t nmemb, size_t elsize,
                        const gbsort_key_desc* key, int method, cudaStream_t st) {
-  if (nmemb == 0) return GBSORT_OK;
+  const unsigned long long l0 = launch_count();
+  int rc = sort_device_dispatch(c, d_in, d_out, nmemb, elsize, key, method, st);
+  if (rc == GBSORT_OK) g_stats.launches = (uint32_t)(launch_count() - l0);
+  return rc;
+}
+
+int sort_device_dispatch(Context& c, const void* d_in, void* d_out, size_t nmemb, size_t elsize,
+                         const gbsort_key_desc* key, int method, cudaStream_t st) {
+  if (nmemb == 0) {
+    g_stats = gbsort_stats{};
+    return GBSORT_OK;
+  }
   if (nmemb >= 0xffffffffull || elsize == 0 || elsize > (1u << 20)) {
     set_err("nmemb must be < 2^32 and elsize in [1, 2^20]");
     return GBSORT_ERR_BAD_ARG;
@@ -544,21 +614,21 @@ int gbsort_sort_segments_device(const void* d_in, void* d_out, const uint64_t* s
   }
   GB_CUDA(c->A.ensure((size_t)N * E));
   GB_CUDA(c->B.ensure((size_t)N * E));
-  const uint32_t cap = (uint32_t)nseg + N / 2048 + 4096;
-  GB_CUDA(c->small.ensure((size_t)cap * 2 * sizeof(SortTask) + (nseg + 1) * 8 + (1 << 20)));
+  const uint32_t cap_split = (uint32_t)nseg * 2 + N / 4096 + 4096;
+  const uint32_t cap_local = 4u * (uint32_t)nseg + N / 512 + 65536;
+  GB_CUDA(c->small.ensure(Level2::bytes(cap_split, cap_local) + (nseg + 1) * 8 + (1 << 20)));
   Bump bump{c->small.as<uint8_t>()};
   uint32_t* counters = bump.take<uint32_t>(64);
   uint32_t* stats = counters;
-  uint32_t* err = counters + 16;
-  uint32_t* nt = counters + 18;
-  uint32_t* work = counters + 20;
+  uint32_t* err = counters + STAT_SLOTS;
   uint64_t* offs = bump.take<uint64_t>(nseg + 1);
-  SortTask* t0 = bump.take<SortTask>(cap);
-  SortTask* t1 = bump.take<SortTask>(cap);
+  Level2 l2;
+  l2.carve(bump, counters + 24, cap_split, cap_local);
   GB_CUDA(cudaMemsetAsync(counters, 0, 64 * sizeof(uint32_t), st));
   GB_CUDA(cudaMemcpyAsync(offs, seg_offsets, (nseg + 1) * 8, cudaMemcpyHostToDevice, st));
   GB_CUDA(cudaMemcpyAsync(c->A.p, d_in, (size_t)N * E, cudaMemcpyDeviceToDevice, st));
-  GB_CUDA(segment_ranges(c->A.as<uint8_t>(), E, key->word[0], offs, (uint32_t)nseg, t0, nt, cap, err, st));
+  GB_CUDA(segment_ranges(c->A.as<uint8_t>(), E, key->word[0], offs, (uint32_t)nseg, l2.split[0], l2.nsplit,
+                         cap_split, err, st));
   HsortParams p{};
   p.in = (const uint8_t*)d_in;
   p.out = (uint8_t*)d_out;
@@ -567,14 +637,15 @@ int gbsort_sort_segments_device(const void* d_in, void* d_out, const uint64_t* s
   p.n = N;
   p.elsize = E;
   p.key = key->word[0];
-  rc = run_tasks_rounds(*c, p, t0, t1, nt, cap, work, stats, err, st);
+  rc = run_level2(p, l2, stats, err, st);
   if (rc) return rc;
   GB_CUDA(cudaMemcpyAsync(c->hc->stats, counters, sizeof(uint32_t) * STAT_SLOTS, cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaMemcpyAsync(&c->hc->err, err, 4, cudaMemcpyDeviceToHost, st));
-  GB_CUDA(cudaMemcpyAsync(c->hc->ntasks, nt, 8, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(c->hc->ntasks, l2.nsplit, 8, cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaStreamSynchronize(st));
-  if (c->hc->err || c->hc->ntasks[0]) {
-    set_err("segmented sort device check failed: code %u, %u tasks left", c->hc->err, c->hc->ntasks[0]);
+  if (c->hc->err || c->hc->ntasks[kSplitRounds & 1]) {
+    set_err("segmented sort device check failed: code %u, %u tasks left", c->hc->err,
+            c->hc->ntasks[kSplitRounds & 1]);
     return GBSORT_ERR_INTERNAL;
   }
   g_stats = gbsort_stats{};

@@ -18,6 +18,8 @@
 #include "common.cuh"
 #include "kernels.h"
 
+#include <type_traits>
+
 namespace gb {
 
 int num_sms();
@@ -26,7 +28,7 @@ namespace {
 
 constexpr int kLocalMax = 4096;        // records a local sort holds in shared memory
 constexpr int kLocalRpt = kLocalMax / kThreads;
-constexpr int kLocalBits = 10;         // digit of the local MSD pass
+constexpr int kLocalBits = 9;          // digit of the local MSD pass
 constexpr int kInsertMax = 24;         // bins up to this size use insertion sort
 constexpr int kSplitBits = 12;         // bins of a bucket split
 constexpr int kSplitBins = 1 << kSplitBits;
@@ -196,14 +198,22 @@ __device__ __forceinline__ uint32_t lookup(const LookupSmem& L, const ModelDev& 
   else return bucket_learned(L.S, m, L.knots, L.win, key, misses);
 }
 
-// Loads splitters (and the model tables) into shared memory at `smem`;
-// returns the first free byte.
+// Loads the lookup tables into shared memory at `smem` and returns the first
+// free byte.  The plain lookup binary-searches every splitter, so they go to
+// shared memory; the learned lookup touches at most a couple of splitters
+// per key (its window), so it reads them through the L1 cache and keeps
+// only the model's knots and windows in shared memory -- which leaves room
+// for more resident CTAs.
 template <int LK>
 __device__ __forceinline__ uint8_t* load_lookup(uint8_t* smem, const uint64_t* S, int nbuckets,
                                                 const ModelDev& m, LookupSmem& L) {
-  L.S = reinterpret_cast<uint64_t*>(smem);
-  for (int i = threadIdx.x; i < nbuckets - 1; i += blockDim.x) L.S[i] = S[i];
-  smem += 8 * (size_t)((nbuckets + 1) & ~1);
+  if constexpr (LK == LOOKUP_PLAIN) {
+    L.S = reinterpret_cast<uint64_t*>(smem);
+    for (int i = threadIdx.x; i < nbuckets - 1; i += blockDim.x) L.S[i] = S[i];
+    smem += 8 * (size_t)((nbuckets + 1) & ~1);
+  } else {
+    L.S = const_cast<uint64_t*>(S);
+  }
   if constexpr (LK == LOOKUP_LEARNED) {
     const int nl = 1 << m.lbits;
     L.knots = reinterpret_cast<float2*>(smem);
@@ -218,14 +228,13 @@ __device__ __forceinline__ uint8_t* load_lookup(uint8_t* smem, const uint64_t* S
 
 template <int LK>
 size_t lookup_smem_bytes(int nbuckets, const ModelDev* m) {
-  size_t b = 8 * (size_t)((nbuckets + 1) & ~1);
-  if (LK == LOOKUP_LEARNED) b += 12 * ((size_t)1 << m->lbits);
-  return b;
+  if (LK == LOOKUP_LEARNED) return 12 * ((size_t)1 << m->lbits);
+  return 8 * (size_t)((nbuckets + 1) & ~1);
 }
 
 // ----------------------------------------------------- level-1 count ------
 template <int LK>
-__global__ void __launch_bounds__(kThreads) k_l1_count(HsortParams p, const uint64_t* __restrict__ S,
+__global__ void __launch_bounds__(kThreads, 2) k_l1_count(HsortParams p, const uint64_t* __restrict__ S,
                                                         int nbuckets, ModelDev model,
                                                         uint32_t* __restrict__ counts,
                                                         uint32_t* __restrict__ stats) {
@@ -237,12 +246,19 @@ __global__ void __launch_bounds__(kThreads) k_l1_count(HsortParams p, const uint
   const uint32_t c = blockIdx.x, g = gridDim.x;
   const uint32_t cb = chunk_begin(p.n, c, g), ce = chunk_end(p.n, c, g);
   constexpr int U = 8;
+  // keys of the next batch are loaded while the current batch is counted
+  uint64_t k[U], kn[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    uint32_t i = cb + u * kThreads + threadIdx.x;
+    kn[u] = i < ce ? key_at(p.in, i, p.elsize, p.key) : 0;
+  }
   for (uint32_t base = cb; base < ce; base += kThreads * U) {
-    uint64_t k[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      uint32_t i = base + u * kThreads + threadIdx.x;
-      k[u] = i < ce ? key_at(p.in, i, p.elsize, p.key) : 0;
+      k[u] = kn[u];
+      uint32_t i = base + kThreads * U + u * kThreads + threadIdx.x;
+      kn[u] = i < ce ? key_at(p.in, i, p.elsize, p.key) : 0;
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
@@ -260,7 +276,7 @@ __global__ void __launch_bounds__(kThreads) k_l1_count(HsortParams p, const uint
 // --------------------------------------------------- level-1 scatter ------
 template <int EW>
 struct Tile {
-  static constexpr int kRpt = (32 / EW) < 1 ? 1 : (32 / EW);
+  static constexpr int kRpt = (32 / EW) < 1 ? 1 : ((32 / EW) > 8 ? 8 : (32 / EW));
   static constexpr int kSize = kThreads * kRpt;
 };
 
@@ -273,7 +289,7 @@ template <int EW, int LK>
 __global__ void __launch_bounds__(kThreads, 1) k_l1_scatter(HsortParams p, const uint64_t* __restrict__ S,
                                                              int nbuckets, ModelDev model,
                                                              const uint32_t* __restrict__ offsets,
-                                                             uint32_t* __restrict__ stats) {
+                                                             int nchunks, uint32_t* __restrict__ stats) {
   uint32_t* err = stats + STAT_SLOTS;  // the error word follows the statistics
   constexpr int RPT = Tile<EW>::kRpt, T = Tile<EW>::kSize;
   using Rank = BlockRank<RPT, 7>;
@@ -292,22 +308,34 @@ __global__ void __launch_bounds__(kThreads, 1) k_l1_scatter(HsortParams p, const
   q += 2 * T;
   __shared__ uint32_t scan_tmp[kWarps];
 
-  const uint32_t c = blockIdx.x, g = gridDim.x;
-  const uint32_t cb = chunk_begin(p.n, c, g), ce = chunk_end(p.n, c, g);
-  for (int b = threadIdx.x; b < nbuckets; b += kThreads) cursor[b] = offsets[(size_t)b * g + c];
-  __syncthreads();
   const uint32_t w = warp_id(), lane = lane_id();
   const uint32_t E = EW * 4;
   const bool two_pass = nbuckets > 128;
+  // the count kernel's chunks, several per CTA
+  for (uint32_t c = blockIdx.x; c < (uint32_t)nchunks; c += gridDim.x) {
+  const uint32_t g = (uint32_t)nchunks;
+  const uint32_t cb = chunk_begin(p.n, c, g), ce = chunk_end(p.n, c, g);
+  __syncthreads();
+  for (int b = threadIdx.x; b < nbuckets; b += kThreads) cursor[b] = offsets[(size_t)b * g + c];
+  __syncthreads();
 
+  // the next tile's records are loaded while the current tile is ranked
+  uint32_t nxt[RPT][EW];
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) {
+    uint32_t e = w * 32 * RPT + r * 32 + lane;
+    if (cb + e < ce) RecIO<EW>::load(p.in + (size_t)(cb + e) * E, nxt[r]);
+  }
   for (uint32_t t0 = cb; t0 < ce; t0 += T) {
     const uint32_t nvalid = min((uint32_t)T, ce - t0);
     uint32_t rec[RPT][EW];
     uint32_t bkt[RPT], dig[RPT], pos[RPT];
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
-      uint32_t e = w * 32 * RPT + r * 32 + lane;
-      if (e < nvalid) RecIO<EW>::load(p.in + (size_t)(t0 + e) * E, rec[r]);
+#pragma unroll
+      for (int q2 = 0; q2 < EW; ++q2) rec[r][q2] = nxt[r][q2];
+      uint32_t e = t0 + T + w * 32 * RPT + r * 32 + lane;
+      if (e < ce) RecIO<EW>::load(p.in + (size_t)e * E, nxt[r]);
     }
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
@@ -370,6 +398,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_l1_scatter(HsortParams p, const
     }
     __syncthreads();
   }
+  }
 }
 
 template <int EW, int LK>
@@ -380,9 +409,42 @@ size_t l1_scatter_smem(int nbuckets, const ModelDev* m) {
 }
 
 // ------------------------------------------------------------- tasks -----
+// Level 2 runs as two kinds of persistent kernels over device task lists:
+//   k_split  -- one CTA per SM takes buckets larger than kLocalMax, splits
+//               each by a histogram of its key range and appends the pieces
+//               to the local list (small), the next split list (still
+//               large) or as copies (one key);
+//   k_local  -- two CTAs per SM drain the local list: shared-memory sorts
+//               and copies, all writing the final output.
+// Local tasks only read their own ranges of A / B, which later splits never
+// touch, so one k_local launch after the last split round serves them all.
+struct TaskLists {
+  const SortTask* split_in;
+  const uint32_t* nsplit_in;
+  SortTask* split_out;
+  uint32_t* nsplit_out;
+  SortTask* local;
+  uint32_t* nlocal;
+  uint32_t cap_split;
+  uint32_t cap_local;
+};
+
+__device__ __forceinline__ void push(SortTask* list, uint32_t* n, uint32_t cap, const SortTask& t, uint32_t* err) {
+  uint32_t at = atomicAdd(n, 1u);
+  if (at < cap) list[at] = t;
+  else set_error(err, DEV_ERR_TASK_OVERFLOW);
+}
+
+// Copies of single-key ranges go to the local list in pieces of kCopyPiece.
+__device__ __forceinline__ void push_copy(const TaskLists& L, uint32_t start, uint32_t cnt, uint64_t lo, uint64_t hi,
+                                          uint32_t src, uint32_t* err) {
+  for (uint32_t s0 = 0; s0 < cnt; s0 += kCopyPiece)
+    push(L.local, L.nlocal, L.cap_local, SortTask{start + s0, min(kCopyPiece, cnt - s0), lo, hi, src, TASK_COPY},
+         err);
+}
+
 __global__ void k_build_tasks(const uint32_t* __restrict__ offsets, int grid,
-                              const uint64_t* __restrict__ S, int nbuckets, uint32_t n,
-                              SortTask* __restrict__ tasks, uint32_t* ntasks, uint32_t cap,
+                              const uint64_t* __restrict__ S, int nbuckets, uint32_t n, TaskLists L,
                               uint32_t* err, uint32_t* stats) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nbuckets) return;
@@ -393,31 +455,48 @@ __global__ void k_build_tasks(const uint32_t* __restrict__ offsets, int grid,
   atomicMax(stats + STAT_MAX_BUCKET, cnt);
   uint64_t lo = b == 0 ? 0ull : S[b - 1];
   uint64_t hi = b == nbuckets - 1 ? ~0ull : S[b] - 1;
-  if (lo == hi || cnt == 1) {
-    uint32_t pieces = (cnt + kCopyPiece - 1) / kCopyPiece;
-    uint32_t at = atomicAdd(ntasks, pieces);
-    if (at + pieces > cap) { set_error(err, DEV_ERR_TASK_OVERFLOW); return; }
-    for (uint32_t i = 0; i < pieces; ++i) {
-      uint32_t s0 = start + i * kCopyPiece;
-      tasks[at + i] = SortTask{s0, min(kCopyPiece, end - s0), lo, hi, 0u, TASK_COPY};
+  if (lo == hi || cnt == 1) push_copy(L, start, cnt, lo, hi, 0u, err);
+  else if (cnt <= (uint32_t)kLocalMax) push(L.local, L.nlocal, L.cap_local, SortTask{start, cnt, lo, hi, 0u, TASK_SORT}, err);
+  else push(L.split_out, L.nsplit_out, L.cap_split, SortTask{start, cnt, lo, hi, 0u, TASK_SORT}, err);
+}
+
+// Block copy with four independent vector loads in flight per thread.
+template <int EW>
+__device__ __forceinline__ void block_copy_ilp(const uint8_t* src, uint8_t* dst, uint32_t count, int nthreads) {
+  constexpr int E = EW * 4;
+  using V = typename std::conditional<EW % 4 == 0, uint4, typename std::conditional<EW % 2 == 0, uint2, uint32_t>::type>::type;
+  const uint64_t nv = (uint64_t)count * E / sizeof(V);
+  const V* s = reinterpret_cast<const V*>(src);
+  V* d = reinterpret_cast<V*>(dst);
+  constexpr int U = sizeof(V) >= 16 ? 2 : 4;
+  for (uint64_t f0 = threadIdx.x; f0 < nv; f0 += (uint64_t)nthreads * U) {
+    V v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      uint64_t f = f0 + (uint64_t)u * nthreads;
+      if (f < nv) v[u] = s[f];
     }
-  } else {
-    uint32_t at = atomicAdd(ntasks, 1u);
-    if (at >= cap) { set_error(err, DEV_ERR_TASK_OVERFLOW); return; }
-    tasks[at] = SortTask{start, cnt, lo, hi, 0u, TASK_SORT};
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      uint64_t f = f0 + (uint64_t)u * nthreads;
+      if (f < nv) d[f] = v[u];
+    }
   }
 }
 
-// Shared memory of the task engine (a union of the split and local phases).
 struct LocalSmem {
-  uint64_t key[kLocalMax];
-  uint16_t idx[kLocalMax];
+  uint64_t keyA[kLocalMax];  // keys in input order (then staging of big bins)
+  uint64_t keyB[kLocalMax];  // keys in sorted order
+  uint16_t idxA[kLocalMax];
+  uint16_t idxB[kLocalMax];
   uint16_t hist[kWarps << kLocalBits];
   uint32_t start[(1 << kLocalBits) + 1];
   uint16_t big[kLocalMax / (kInsertMax + 1) + 2];  // start of pending bins
   uint16_t bigsz[kLocalMax / (kInsertMax + 1) + 2];
   uint32_t nbig;
   uint64_t red[2 * kWarps];
+  uint32_t scan_tmp[kWarps];
+  uint32_t task_id;
 };
 struct SplitSmem {
   uint32_t hist[kSplitBins];
@@ -425,13 +504,8 @@ struct SplitSmem {
   uint32_t cursor[kMaxGroups];
   uint32_t dstart[kMaxGroups + 1];
   uint16_t rhist[kWarps * kMaxGroups];
-};
-struct EngineSmem {
-  union {
-    LocalSmem loc;
-    SplitSmem spl;
-  };
-  uint32_t gstart[kMaxGroups + 1];  // split groups: kept while local sorts reuse the union
+  uint64_t red[2 * kWarps];
+  uint32_t gstart[kMaxGroups + 1];
   uint32_t gfirst[kMaxGroups + 1];
   uint32_t scan_tmp[kWarps];
   uint32_t task_id;
@@ -459,13 +533,11 @@ __device__ __forceinline__ void block_minmax(uint64_t& mn, uint64_t& mx, uint64_
   __syncthreads();
 }
 
-// One MSD counting pass over positions [a, a+s) whose keys and indices are in
-// registers (warp-chunk order): stable by (key - mn) >> shift, written to
-// sm.key / sm.idx at [a, a+s); small bins are then insertion-sorted and large
-// bins queued for another pass.
-__device__ void local_msd_pass(LocalSmem& sm, uint32_t* scan_tmp, const uint64_t (&k)[kLocalRpt],
-                               const uint32_t (&ix)[kLocalRpt], uint32_t a, uint32_t s, uint64_t mn,
-                               uint64_t mx, uint32_t* stats) {
+// One MSD counting pass over positions [a, a+s) of keyA / idxA: stable by
+// (key - mn) >> shift into keyB / idxB at [a, a+s); small bins are then
+// insertion-sorted there and large bins queued for another pass.  Keys stay
+// in shared memory, so the pass needs few registers.
+__device__ void local_msd_pass(LocalSmem& sm, uint32_t a, uint32_t s, uint64_t mn, uint64_t mx) {
   using Rank = BlockRank<kLocalRpt, kLocalBits>;
   const uint32_t w = warp_id(), lane = lane_id();
   const int bits = bitlen64(mx - mn);
@@ -474,15 +546,15 @@ __device__ void local_msd_pass(LocalSmem& sm, uint32_t* scan_tmp, const uint64_t
 #pragma unroll
   for (int r = 0; r < kLocalRpt; ++r) {
     uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
-    dig[r] = e < s ? (uint32_t)((k[r] - mn) >> shift) : ((1u << kLocalBits) - 1);
+    dig[r] = e < s ? (uint32_t)((sm.keyA[a + e] - mn) >> shift) : ((1u << kLocalBits) - 1);
   }
-  Rank::rank(dig, pos, sm.hist, scan_tmp, sm.start);
+  Rank::rank(dig, pos, sm.hist, sm.scan_tmp, sm.start);
 #pragma unroll
   for (int r = 0; r < kLocalRpt; ++r) {
     uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
     if (e < s) {
-      sm.key[a + pos[r]] = k[r];
-      sm.idx[a + pos[r]] = (uint16_t)ix[r];
+      sm.keyB[a + pos[r]] = sm.keyA[a + e];
+      sm.idxB[a + pos[r]] = sm.idxA[a + e];
     }
   }
   __syncthreads();
@@ -491,8 +563,8 @@ __device__ void local_msd_pass(LocalSmem& sm, uint32_t* scan_tmp, const uint64_t
     if (b1 <= b0 + 1) continue;
     uint32_t sz = b1 - b0;
     if (sz <= (uint32_t)kInsertMax) {
-      uint64_t* key = sm.key + a + b0;
-      uint16_t* idx = sm.idx + a + b0;
+      uint64_t* key = sm.keyB + a + b0;
+      uint16_t* idx = sm.idxB + a + b0;
       for (uint32_t i = 1; i < sz; ++i) {
         uint64_t kv = key[i];
         uint16_t iv = idx[i];
@@ -514,35 +586,39 @@ __device__ void local_msd_pass(LocalSmem& sm, uint32_t* scan_tmp, const uint64_t
   __syncthreads();
 }
 
-// Stable sort of `m` <= kLocalMax records of src by key into dst.
+// Stable sort of `m` <= kLocalMax records of src by key into dst (distinct).
 template <int EW>
-__device__ void local_sort(EngineSmem& es, const uint8_t* src, uint8_t* dst, uint32_t m,
+__device__ void local_sort(LocalSmem& sm, const uint8_t* src, uint8_t* dst, uint32_t m,
                            const gbsort_key_word& kw, uint32_t* stats) {
-  LocalSmem& sm = es.loc;
   constexpr uint32_t E = EW * 4;
   const uint32_t w = warp_id(), lane = lane_id();
-  uint64_t k[kLocalRpt];
-  uint32_t ix[kLocalRpt];
   uint64_t mn = ~0ull, mx = 0;
+  {
+    uint64_t k[kLocalRpt];
 #pragma unroll
-  for (int r = 0; r < kLocalRpt; ++r) {
-    uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
-    ix[r] = e;
-    if (e < m) {
-      k[r] = key_at(src, e, E, kw);
-      mn = k[r] < mn ? k[r] : mn;
-      mx = k[r] > mx ? k[r] : mx;
-    } else {
-      k[r] = 0;
+    for (int r = 0; r < kLocalRpt; ++r) {
+      uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
+      k[r] = e < m ? key_at(src, e, E, kw) : 0;
+    }
+#pragma unroll
+    for (int r = 0; r < kLocalRpt; ++r) {
+      uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
+      if (e < m) {
+        sm.keyA[e] = k[r];
+        sm.idxA[e] = (uint16_t)e;
+        mn = k[r] < mn ? k[r] : mn;
+        mx = k[r] > mx ? k[r] : mx;
+      }
     }
   }
   if (threadIdx.x == 0) sm.nbig = 0;
   block_minmax(mn, mx, sm.red);
   if (mn == mx) {  // one key: the input order is the stable order
-    block_copy<EW>(src, dst, m);
+    block_copy_ilp<EW>(src, dst, m, kThreads);
+    __syncthreads();
     return;
   }
-  local_msd_pass(sm, es.scan_tmp, k, ix, 0, m, mn, mx, stats);
+  local_msd_pass(sm, 0, m, mn, mx);
   // further passes over bins too large for insertion sort
   for (;;) {
     uint32_t nb = sm.nbig;
@@ -552,81 +628,99 @@ __device__ void local_sort(EngineSmem& es, const uint8_t* src, uint8_t* dst, uin
     __syncthreads();
     if (threadIdx.x == 0) sm.nbig = nb - 1;
     uint64_t bmn = ~0ull, bmx = 0;
-#pragma unroll
-    for (int r = 0; r < kLocalRpt; ++r) {
-      uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
-      if (e < s) {
-        k[r] = sm.key[a + e];
-        ix[r] = sm.idx[a + e];
-        bmn = k[r] < bmn ? k[r] : bmn;
-        bmx = k[r] > bmx ? k[r] : bmx;
-      }
+    for (uint32_t e = threadIdx.x; e < s; e += kThreads) {
+      uint64_t kv = sm.keyB[a + e];
+      sm.keyA[a + e] = kv;
+      sm.idxA[a + e] = sm.idxB[a + e];
+      bmn = kv < bmn ? kv : bmn;
+      bmx = kv > bmx ? kv : bmx;
     }
     block_minmax(bmn, bmx, sm.red);
     if (bmn == bmx) continue;  // equal keys are already in input order
     if (threadIdx.x == 0) atomicAdd(stats + STAT_BIGBIN, 1u);
-    local_msd_pass(sm, es.scan_tmp, k, ix, a, s, bmn, bmx, stats);
+    local_msd_pass(sm, a, s, bmn, bmx);
   }
-  // gather the records into dst in sorted order
-  if constexpr (EW % 4 == 0) {
-    constexpr int V = EW / 4;
-    for (uint32_t f = threadIdx.x; f < m * V; f += kThreads) {
-      uint32_t i = f / V, v = f % V;
-      reinterpret_cast<uint4*>(dst + (size_t)i * E)[v] =
-          reinterpret_cast<const uint4*>(src + (size_t)sm.idx[i] * E)[v];
-    }
-  } else if constexpr (EW % 2 == 0) {
-    constexpr int V = EW / 2;
-    for (uint32_t f = threadIdx.x; f < m * V; f += kThreads) {
-      uint32_t i = f / V, v = f % V;
-      reinterpret_cast<uint2*>(dst + (size_t)i * E)[v] =
-          reinterpret_cast<const uint2*>(src + (size_t)sm.idx[i] * E)[v];
-    }
-  } else {
-    for (uint32_t f = threadIdx.x; f < m * EW; f += kThreads) {
-      uint32_t i = f / EW, v = f % EW;
-      reinterpret_cast<uint32_t*>(dst + (size_t)i * E)[v] =
-          reinterpret_cast<const uint32_t*>(src + (size_t)sm.idx[i] * E)[v];
+  // gather the records into dst in sorted order, four loads in flight
+  {
+    using V = typename std::conditional<EW % 4 == 0, uint4,
+                                        typename std::conditional<EW % 2 == 0, uint2, uint32_t>::type>::type;
+    constexpr int VPR = E / sizeof(V);
+    constexpr int U = sizeof(V) >= 16 ? 2 : 4;
+    const uint32_t nv = m * VPR;
+    for (uint32_t f0 = threadIdx.x; f0 < nv; f0 += kThreads * U) {
+      V v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        uint32_t f = f0 + u * kThreads;
+        if (f < nv) v[u] = reinterpret_cast<const V*>(src + (size_t)sm.idxB[f / VPR] * E)[f % VPR];
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        uint32_t f = f0 + u * kThreads;
+        if (f < nv) reinterpret_cast<V*>(dst + (size_t)(f / VPR) * E)[f % VPR] = v[u];
+      }
     }
   }
   __syncthreads();
 }
 
 // Split of one large bucket: 4096 bins of its key range, grouped into at most
-// 256 runs of consecutive bins, a stable scatter src -> other by group, then
-// a local sort (or a new task) per group.
+// 256 runs of consecutive bins, a stable scatter src -> other by group, and
+// one task per group (local sort, copy, or another split).
 template <int EW>
-__device__ void split_task(EngineSmem& es, const HsortParams& p, const SortTask& task,
-                           SortTask* tasks_out, uint32_t* ntasks_out, uint32_t cap, uint32_t* stats,
-                           uint32_t* err) {
-  SplitSmem& sm = es.spl;
+__device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& task, const TaskLists& L,
+                           uint32_t* stats, uint32_t* err) {
   constexpr uint32_t E = EW * 4;
   constexpr int RPT = Tile<EW>::kRpt, T = Tile<EW>::kSize;
   using Rank = BlockRank<RPT, 8>;
   const uint8_t* src = (task.src ? p.bufB : p.bufA) + (size_t)task.start * E;
   uint8_t* oth = (task.src ? p.bufA : p.bufB) + (size_t)task.start * E;
-  uint8_t* out = p.out + (size_t)task.start * E;
   const uint32_t m = task.count;
-  const int bits = bitlen64(task.hi - task.lo);
-  const int shift = bits > kSplitBits ? bits - kSplitBits : 0;
-  const uint32_t nbins = (uint32_t)((task.hi - task.lo) >> shift) + 1;
+  int bits = bitlen64(task.hi - task.lo);
+  int shift = bits > kSplitBits ? bits - kSplitBits : 0;
+  uint32_t nbins = (uint32_t)((task.hi - task.lo) >> shift) + 1;
   const uint32_t w = warp_id(), lane = lane_id();
 
-  for (int i = threadIdx.x; i < kSplitBins; i += kThreads) sm.hist[i] = 0;
-  __syncthreads();
-  for (uint32_t i0 = 0; i0 < m; i0 += kThreads) {
-    uint32_t i = i0 + threadIdx.x;
-    bool v = i < m;
-    uint32_t bin = 0xffffffffu;
-    if (v) {
-      uint64_t key = key_at(src, i, E, p.key);
-      uint64_t x = key > task.lo ? key - task.lo : 0;
-      bin = (uint32_t)min(x >> shift, (uint64_t)(nbins - 1));
+  // Histogram over the task's key range; if the keys actually present span
+  // far fewer bits, histogram again over their own range so that the bins
+  // split them finely.
+  uint64_t blo = task.lo, bhi = task.hi;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int i = threadIdx.x; i < kSplitBins; i += kThreads) sm.hist[i] = 0;
+    __syncthreads();
+    uint64_t mn = ~0ull, mx = 0;
+    constexpr int U = 8;  // keys in flight per thread
+    for (uint32_t i0 = 0; i0 < m; i0 += kThreads * U) {
+      uint64_t kk[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        uint32_t i = i0 + u * kThreads + threadIdx.x;
+        kk[u] = i < m ? key_at(src, i, E, p.key) : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        uint32_t i = i0 + u * kThreads + threadIdx.x;
+        bool v = i < m;
+        uint32_t bin = 0xffffffffu;
+        if (v) {
+          uint64_t key = kk[u];
+          mn = key < mn ? key : mn;
+          mx = key > mx ? key : mx;
+          uint64_t x = key > blo ? key - blo : 0;
+          bin = (uint32_t)min(x >> shift, (uint64_t)(nbins - 1));
+        }
+        uint32_t peers = __match_any_sync(GB_FULL_MASK, bin);
+        if (v && (peers & lanemask_lt()) == 0) atomicAdd(&sm.hist[bin], (uint32_t)__popc(peers));
+      }
     }
-    uint32_t peers = __match_any_sync(GB_FULL_MASK, bin);
-    if (v && (peers & lanemask_lt()) == 0) atomicAdd(&sm.hist[bin], (uint32_t)__popc(peers));
+    block_minmax(mn, mx, sm.red);
+    if (pass == 1 || bitlen64(mx - mn) + 4 > bits) break;
+    blo = mn;
+    bhi = mx;
+    bits = bitlen64(bhi - blo);
+    shift = bits > kSplitBits ? bits - kSplitBits : 0;
+    nbins = (uint32_t)((bhi - blo) >> shift) + 1;
   }
-  __syncthreads();
   // exclusive scan of the bins, then the group of every bin
   {
     constexpr int PER = kSplitBins / kThreads;
@@ -636,7 +730,7 @@ __device__ void split_task(EngineSmem& es, const HsortParams& p, const SortTask&
       loc[i] = sm.hist[threadIdx.x * PER + i];
       s += loc[i];
     }
-    uint32_t pre = block_exclusive_scan<uint32_t>(s, es.scan_tmp, nullptr);
+    uint32_t pre = block_exclusive_scan<uint32_t>(s, sm.scan_tmp, nullptr);
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
       sm.hist[threadIdx.x * PER + i] = pre;
@@ -644,9 +738,17 @@ __device__ void split_task(EngineSmem& es, const HsortParams& p, const SortTask&
     }
   }
   __syncthreads();
-  uint32_t target = max((uint32_t)(kLocalMax / 2), (m + kMaxGroups - 1) / kMaxGroups);
+  // group of a bin = slot of its midpoint: a bin holding most of the records
+  // never shares a group with the empty bins on either side, so every group
+  // that is split again covers a strictly narrower key range
+  const uint32_t target = max((uint32_t)(kLocalMax / 2), (m + kMaxGroups - 1) / kMaxGroups);
   for (uint32_t b = threadIdx.x; b < (uint32_t)kSplitBins; b += kThreads) {
-    uint32_t gb_ = b < nbins ? min(sm.hist[b] / target, (uint32_t)(kMaxGroups - 1)) : kMaxGroups - 1;
+    uint32_t gb_ = kMaxGroups - 1;
+    if (b < nbins) {
+      uint64_t incl = b + 1 < (uint32_t)kSplitBins ? sm.hist[b + 1] : m;
+      unsigned long long mid2 = (unsigned long long)sm.hist[b] + incl;
+      gb_ = (uint32_t)min(mid2 / (2ull * target), (unsigned long long)(kMaxGroups - 1));
+    }
     sm.gmap[b] = (uint8_t)gb_;
   }
   __syncthreads();
@@ -654,18 +756,18 @@ __device__ void split_task(EngineSmem& es, const HsortParams& p, const SortTask&
     int gcur = sm.gmap[b];
     int gprev = b ? (int)sm.gmap[b - 1] : -1;
     for (int g = gprev + 1; g <= gcur; ++g) {
-      es.gstart[g] = sm.hist[b];
-      es.gfirst[g] = b;
+      sm.gstart[g] = sm.hist[b];
+      sm.gfirst[g] = b;
     }
     if (b == nbins - 1) {
       for (int g = gcur + 1; g <= kMaxGroups; ++g) {
-        es.gstart[g] = m;
-        es.gfirst[g] = nbins;
+        sm.gstart[g] = m;
+        sm.gfirst[g] = nbins;
       }
     }
   }
   __syncthreads();
-  for (int g = threadIdx.x; g < kMaxGroups; g += kThreads) sm.cursor[g] = es.gstart[g];
+  for (int g = threadIdx.x; g < kMaxGroups; g += kThreads) sm.cursor[g] = sm.gstart[g];
   __syncthreads();
   // stable scatter src -> other by group
   for (uint32_t t0 = 0; t0 < m; t0 += T) {
@@ -678,14 +780,14 @@ __device__ void split_task(EngineSmem& es, const HsortParams& p, const SortTask&
       if (e < nvalid) {
         RecIO<EW>::load(src + (size_t)(t0 + e) * E, rec[r]);
         uint64_t key = key_from_regs<EW>(rec[r], p.key);
-        uint64_t x = key > task.lo ? key - task.lo : 0;
+        uint64_t x = key > blo ? key - blo : 0;
         uint32_t bin = (uint32_t)min(x >> shift, (uint64_t)(nbins - 1));
         dig[r] = sm.gmap[bin];
       } else {
         dig[r] = kMaxGroups - 1;
       }
     }
-    Rank::rank(dig, pos, sm.rhist, es.scan_tmp, sm.dstart);
+    Rank::rank(dig, pos, sm.rhist, sm.scan_tmp, sm.dstart);
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
       uint32_t e = w * 32 * RPT + r * 32 + lane;
@@ -705,75 +807,74 @@ __device__ void split_task(EngineSmem& es, const HsortParams& p, const SortTask&
     __syncthreads();
   }
   __threadfence_block();
-  // per group: local sort, copy, or a new task for the next round
-  for (int g = 0; g < kMaxGroups; ++g) {
-    const uint32_t g0 = es.gstart[g], g1 = es.gstart[g + 1];
-    const uint32_t b0 = es.gfirst[g], b1 = es.gfirst[g + 1];
-    __syncthreads();
+  // one task per group
+  for (int g = threadIdx.x; g < kMaxGroups; g += kThreads) {
+    const uint32_t g0 = sm.gstart[g], g1 = sm.gstart[g + 1];
     if (g1 == g0) continue;
+    const uint32_t b0 = sm.gfirst[g], b1 = sm.gfirst[g + 1];
     const uint32_t s = g1 - g0;
-    uint64_t glo = task.lo + ((uint64_t)b0 << shift);
-    uint64_t ghi = b1 >= nbins ? task.hi : task.lo + ((uint64_t)b1 << shift) - 1;
+    const uint64_t glo = blo + ((uint64_t)b0 << shift);
+    const uint64_t ghi = b1 >= nbins ? bhi : blo + ((uint64_t)b1 << shift) - 1;
+    const uint32_t nsrc = task.src ^ 1u;
     if (glo == ghi || s == 1) {
-      if (s <= kCopyPiece) {
-        block_copy<EW>(oth + (size_t)g0 * E, out + (size_t)g0 * E, s);
-        __syncthreads();
-      } else if (threadIdx.x == 0) {
-        uint32_t pieces = (s + kCopyPiece - 1) / kCopyPiece;
-        uint32_t at = atomicAdd(ntasks_out, pieces);
-        if (at + pieces > cap) set_error(err, DEV_ERR_TASK_OVERFLOW);
-        else
-          for (uint32_t i = 0; i < pieces; ++i) {
-            uint32_t s0 = i * kCopyPiece;
-            tasks_out[at + i] = SortTask{task.start + g0 + s0, min(kCopyPiece, s - s0), glo, ghi,
-                                         task.src ^ 1u, TASK_COPY};
-          }
-      }
+      push_copy(L, task.start + g0, s, glo, ghi, nsrc, err);
     } else if (s <= (uint32_t)kLocalMax) {
-      local_sort<EW>(es, oth + (size_t)g0 * E, out + (size_t)g0 * E, s, p.key, stats);
-      if (threadIdx.x == 0) atomicAdd(stats + STAT_LOCAL, 1u);
-    } else if (threadIdx.x == 0) {
-      uint32_t at = atomicAdd(ntasks_out, 1u);
+      push(L.local, L.nlocal, L.cap_local, SortTask{task.start + g0, s, glo, ghi, nsrc, TASK_SORT}, err);
+    } else {
       atomicAdd(stats + STAT_PUSHED, 1u);
-      if (at >= cap) set_error(err, DEV_ERR_TASK_OVERFLOW);
-      else tasks_out[at] = SortTask{task.start + g0, s, glo, ghi, task.src ^ 1u, TASK_SORT};
+      push(L.split_out, L.nsplit_out, L.cap_split, SortTask{task.start + g0, s, glo, ghi, nsrc, TASK_SORT}, err);
     }
   }
   __syncthreads();
 }
 
 template <int EW>
-__global__ void __launch_bounds__(kThreads, 1) k_tasks(HsortParams p, const SortTask* __restrict__ tasks_in,
-                                                        const uint32_t* __restrict__ ntasks_in,
-                                                        SortTask* __restrict__ tasks_out,
-                                                        uint32_t* __restrict__ ntasks_out, uint32_t cap,
-                                                        uint32_t* __restrict__ work,
-                                                        uint32_t* __restrict__ stats,
-                                                        uint32_t* __restrict__ err) {
+__global__ void __launch_bounds__(kThreads, 1) k_split(HsortParams p, TaskLists L, uint32_t* __restrict__ work,
+                                                        uint32_t* __restrict__ stats, uint32_t* __restrict__ err) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
-  EngineSmem& es = *reinterpret_cast<EngineSmem*>(smem_raw);
-  constexpr uint32_t E = EW * 4;
-  const uint32_t nt = min(*ntasks_in, cap);
+  SplitSmem& sm = *reinterpret_cast<SplitSmem*>(smem_raw);
+  const uint32_t nt = min(*L.nsplit_in, L.cap_split);
   for (;;) {
-    if (threadIdx.x == 0) es.task_id = atomicAdd(work, 1u);
+    if (threadIdx.x == 0) sm.task_id = atomicAdd(work, 1u);
     __syncthreads();
-    const uint32_t t = es.task_id;
+    const uint32_t t = sm.task_id;
     __syncthreads();
     if (t >= nt) break;
-    const SortTask task = tasks_in[t];
+    const SortTask task = L.split_in[t];
+    if (task.kind == TASK_COPY || task.count <= (uint32_t)kLocalMax) {  // forwarded as is
+      if (threadIdx.x == 0) push(L.local, L.nlocal, L.cap_local, task, err);
+      continue;
+    }
+    if (threadIdx.x == 0) atomicAdd(stats + STAT_SPLIT, 1u);
+    split_task<EW>(sm, p, task, L, stats, err);
+  }
+}
+
+template <int EW>
+__global__ void __launch_bounds__(kThreads, 2) k_local(HsortParams p, const SortTask* __restrict__ tasks,
+                                                        const uint32_t* __restrict__ ntasks, uint32_t cap,
+                                                        uint32_t* __restrict__ work, uint32_t* __restrict__ stats) {
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  LocalSmem& sm = *reinterpret_cast<LocalSmem*>(smem_raw);
+  constexpr uint32_t E = EW * 4;
+  const uint32_t nt = min(*ntasks, cap);
+  for (;;) {
+    if (threadIdx.x == 0) sm.task_id = atomicAdd(work, 1u);
+    __syncthreads();
+    const uint32_t t = sm.task_id;
+    __syncthreads();
+    if (t >= nt) break;
+    const SortTask task = tasks[t];
     const uint8_t* src = (task.src ? p.bufB : p.bufA) + (size_t)task.start * E;
     uint8_t* out = p.out + (size_t)task.start * E;
     if (task.kind == TASK_COPY || task.count == 1) {
-      block_copy<EW>(src, out, task.count);
+      block_copy_ilp<EW>(src, out, task.count, kThreads);
       if (threadIdx.x == 0) atomicAdd(stats + STAT_COPY, 1u);
-    } else if (task.count <= (uint32_t)kLocalMax) {
-      local_sort<EW>(es, src, out, task.count, p.key, stats);
-      if (threadIdx.x == 0) atomicAdd(stats + STAT_LOCAL, 1u);
+      __syncthreads();
     } else {
-      if (threadIdx.x == 0) atomicAdd(stats + STAT_SPLIT, 1u);
-      split_task<EW>(es, p, task, tasks_out, ntasks_out, cap, stats, err);
+      local_sort<EW>(sm, src, out, task.count, p.key, stats);
+      if (threadIdx.x == 0) atomicAdd(stats + STAT_LOCAL, 1u);
     }
-    __syncthreads();
   }
 }
 
@@ -804,13 +905,11 @@ bool hsort_supported(uint32_t elsize) {
 }
 
 int hsort_grid(uint32_t n) {
-  int g = num_sms();
+  int g = num_sms() * 2;  // chunks of the count matrix: two CTAs per SM count them
   uint64_t maxg = ((uint64_t)n + 4095) / 4096;
   if ((uint64_t)g > maxg) g = (int)(maxg < 1 ? 1 : maxg);
   return g;
 }
-
-int task_engine_grid() { return num_sms(); }
 
 cudaError_t sample_keys(const uint8_t* rec, uint32_t n, uint32_t elsize, gbsort_key_word key, uint32_t s,
                         uint64_t* out, cudaStream_t stream) {
@@ -818,6 +917,7 @@ cudaError_t sample_keys(const uint8_t* rec, uint32_t n, uint32_t elsize, gbsort_
   unsigned blocks = (s + 255) / 256;
   if (blocks > 4096) blocks = 4096;
   k_sample<<<blocks, 256, 0, stream>>>(rec, n, elsize, key, s, out);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -828,6 +928,7 @@ cudaError_t plain_splitters(const uint64_t* sorted_sample, uint32_t s, int nspli
   if (e != cudaSuccess) return e;
   k_plain_splitters<<<(nsplit + 127) / 128, 128, 0, stream>>>(sorted_sample, s, nsplit, splitters, iters,
                                                                clt, cle);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -835,6 +936,7 @@ cudaError_t finalize_splitters(uint64_t* splitters, int nsplit, cudaStream_t str
   if (nsplit <= 1) return cudaSuccess;
   if (nsplit > 8192) return cudaErrorInvalidValue;
   k_finalize_splitters<<<1, 1024, 0, stream>>>(splitters, nsplit);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -852,10 +954,12 @@ cudaError_t l1_count(const HsortParams& p, int lookup_kind, const uint64_t* spli
     size_t sm = lookup_smem_bytes<LOOKUP_LEARNED>(nbuckets, &m) + 4 * (size_t)nbuckets;
     if ((e = set_smem((const void*)k_l1_count<LOOKUP_LEARNED>, sm)) != cudaSuccess) return e;
     k_l1_count<LOOKUP_LEARNED><<<g, kThreads, sm, stream>>>(p, splitters, nbuckets, m, counts, stats);
+    note_launches(1);
   } else {
     size_t sm = lookup_smem_bytes<LOOKUP_PLAIN>(nbuckets, &m) + 4 * (size_t)nbuckets;
     if ((e = set_smem((const void*)k_l1_count<LOOKUP_PLAIN>, sm)) != cudaSuccess) return e;
     k_l1_count<LOOKUP_PLAIN><<<g, kThreads, sm, stream>>>(p, splitters, nbuckets, m, counts, stats);
+    note_launches(1);
   }
   return cudaGetLastError();
 }
@@ -871,14 +975,16 @@ cudaError_t l1_scatter(const HsortParams& p, int lookup_kind, const uint64_t* sp
       size_t sm = l1_scatter_smem<EW, LOOKUP_LEARNED>(nbuckets, &m);
       e = set_smem((const void*)k_l1_scatter<EW, LOOKUP_LEARNED>, sm);
       if (e == cudaSuccess)
-        k_l1_scatter<EW, LOOKUP_LEARNED><<<g, kThreads, sm, stream>>>(p, splitters, nbuckets, m, offsets,
-                                                                       stats);
+        k_l1_scatter<EW, LOOKUP_LEARNED><<<num_sms(), kThreads, sm, stream>>>(p, splitters, nbuckets, m,
+                                                                               offsets, g, stats);
+      note_launches(1);
     } else {
       size_t sm = l1_scatter_smem<EW, LOOKUP_PLAIN>(nbuckets, &m);
       e = set_smem((const void*)k_l1_scatter<EW, LOOKUP_PLAIN>, sm);
       if (e == cudaSuccess)
-        k_l1_scatter<EW, LOOKUP_PLAIN><<<g, kThreads, sm, stream>>>(p, splitters, nbuckets, m, offsets,
-                                                                     stats);
+        k_l1_scatter<EW, LOOKUP_PLAIN><<<num_sms(), kThreads, sm, stream>>>(p, splitters, nbuckets, m,
+                                                                             offsets, g, stats);
+      note_launches(1);
     }
   });
   if (!ok) return cudaErrorInvalidValue;
@@ -886,27 +992,58 @@ cudaError_t l1_scatter(const HsortParams& p, int lookup_kind, const uint64_t* sp
   return cudaGetLastError();
 }
 
-cudaError_t build_tasks(const uint32_t* offsets, int grid, const uint64_t* splitters, int nbuckets,
-                        uint32_t n, SortTask* tasks, uint32_t* ntasks, uint32_t cap, uint32_t* err,
-                        uint32_t* stats, cudaStream_t stream) {
-  k_build_tasks<<<(nbuckets + 255) / 256, 256, 0, stream>>>(offsets, grid, splitters, nbuckets, n, tasks,
-                                                            ntasks, cap, err, stats);
+static TaskLists lists_of(const TaskListsHost& h) {
+  TaskLists L;
+  L.split_in = h.split_in;
+  L.nsplit_in = h.nsplit_in;
+  L.split_out = h.split_out;
+  L.nsplit_out = h.nsplit_out;
+  L.local = h.local;
+  L.nlocal = h.nlocal;
+  L.cap_split = h.cap_split;
+  L.cap_local = h.cap_local;
+  return L;
+}
+
+cudaError_t build_tasks(const uint32_t* offsets, int grid, const uint64_t* splitters, int nbuckets, uint32_t n,
+                        const TaskListsHost& lists, uint32_t* err, uint32_t* stats, cudaStream_t stream) {
+  k_build_tasks<<<(nbuckets + 255) / 256, 256, 0, stream>>>(offsets, grid, splitters, nbuckets, n, lists_of(lists),
+                                                            err, stats);
+  note_launches(1);
   return cudaGetLastError();
 }
 
+int split_grid() { return num_sms(); }
+int local_grid() { return num_sms() * 2; }
 
-cudaError_t run_tasks(const HsortParams& p, const SortTask* tasks_in, const uint32_t* ntasks_in,
-                      SortTask* tasks_out, uint32_t* ntasks_out, uint32_t cap, uint32_t* work_counter,
-                      uint32_t* stats, uint32_t* err, cudaStream_t stream) {
+cudaError_t run_split_round(const HsortParams& p, const TaskListsHost& lists, uint32_t* work_counter,
+                            uint32_t* stats, uint32_t* err, cudaStream_t stream) {
   cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(uint32_t), stream);
   if (e != cudaSuccess) return e;
   bool ok = dispatch_ew(p.elsize, [&](auto ewc) {
     constexpr int EW = decltype(ewc)::value;
-    size_t sm = sizeof(EngineSmem);
-    e = set_smem((const void*)k_tasks<EW>, sm);
+    size_t sm = sizeof(SplitSmem);
+    e = set_smem((const void*)k_split<EW>, sm);
     if (e == cudaSuccess)
-      k_tasks<EW><<<task_engine_grid(), kThreads, sm, stream>>>(p, tasks_in, ntasks_in, tasks_out, ntasks_out,
-                                                                 cap, work_counter, stats, err);
+      k_split<EW><<<split_grid(), kThreads, sm, stream>>>(p, lists_of(lists), work_counter, stats, err);
+    note_launches(1);
+  });
+  if (!ok) return cudaErrorInvalidValue;
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+cudaError_t run_local(const HsortParams& p, const SortTask* tasks, const uint32_t* ntasks, uint32_t cap,
+                      uint32_t* work_counter, uint32_t* stats, cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return e;
+  bool ok = dispatch_ew(p.elsize, [&](auto ewc) {
+    constexpr int EW = decltype(ewc)::value;
+    size_t sm = sizeof(LocalSmem);
+    e = set_smem((const void*)k_local<EW>, sm);
+    if (e == cudaSuccess)
+      k_local<EW><<<local_grid(), kThreads, sm, stream>>>(p, tasks, ntasks, cap, work_counter, stats);
+    note_launches(1);
   });
   if (!ok) return cudaErrorInvalidValue;
   if (e != cudaSuccess) return e;

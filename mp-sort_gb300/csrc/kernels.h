@@ -12,6 +12,11 @@
 
 namespace gb {
 
+// Count of kernels this library has enqueued (every wrapper below adds the
+// launches it made); read before and after a sort for its launch count.
+void note_launches(int k);
+unsigned long long launch_count();
+
 // ---- scan.cu --------------------------------------------------------------
 // Exclusive prefix sum of n uint32 values (n <= 2^24); `tmp` needs
 // scan_tmp_words(n) words.  out may alias in.
@@ -97,15 +102,24 @@ cudaError_t l1_count(const HsortParams& p, int lookup, const uint64_t* splitters
                      const void* model, uint32_t* counts, uint32_t* stats, cudaStream_t stream);
 cudaError_t l1_scatter(const HsortParams& p, int lookup, const uint64_t* splitters, int nbuckets,
                        const void* model, const uint32_t* offsets, uint32_t* stats, cudaStream_t stream);
-// Level-2 tasks from the level-1 buckets.
+// Level-2 task lists (device memory).  A split round consumes split_in and
+// appends to split_out and local; build_tasks appends to split_out and local.
+struct TaskListsHost {
+  const SortTask* split_in;
+  const uint32_t* nsplit_in;
+  SortTask* split_out;
+  uint32_t* nsplit_out;
+  SortTask* local;
+  uint32_t* nlocal;
+  uint32_t cap_split;
+  uint32_t cap_local;
+};
 cudaError_t build_tasks(const uint32_t* offsets, int grid, const uint64_t* splitters, int nbuckets,
-                        uint32_t n, SortTask* tasks, uint32_t* ntasks, uint32_t cap,
-                        uint32_t* err, uint32_t* stats, cudaStream_t stream);
-// One round of the persistent task engine: consumes tasks_in, appends
-// oversize sub-buckets to tasks_out.
-int task_engine_grid();
-cudaError_t run_tasks(const HsortParams& p, const SortTask* tasks_in, const uint32_t* ntasks_in,
-                      SortTask* tasks_out, uint32_t* ntasks_out, uint32_t cap, uint32_t* work_counter,
-                      uint32_t* stats, uint32_t* err, cudaStream_t stream);
+                        uint32_t n, const TaskListsHost& lists, uint32_t* err, uint32_t* stats,
+                        cudaStream_t stream);
+cudaError_t run_split_round(const HsortParams& p, const TaskListsHost& lists, uint32_t* work_counter,
+                            uint32_t* stats, uint32_t* err, cudaStream_t stream);
+cudaError_t run_local(const HsortParams& p, const SortTask* tasks, const uint32_t* ntasks, uint32_t cap,
+                      uint32_t* work_counter, uint32_t* stats, cudaStream_t stream);
 
 }  // namespace gb

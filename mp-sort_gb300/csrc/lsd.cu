@@ -190,6 +190,7 @@ cudaError_t extract_keys(const void* rec, uint32_t n, uint32_t elsize, const gbs
   for (uint32_t w = 0; w < key.nwords; ++w) aligned4 &= (key.word[w].offset % 4 == 0);
   k_extract_keys<<<blocks_for(n, 256), 256, 0, stream>>>((const uint8_t*)rec, n, elsize, key, aligned4,
                                                           keys, idx);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -197,6 +198,7 @@ cudaError_t radix_bytes_to_keys(const uint8_t* radix, uint32_t n, uint32_t rsize
                                 uint32_t* idx, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   k_radix_bytes<<<blocks_for(n, 256), 256, 0, stream>>>(radix, n, rsize, keys, idx);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -207,6 +209,7 @@ cudaError_t lsd_digit_histograms(const uint64_t* keys, uint32_t n, int nwords, u
   for (int w = 0; w < nwords; ++w)
     k_digit_hist<<<blocks_for(n, kThreads), kThreads, 0, stream>>>(keys + (size_t)w * n, n,
                                                                     hist + (size_t)w * 8 * 256);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -219,6 +222,7 @@ int lsd_grid(uint32_t n) {
 cudaError_t lsd_count(const uint64_t* keys_word, uint32_t n, int shift, uint32_t* counts,
                       cudaStream_t stream) {
   k_lsd_count<<<lsd_grid(n), kThreads, 0, stream>>>(keys_word, n, shift, counts);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -244,6 +248,7 @@ cudaError_t lsd_scatter(const uint64_t* keys_in, const uint32_t* idx_in, uint64_
       return cudaErrorInvalidValue;
   }
 #undef GB_LSD_CASE
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -261,6 +266,7 @@ cudaError_t gather_records(const void* in, void* out, const uint32_t* idx, uint3
     k_gather<uint32_t><<<blocks_for((uint64_t)n * (elsize / 4), 256), 256, 0, stream>>>(i8, o8, idx, n, elsize);
   else
     k_gather<uint8_t><<<blocks_for((uint64_t)n * elsize, 256), 256, 0, stream>>>(i8, o8, idx, n, elsize);
+  note_launches(1);
   return cudaGetLastError();
 }
 

@@ -4,10 +4,16 @@
 // (digit x chunk) matrices of the LSD passes: the device counterpart of the
 // reference's count reductions (mpsort-omp.c:110-121) and displacement
 // arithmetic (mpsort-mpi.c:483-510).
+#include <atomic>
+
 #include "common.cuh"
 #include "kernels.h"
 
 namespace gb {
+
+static std::atomic<unsigned long long> g_launches{0};
+void note_launches(int k) { g_launches.fetch_add((unsigned long long)k, std::memory_order_relaxed); }
+unsigned long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 namespace {
 
@@ -79,6 +85,7 @@ cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n, uint
   k_segment_sums<<<(unsigned)nseg, kThreads, 0, stream>>>(in, n, tmp);
   k_scan_sums<<<1, kThreads, 0, stream>>>(tmp, (int)nseg);
   k_segment_scan<<<(unsigned)nseg, kThreads, 0, stream>>>(in, out, n, tmp);
+  note_launches(3);
   return cudaGetLastError();
 }
 

@@ -204,6 +204,7 @@ cudaError_t segment_ranges(const uint8_t* rec, uint32_t elsize, gbsort_key_word 
                            cudaStream_t st) {
   uint32_t g = nseg < (uint32_t)num_sms() * 8 ? nseg : (uint32_t)num_sms() * 8;
   k_segment_ranges<<<g, kThreads, 0, st>>>(rec, elsize, key, offsets, nseg, tasks, ntasks, cap, err);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -216,6 +217,7 @@ int join_grid(uint32_t na) {
 cudaError_t join_count(const uint8_t* a, uint32_t na, const uint8_t* b, uint32_t nb, uint32_t elsize,
                        gbsort_key_word key, uint32_t* counts, int grid, cudaStream_t st) {
   k_join_count<<<grid, kThreads, 0, st>>>(a, na, b, nb, elsize, key, counts);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -223,6 +225,7 @@ cudaError_t join_write(const uint8_t* a, uint32_t na, const uint8_t* b, uint32_t
                        gbsort_key_word key, const uint32_t* offsets, int grid, uint64_t* pa, uint64_t* pb,
                        uint64_t* npairs, cudaStream_t st) {
   k_join_write<<<grid, kThreads, 0, st>>>(a, na, b, nb, elsize, key, offsets, pa, pb, npairs);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -233,6 +236,7 @@ cudaError_t probe_buckets(const uint64_t* keys, uint32_t nkeys, const uint64_t* 
   if (g > 4096) g = 4096;
   if (g == 0) return cudaSuccess;
   k_probe_buckets<<<g, 256, 0, st>>>(keys, nkeys, S, m, learned, search, misses);
+  note_launches(1);
   return cudaGetLastError();
 }
 

@@ -37,10 +37,14 @@ class Stats(ctypes.Structure):
                 ("bigbin_passes", ctypes.c_uint32), ("window_misses", ctypes.c_uint32),
                 ("max_bucket", ctypes.c_uint32), ("lsd_passes", ctypes.c_uint32),
                 ("widest_window", ctypes.c_uint32), ("model_loss", ctypes.c_float),
-                ("reserved", ctypes.c_uint32 * 4)]
+                ("stage_ms", ctypes.c_float * 6), ("launches", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 3)]
+
+    STAGES = ("splitters", "count", "scan", "scatter", "split", "local")
 
     def as_dict(self):
-        d = {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("reserved", "stage_ms")}
+        d["stage_ms"] = {k: round(float(v), 4) for k, v in zip(self.STAGES, self.stage_ms)}
         d["method"] = METHOD_NAMES.get(self.method, self.method)
         return d
 

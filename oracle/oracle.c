@@ -19,8 +19,9 @@
  *   a10 _solve_for_layout                 mpsort-omp.c:143-218
  *   a11 exchange + second local sort      mpsort-omp.c:336-389
  *
- * The "threads" of mpsort_omp run one after another here, so the result is
- * deterministic for any task count.  Errors are returned, never abort().
+ * The tasks of mpsort_omp run on OpenMP threads when this file is built with
+ * -fopenmp (oracle/Makefile does), else one after another; the result is the
+ * same either way.  Errors are returned, never abort().
  */
 #include <stdint.h>
 #include <stdlib.h>
@@ -364,14 +365,21 @@ int oracle_mpsort_tasks(void *base, size_t n, size_t elsize, oracle_radix_fn rad
 
     for (i = 0; i < T; i++) C[i + 1] = (int64_t)(n * (size_t)(i + 1) / (size_t)T);
 
-    /* first local sort of every chunk, then the global min / max radix */
-    for (t = 0; t < T; t++) {
-        size_t lo = n * (size_t)t / (size_t)T, hi = n * (size_t)(t + 1) / (size_t)T;
-        if (oracle_radix_sort(rec + lo * elsize, hi - lo, elsize, radix, rsize, arg)) goto out;
+    /* first local sort of every chunk (the tasks run on OpenMP threads when
+     * built with -fopenmp, as mpsort_omp's do), then the min / max radix */
+    {
+        int fail = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : fail)
+        for (t = 0; t < T; t++) {
+            size_t lo = n * (size_t)t / (size_t)T, hi = n * (size_t)(t + 1) / (size_t)T;
+            if (oracle_radix_sort(rec + lo * elsize, hi - lo, elsize, radix, rsize, arg)) fail = 1;
+        }
+        if (fail) goto out;
     }
     {
-        size_t k;
-        for (k = 0; k < n; k++) radix(rec + k * elsize, radixbuf + k * rsize, arg);
+        long k;
+#pragma omp parallel for schedule(static)
+        for (k = 0; k < (long)n; k++) radix(rec + (size_t)k * elsize, radixbuf + (size_t)k * rsize, arg);
     }
     for (t = 0; t < T; t++) {
         size_t lo = n * (size_t)t / (size_t)T, hi = n * (size_t)(t + 1) / (size_t)T;
@@ -395,15 +403,22 @@ int oracle_mpsort_tasks(void *base, size_t n, size_t elsize, oracle_radix_fn rad
         piter_bisect(&pi, P);
         memset(CLT, 0, T1 * sizeof(int64_t));
         memset(CLE, 0, T1 * sizeof(int64_t));
+#pragma omp parallel for schedule(static)
         for (t = 0; t < T; t++) {
             size_t lo = n * (size_t)t / (size_t)T, hi = n * (size_t)(t + 1) / (size_t)T;
-            oracle_histogram(P, T - 1, radixbuf + lo * rsize, hi - lo, rsize, myCLT, myCLE);
-            for (i = 0; i < T1; i++) { CLT[i] += myCLT[i]; CLE[i] += myCLE[i]; }
+            oracle_histogram(P, T - 1, radixbuf + lo * rsize, hi - lo, rsize,
+                             GL_CLT + (size_t)t * T1, GL_CLE + (size_t)t * T1);
         }
+        for (t = 0; t < T; t++)     /* _reduce_sum, in task order */
+            for (i = 0; i < T1; i++) {
+                CLT[i] += GL_CLT[(size_t)t * T1 + i];
+                CLE[i] += GL_CLE[(size_t)t * T1 + i];
+            }
         piter_accept(&pi, P, C, CLT, CLE);
     } while (!piter_done(&pi));
 
     /* final per-task brackets, layout and exchange (mpsort-omp.c:315-369) */
+#pragma omp parallel for schedule(static)
     for (t = 0; t < T; t++) {
         size_t lo = n * (size_t)t / (size_t)T, hi = n * (size_t)(t + 1) / (size_t)T;
         oracle_histogram(P, T - 1, radixbuf + lo * rsize, hi - lo, rsize,
@@ -411,24 +426,32 @@ int oracle_mpsort_tasks(void *base, size_t n, size_t elsize, oracle_radix_fn rad
     }
     if (oracle_solve_layout(T, C, GL_CLT, GL_CLE, GL_C)) goto out;
     {
-        size_t o = 0;
-        int r, s;
-        for (r = 0; r < T; r++) {
-            for (s = 0; s < T; s++) {
-                size_t slo = n * (size_t)s / (size_t)T;
-                int64_t a = GL_C[(size_t)s * T1 + r], b = GL_C[(size_t)s * T1 + r + 1];
+        int r, bad = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : bad)
+        for (r = 0; r < T; r++) {   /* receiver r gathers its slices, senders in order */
+            size_t o = (size_t)C[r];
+            int s2;
+            for (s2 = 0; s2 < T; s2++) {
+                size_t slo = n * (size_t)s2 / (size_t)T;
+                int64_t a = GL_C[(size_t)s2 * T1 + r], b = GL_C[(size_t)s2 * T1 + r + 1];
                 memcpy(outbuf + o * elsize, rec + (slo + (size_t)a) * elsize,
                        (size_t)(b - a) * elsize);
                 o += (size_t)(b - a);
             }
-            if (o != (size_t)C[r + 1]) goto out;
+            if (o != (size_t)C[r + 1]) bad = 1;
         }
+        if (bad) goto out;
         memcpy(rec, outbuf, n * elsize);
     }
     /* second local sort of every chunk */
-    for (t = 0; t < T; t++) {
-        size_t lo = n * (size_t)t / (size_t)T, hi = n * (size_t)(t + 1) / (size_t)T;
-        if (oracle_radix_sort(rec + lo * elsize, hi - lo, elsize, radix, rsize, arg)) goto out;
+    {
+        int fail = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : fail)
+        for (t = 0; t < T; t++) {
+            size_t lo = n * (size_t)t / (size_t)T, hi = n * (size_t)(t + 1) / (size_t)T;
+            if (oracle_radix_sort(rec + lo * elsize, hi - lo, elsize, radix, rsize, arg)) fail = 1;
+        }
+        if (fail) goto out;
     }
     if (splitters_out && T > 1) memcpy(splitters_out, P, (size_t)(T - 1) * rsize);
     if (iters_out) *iters_out = iters;

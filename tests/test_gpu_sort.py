@@ -113,7 +113,7 @@ def make(dtype, key, n, dist, rng):
     a[key] = k
     for f in a.dtype.names:
         if f != key and a[f].dtype.kind in "iu" and a[f].ndim == 1:
-            a[f] = numpy.arange(n) % numpy.iinfo(a[f].dtype).max
+            a[f] = (numpy.arange(n, dtype=numpy.uint64) % numpy.uint64(1 << 31)).astype(a[f].dtype)
     return a
 
 
