@@ -128,6 +128,25 @@ GBSORT_API int gbsort_debug_buckets(const uint64_t *sample, uint32_t s, int nbuc
 GBSORT_API int gbsort_debug_bisect(const uint64_t *sorted, uint32_t s, int nsplit, uint64_t *splitters,
                         int64_t *clt, int64_t *cle, uint32_t *rounds);
 
+/* Largest sort (nmemb * elsize bytes) gbsort_sort_device_noalloc accepts. */
+#define GBSORT_NOALLOC_MAX_BYTES (8u << 20)
+
+/* The histogram sort without any allocation, for callers that cannot call
+ * cudaMalloc (a framework's caching allocator owns the memory budget, an
+ * allocation would stall a latency-critical path, or running out of memory
+ * half-way is not acceptable).  No counterpart in the reference, which
+ * always allocates its temporaries.  Its scratch space is one fixed device
+ * array inside libgbsort, held by every GPU that loads the library until
+ * the process exits; sorts larger than GBSORT_NOALLOC_MAX_BYTES return
+ * GBSORT_ERR_BAD_ARG.  Same layouts as the histogram sort (one-word key at a
+ * 4-byte offset, 8-64 byte records); the result is the same stable order.
+ * All calls share the array and leave their data in it, so calls whose work
+ * overlaps on the GPU race.  The first call on a device looks up the array's
+ * address with that device current: make it before any stream capture.
+ * Waits for its work on `stream` to finish before returning. */
+GBSORT_API int gbsort_sort_device_noalloc(const void *d_in, void *d_out, size_t nmemb, size_t elsize,
+                                          const gbsort_key_desc *key, void *stream);
+
 GBSORT_API int gbsort_last_stats(gbsort_stats *out);
 GBSORT_API const char *gbsort_status_string(int status);
 GBSORT_API const char *gbsort_last_error(void);

@@ -66,6 +66,7 @@ _I = ctypes.c_int
 # name: (restype, argtypes)
 SIGNATURES = {
     "gbsort_sort_device": (_I, [_P, _P, _SZ, _SZ, _P, _I, _P]),
+    "gbsort_sort_device_noalloc": (_I, [_P, _P, _SZ, _SZ, _P, _P]),
     "gbsort_sort_host": (_I, [_P, _P, _SZ, _SZ, _P, _I]),
     "gbsort_sort_radix_host": (_I, [_P, _SZ, _SZ, _P, _SZ, _P]),
     "gbsort_sort_segments_device": (_I, [_P, _P, _P, _SZ, _SZ, _P, _I, _P]),
