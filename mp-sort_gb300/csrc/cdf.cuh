@@ -10,8 +10,9 @@
 //   learned -- a monotone piecewise-linear CDF F of the key predicts
 //              g = floor(F(key) * nbuckets); a per-leaf window [g-dlo, g+dhi],
 //              computed exactly from the splitters, brackets t, and a short
-//              search inside it finishes.  If a window ever misses, the full
-//              search runs and a counter records it; the result is t either way.
+//              search inside it finishes (no search at all for a zero window).
+//              If a window ever misses, the full search runs and a counter
+//              records it; the result is t either way.
 //
 // The model: L = 2^lbits leaves uniform in (key - kmin) >> lshift; leaf j
 // interpolates linearly between knots y[j] and y[j+1] (fp32, trained on
@@ -87,6 +88,10 @@ __device__ __forceinline__ uint32_t bucket_learned(const uint64_t* S, const Mode
   uint32_t leaf, g;
   model_predict(key, m.kmin, m.lshift, m.lbits, m.nbuckets, knots, leaf, g);
   const uint32_t w = win[leaf];
+  // a zero window means the prediction equals the true bucket at every key
+  // of the leaf (the windows are exact maxima over the leaf), so no splitter
+  // needs to be read
+  if (w == 0) return g;
   const uint32_t nsplit = (uint32_t)(m.nbuckets - 1);
   uint32_t lo = g > (w >> 16) ? g - (w >> 16) : 0u;
   uint32_t hi = min(g + (w & 0xffffu), nsplit);

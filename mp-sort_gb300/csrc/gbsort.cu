@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -274,11 +275,21 @@ struct HsortRun {
   uint32_t sample = 0;
 };
 
+// Level-1 bucket count: about 2048 records per bucket, at most 2048 (or
+// GBSORT_MAX_BUCKETS, a power of two up to 8192, when set).  Fewer, larger
+// buckets keep the scatter's runs long enough to fill whole DRAM sectors;
+// the bucket splits then carry more of the work.
 int choose_buckets(uint32_t n) {
   if (n <= 4096) return 1;
+  static int cap = -1;
+  if (cap < 0) {
+    const char* e = getenv("GBSORT_MAX_BUCKETS");
+    int v = e ? atoi(e) : 0;
+    cap = (v >= 2 && v <= 8192 && (v & (v - 1)) == 0) ? v : 2048;
+  }
   uint64_t want = ((uint64_t)n + 2047) / 2048;
   uint32_t nb = pow2_ceil(want);
-  return (int)std::min<uint32_t>(nb, 8192);
+  return (int)std::min<uint32_t>(nb, (uint32_t)cap);
 }
 
 // Device task lists of level 2 and their counters.

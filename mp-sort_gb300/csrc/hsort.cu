@@ -64,6 +64,26 @@ struct RecIO {
       for (int i = 0; i < EW; ++i) r[i] = reinterpret_cast<const uint32_t*>(p)[i];
     }
   }
+  // Same, for data read exactly once: evict-first, so the stream does not
+  // push out of L2 the partly written bucket lines of the scatter.
+  __device__ __forceinline__ static void load_stream(const uint8_t* p, uint32_t (&r)[EW]) {
+    if constexpr (EW % 4 == 0) {
+#pragma unroll
+      for (int i = 0; i < EW / 4; ++i) {
+        uint4 v = __ldcs(reinterpret_cast<const uint4*>(p) + i);
+        r[4 * i] = v.x; r[4 * i + 1] = v.y; r[4 * i + 2] = v.z; r[4 * i + 3] = v.w;
+      }
+    } else if constexpr (EW % 2 == 0) {
+#pragma unroll
+      for (int i = 0; i < EW / 2; ++i) {
+        uint2 v = __ldcs(reinterpret_cast<const uint2*>(p) + i);
+        r[2 * i] = v.x; r[2 * i + 1] = v.y;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < EW; ++i) r[i] = __ldcs(reinterpret_cast<const unsigned int*>(p) + i);
+    }
+  }
   __device__ __forceinline__ static void store(uint8_t* p, const uint32_t (&r)[EW]) {
     if constexpr (EW % 4 == 0) {
 #pragma unroll
@@ -276,7 +296,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_count(HsortParams p, const u
 // --------------------------------------------------- level-1 scatter ------
 template <int EW>
 struct Tile {
-  static constexpr int kRpt = (32 / EW) < 1 ? 1 : ((32 / EW) > 8 ? 8 : (32 / EW));
+  static constexpr int kRpt = (16 / EW) < 1 ? 1 : ((16 / EW) > 4 ? 4 : (16 / EW));
   static constexpr int kSize = kThreads * kRpt;
 };
 
@@ -286,20 +306,21 @@ struct Tile {
 // bucket's run of the tile; cursors start at the scanned (bucket, chunk)
 // offsets, so chunk order and tile order are both preserved.
 template <int EW, int LK>
-__global__ void __launch_bounds__(kThreads, 1) k_l1_scatter(HsortParams p, const uint64_t* __restrict__ S,
+__global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const uint64_t* __restrict__ S,
                                                              int nbuckets, ModelDev model,
                                                              const uint32_t* __restrict__ offsets,
                                                              int nchunks, uint32_t* __restrict__ stats) {
   uint32_t* err = stats + STAT_SLOTS;  // the error word follows the statistics
   constexpr int RPT = Tile<EW>::kRpt, T = Tile<EW>::kSize;
   using Rank = BlockRank<RPT, 7>;
+  using Rank8 = BlockRank<RPT, 8>;
   extern __shared__ __align__(16) uint8_t smem[];
   LookupSmem L;
   uint8_t* q = load_lookup<LK>(smem, S, nbuckets, model, L);
   uint32_t* cursor = reinterpret_cast<uint32_t*>(q);
   q += 4 * (size_t)((nbuckets + 3) & ~3);
   uint16_t* hist = reinterpret_cast<uint16_t*>(q);
-  q += 2 * Rank::kCounters;
+  q += 2 * Rank8::kCounters;
   uint16_t* bsorted = reinterpret_cast<uint16_t*>(q);
   q += 2 * T;
   uint16_t* fpos = reinterpret_cast<uint16_t*>(q);
@@ -310,7 +331,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_l1_scatter(HsortParams p, const
 
   const uint32_t w = warp_id(), lane = lane_id();
   const uint32_t E = EW * 4;
-  const bool two_pass = nbuckets > 128;
+  const bool two_pass = nbuckets > 256;
   // the count kernel's chunks, several per CTA
   for (uint32_t c = blockIdx.x; c < (uint32_t)nchunks; c += gridDim.x) {
   const uint32_t g = (uint32_t)nchunks;
@@ -324,7 +345,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_l1_scatter(HsortParams p, const
 #pragma unroll
   for (int r = 0; r < RPT; ++r) {
     uint32_t e = w * 32 * RPT + r * 32 + lane;
-    if (cb + e < ce) RecIO<EW>::load(p.in + (size_t)(cb + e) * E, nxt[r]);
+    if (cb + e < ce) RecIO<EW>::load_stream(p.in + (size_t)(cb + e) * E, nxt[r]);
   }
   for (uint32_t t0 = cb; t0 < ce; t0 += T) {
     const uint32_t nvalid = min((uint32_t)T, ce - t0);
@@ -335,7 +356,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_l1_scatter(HsortParams p, const
 #pragma unroll
       for (int q2 = 0; q2 < EW; ++q2) rec[r][q2] = nxt[r][q2];
       uint32_t e = t0 + T + w * 32 * RPT + r * 32 + lane;
-      if (e < ce) RecIO<EW>::load(p.in + (size_t)e * E, nxt[r]);
+      if (e < ce) RecIO<EW>::load_stream(p.in + (size_t)e * E, nxt[r]);
     }
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
@@ -348,8 +369,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_l1_scatter(HsortParams p, const
       }
       dig[r] = bkt[r] & 127u;
     }
-    Rank::rank(dig, pos, hist, scan_tmp, nullptr);
-    if (two_pass) {
+    if (!two_pass) {
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) dig[r] = bkt[r] > 255u ? 255u : bkt[r];
+      Rank8::rank(dig, pos, hist, scan_tmp, nullptr);
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) bfinal[pos[r]] = (uint16_t)bkt[r];
+      __syncthreads();
+    } else {
+      Rank::rank(dig, pos, hist, scan_tmp, nullptr);
 #pragma unroll
       for (int r = 0; r < RPT; ++r) bsorted[pos[r]] = (uint16_t)bkt[r];
       __syncthreads();
@@ -370,10 +398,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_l1_scatter(HsortParams p, const
       __syncthreads();
 #pragma unroll
       for (int r = 0; r < RPT; ++r) pos[r] = fpos[pos[r]];
-    } else {
-#pragma unroll
-      for (int r = 0; r < RPT; ++r) bfinal[pos[r]] = (uint16_t)bkt[r];
-      __syncthreads();
     }
     // run heads turn cursor[b] into cursor[b] - head_position
     for (uint32_t i = threadIdx.x; i < nvalid; i += kThreads) {
@@ -403,9 +427,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_l1_scatter(HsortParams p, const
 
 template <int EW, int LK>
 size_t l1_scatter_smem(int nbuckets, const ModelDev* m) {
-  using Rank = BlockRank<Tile<EW>::kRpt, 7>;
+  using Rank8 = BlockRank<Tile<EW>::kRpt, 8>;
   return lookup_smem_bytes<LK>(nbuckets, m) + 4 * (size_t)((nbuckets + 3) & ~3) +
-         2 * Rank::kCounters + 3 * 2 * (size_t)Tile<EW>::kSize;
+         2 * Rank8::kCounters + 3 * 2 * (size_t)Tile<EW>::kSize;
 }
 
 // ------------------------------------------------------------- tasks -----
@@ -497,6 +521,7 @@ struct LocalSmem {
   uint64_t red[2 * kWarps];
   uint32_t scan_tmp[kWarps];
   uint32_t task_id;
+  SortTask next;
 };
 struct SplitSmem {
   uint32_t hist[kSplitBins];
@@ -509,6 +534,7 @@ struct SplitSmem {
   uint32_t gfirst[kMaxGroups + 1];
   uint32_t scan_tmp[kWarps];
   uint32_t task_id;
+  SortTask next;
 };
 
 __device__ __forceinline__ void block_minmax(uint64_t& mn, uint64_t& mx, uint64_t* red) {
@@ -533,10 +559,13 @@ __device__ __forceinline__ void block_minmax(uint64_t& mn, uint64_t& mx, uint64_
   __syncthreads();
 }
 
-// One MSD counting pass over positions [a, a+s) of keyA / idxA: stable by
-// (key - mn) >> shift into keyB / idxB at [a, a+s); small bins are then
-// insertion-sorted there and large bins queued for another pass.  Keys stay
-// in shared memory, so the pass needs few registers.
+// One MSD counting pass over positions [a, a+s) of keyA / idxA, in place:
+// a stable counting sort by (key - mn) >> shift into keyB / idxB, then every
+// element of a small bin takes its place by counting the bin's members with
+// a smaller (key, input index) and is written back to keyA / idxA.  That
+// step is one element per thread, so a large bin costs its own threads only.
+// Elements of bins above kInsertMax go back unchanged and their bins are
+// queued for another pass.  Keys stay in shared memory (few registers).
 __device__ void local_msd_pass(LocalSmem& sm, uint32_t a, uint32_t s, uint64_t mn, uint64_t mx) {
   using Rank = BlockRank<kLocalRpt, kLocalBits>;
   const uint32_t w = warp_id(), lane = lane_id();
@@ -558,30 +587,27 @@ __device__ void local_msd_pass(LocalSmem& sm, uint32_t a, uint32_t s, uint64_t m
     }
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < (1 << kLocalBits); d += kThreads) {
-    uint32_t b0 = sm.start[d], b1 = min(sm.start[d + 1], s);
-    if (b1 <= b0 + 1) continue;
-    uint32_t sz = b1 - b0;
+  for (uint32_t i = threadIdx.x; i < s; i += kThreads) {
+    const uint64_t kv = sm.keyB[a + i];
+    const uint16_t iv = sm.idxB[a + i];
+    const uint32_t d = (uint32_t)((kv - mn) >> shift);
+    const uint32_t b0 = sm.start[d], b1 = min(sm.start[d + 1], s);
+    const uint32_t sz = b1 - b0;
+    uint32_t at = i;
     if (sz <= (uint32_t)kInsertMax) {
-      uint64_t* key = sm.keyB + a + b0;
-      uint16_t* idx = sm.idxB + a + b0;
-      for (uint32_t i = 1; i < sz; ++i) {
-        uint64_t kv = key[i];
-        uint16_t iv = idx[i];
-        uint32_t j = i;
-        while (j > 0 && key[j - 1] > kv) {
-          key[j] = key[j - 1];
-          idx[j] = idx[j - 1];
-          --j;
-        }
-        key[j] = kv;
-        idx[j] = iv;
+      uint32_t r = 0;
+      for (uint32_t j = b0; j < b1; ++j) {
+        const uint64_t kj = sm.keyB[a + j];
+        r += (kj < kv) || (kj == kv && sm.idxB[a + j] < iv);
       }
-    } else {
-      uint32_t at = atomicAdd(&sm.nbig, 1u);
-      sm.big[at] = (uint16_t)(a + b0);
-      sm.bigsz[at] = (uint16_t)sz;
+      at = b0 + r;
+    } else if (i == b0) {
+      uint32_t q = atomicAdd(&sm.nbig, 1u);
+      sm.big[q] = (uint16_t)(a + b0);
+      sm.bigsz[q] = (uint16_t)sz;
     }
+    sm.keyA[a + at] = kv;
+    sm.idxA[a + at] = iv;
   }
   __syncthreads();
 }
@@ -629,9 +655,7 @@ __device__ void local_sort(LocalSmem& sm, const uint8_t* src, uint8_t* dst, uint
     if (threadIdx.x == 0) sm.nbig = nb - 1;
     uint64_t bmn = ~0ull, bmx = 0;
     for (uint32_t e = threadIdx.x; e < s; e += kThreads) {
-      uint64_t kv = sm.keyB[a + e];
-      sm.keyA[a + e] = kv;
-      sm.idxA[a + e] = sm.idxB[a + e];
+      uint64_t kv = sm.keyA[a + e];
       bmn = kv < bmn ? kv : bmn;
       bmx = kv > bmx ? kv : bmx;
     }
@@ -652,7 +676,7 @@ __device__ void local_sort(LocalSmem& sm, const uint8_t* src, uint8_t* dst, uint
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         uint32_t f = f0 + u * kThreads;
-        if (f < nv) v[u] = reinterpret_cast<const V*>(src + (size_t)sm.idxB[f / VPR] * E)[f % VPR];
+        if (f < nv) v[u] = reinterpret_cast<const V*>(src + (size_t)sm.idxA[f / VPR] * E)[f % VPR];
       }
 #pragma unroll
       for (int u = 0; u < U; ++u) {
@@ -741,7 +765,9 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
   // group of a bin = slot of its midpoint: a bin holding most of the records
   // never shares a group with the empty bins on either side, so every group
   // that is split again covers a strictly narrower key range
-  const uint32_t target = max((uint32_t)(kLocalMax / 2), (m + kMaxGroups - 1) / kMaxGroups);
+  // target <= m / 2 keeps the first and the last bin's midpoints at least a
+  // target apart, so no group spans every bin: each re-split narrows
+  const uint32_t target = min(max((uint32_t)(kLocalMax - kLocalMax / 8), (m + kMaxGroups - 1) / kMaxGroups), m / 2);
   for (uint32_t b = threadIdx.x; b < (uint32_t)kSplitBins; b += kThreads) {
     uint32_t gb_ = kMaxGroups - 1;
     if (b < nbins) {
@@ -829,18 +855,22 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
 }
 
 template <int EW>
-__global__ void __launch_bounds__(kThreads, 1) k_split(HsortParams p, TaskLists L, uint32_t* __restrict__ work,
+__global__ void __launch_bounds__(kThreads, 2) k_split(HsortParams p, TaskLists L, uint32_t* __restrict__ work,
                                                         uint32_t* __restrict__ stats, uint32_t* __restrict__ err) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   SplitSmem& sm = *reinterpret_cast<SplitSmem*>(smem_raw);
   const uint32_t nt = min(*L.nsplit_in, L.cap_split);
   for (;;) {
-    if (threadIdx.x == 0) sm.task_id = atomicAdd(work, 1u);
+    if (threadIdx.x == 0) {
+      uint32_t id = atomicAdd(work, 1u);
+      sm.task_id = id;
+      if (id < nt) sm.next = L.split_in[id];
+    }
     __syncthreads();
     const uint32_t t = sm.task_id;
+    const SortTask task = sm.next;
     __syncthreads();
     if (t >= nt) break;
-    const SortTask task = L.split_in[t];
     if (task.kind == TASK_COPY || task.count <= (uint32_t)kLocalMax) {  // forwarded as is
       if (threadIdx.x == 0) push(L.local, L.nlocal, L.cap_local, task, err);
       continue;
@@ -858,13 +888,25 @@ __global__ void __launch_bounds__(kThreads, 2) k_local(HsortParams p, const Sort
   LocalSmem& sm = *reinterpret_cast<LocalSmem*>(smem_raw);
   constexpr uint32_t E = EW * 4;
   const uint32_t nt = min(*ntasks, cap);
+  // thread 0 claims the next task while the current one is sorted, so the
+  // claim (a global atomic) and the descriptor load overlap with work
+  if (threadIdx.x == 0) {
+    uint32_t id = atomicAdd(work, 1u);
+    sm.task_id = id;
+    if (id < nt) sm.next = tasks[id];
+  }
+  __syncthreads();
   for (;;) {
-    if (threadIdx.x == 0) sm.task_id = atomicAdd(work, 1u);
-    __syncthreads();
     const uint32_t t = sm.task_id;
-    __syncthreads();
     if (t >= nt) break;
-    const SortTask task = tasks[t];
+    const SortTask task = sm.next;
+    __syncthreads();
+    uint32_t nid = 0;
+    SortTask nxt{};
+    if (threadIdx.x == 0) {
+      nid = atomicAdd(work, 1u);
+      if (nid < nt) nxt = tasks[nid];
+    }
     const uint8_t* src = (task.src ? p.bufB : p.bufA) + (size_t)task.start * E;
     uint8_t* out = p.out + (size_t)task.start * E;
     if (task.kind == TASK_COPY || task.count == 1) {
@@ -875,6 +917,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_local(HsortParams p, const Sort
       local_sort<EW>(sm, src, out, task.count, p.key, stats);
       if (threadIdx.x == 0) atomicAdd(stats + STAT_LOCAL, 1u);
     }
+    if (threadIdx.x == 0) {
+      sm.task_id = nid;
+      sm.next = nxt;
+    }
+    __syncthreads();
   }
 }
 
@@ -940,8 +987,9 @@ cudaError_t finalize_splitters(uint64_t* splitters, int nsplit, cudaStream_t str
   return cudaGetLastError();
 }
 
+// Opt the kernel in to `bytes` of dynamic shared memory (needed above 48 KB
+// of dynamic plus static shared memory; harmless below).
 static cudaError_t set_smem(const void* fn, size_t bytes) {
-  if (bytes <= 48 * 1024) return cudaSuccess;
   return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
@@ -975,14 +1023,14 @@ cudaError_t l1_scatter(const HsortParams& p, int lookup_kind, const uint64_t* sp
       size_t sm = l1_scatter_smem<EW, LOOKUP_LEARNED>(nbuckets, &m);
       e = set_smem((const void*)k_l1_scatter<EW, LOOKUP_LEARNED>, sm);
       if (e == cudaSuccess)
-        k_l1_scatter<EW, LOOKUP_LEARNED><<<num_sms(), kThreads, sm, stream>>>(p, splitters, nbuckets, m,
+        k_l1_scatter<EW, LOOKUP_LEARNED><<<g, kThreads, sm, stream>>>(p, splitters, nbuckets, m,
                                                                                offsets, g, stats);
       note_launches(1);
     } else {
       size_t sm = l1_scatter_smem<EW, LOOKUP_PLAIN>(nbuckets, &m);
       e = set_smem((const void*)k_l1_scatter<EW, LOOKUP_PLAIN>, sm);
       if (e == cudaSuccess)
-        k_l1_scatter<EW, LOOKUP_PLAIN><<<num_sms(), kThreads, sm, stream>>>(p, splitters, nbuckets, m,
+        k_l1_scatter<EW, LOOKUP_PLAIN><<<g, kThreads, sm, stream>>>(p, splitters, nbuckets, m,
                                                                              offsets, g, stats);
       note_launches(1);
     }
@@ -1013,7 +1061,7 @@ cudaError_t build_tasks(const uint32_t* offsets, int grid, const uint64_t* split
   return cudaGetLastError();
 }
 
-int split_grid() { return num_sms(); }
+int split_grid() { return num_sms() * 2; }
 int local_grid() { return num_sms() * 2; }
 
 cudaError_t run_split_round(const HsortParams& p, const TaskListsHost& lists, uint32_t* work_counter,
