@@ -30,18 +30,17 @@ METRIC = "sorted records/s (1e9 x 16 B u64-keyed records)"
 UNIT = "records/s"
 DTYPE_DESC = [('key', 'u8'), ('val', 'i8')]
 
-# Algorithmic bytes per record of the dominant kernel (the level-1 bucket
-# scatter reads and writes every record once) and of the whole pipeline
-# (two passes, each a read and a write of every record).
+# Algorithmic bytes per record of the pipeline's kernels: each must read
+# (and, for the last three, also write) every record once.  The pipeline as a
+# whole needs two passes, each a read and a write of every record.
 E = 16
-SCATTER_BYTES_PER_RECORD = 2 * E
+STAGE_KERNELS = {  # stage_ms key -> (kernel, algorithmic bytes per record, ncu summary)
+    "count": ("k_l1_count", E, "l1_count_16B.md"),
+    "scatter": ("k_l1_scatter", 2 * E, "l1_scatter_16B.md"),
+    "split": ("k_split", 2 * E, "split_16B.md"),
+    "local": ("k_local", 2 * E, "local_16B.md"),
+}
 PIPELINE_BYTES_PER_RECORD = 2 * 2 * E
-
-# DRAM bytes per record of the scatter kernel measured by ncu
-# (profiles/l1_scatter_16B.md: dram__bytes_read.sum + dram__bytes_write.sum
-# of one launch on 1e8 records, divided by 1e8; traffic grows in proportion
-# to the records processed).
-SCATTER_NCU_BYTES_PER_RECORD = None
 
 
 def load_peaks():
@@ -54,10 +53,12 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
-def scatter_traffic_per_record():
-    """Per-record DRAM traffic of the scatter kernel from the committed ncu
-    summary (a `bytes_per_record:` line), or None."""
-    path = os.path.join(REPO, "profiles", "l1_scatter_16B.md")
+def ncu_bytes_per_record(summary):
+    """DRAM bytes per record of a kernel from its committed ncu summary
+    under profiles/ (its `bytes_per_record:` line: dram__bytes_read.sum +
+    dram__bytes_write.sum of one launch over 5e7 records, divided by 5e7;
+    the traffic grows in proportion to the records), or None."""
+    path = os.path.join(REPO, "profiles", summary)
     try:
         for line in open(path):
             if line.strip().startswith("bytes_per_record:"):
@@ -254,14 +255,18 @@ def run_ours(args):
         mpsort._lib.lib().gbsort_release()
 
     peak, peak_kind = load_peaks()
-    scat_ms = stage_ms["scatter"]
-    achieved = n * SCATTER_BYTES_PER_RECORD / (scat_ms / 1e3) / 1e9 if scat_ms > 0 else None
-    tpr = scatter_traffic_per_record()
-    roofline = {"bound": "hbm", "kernel": "k_l1_scatter (level-1 bucket scatter)",
-                "achieved": achieved, "peak": peak, "unit": "GB/s",
+    # the dominant kernel: the stage with the most device time per sort
+    dom = max(STAGE_KERNELS, key=lambda k: stage_ms.get(k, 0.0))
+    kname, alg_bpr, summary = STAGE_KERNELS[dom]
+    dom_ms = stage_ms[dom]
+    achieved = n * alg_bpr / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
+    tpr = ncu_bytes_per_record(summary)
+    roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if achieved else None, "peak_kind": peak_kind,
                 "traffic": tpr * n if tpr else None,
-                "algorithmic_bytes_per_launch": n * SCATTER_BYTES_PER_RECORD,
+                "algorithmic_bytes_per_launch": n * alg_bpr,
+                "per_stage_frac": {k: (n * STAGE_KERNELS[k][1] / (stage_ms[k] / 1e3) / 1e9 / peak
+                                       if stage_ms.get(k) else None) for k in STAGE_KERNELS},
                 "pipeline_frac": n * PIPELINE_BYTES_PER_RECORD / (ms_per_step / 1e3) / 1e9 / peak}
 
     launches = st.get("launches")
@@ -284,7 +289,7 @@ def run_ours(args):
         "clocks": clk.summary(),
     }
     if rank == 0:
-        line["cpu_baseline"] = cpu_baseline(args)
+        line["cpu_baseline"] = None if args.no_cpu else cpu_baseline(args)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -375,6 +380,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=20_000_000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-compare", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
