@@ -49,7 +49,7 @@ def build(force=False, verbose=False):
 
     def compile_one(job):
         src, obj = job
-        cmd = [nvcc()] + ARCH + FLAGS + ["-c", src, "-o", obj]
+        cmd = [nvcc()] + ARCH + FLAGS + os.environ.get("GBSORT_NVCC_FLAGS", "").split() + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         return src, r.returncode, r.stdout + r.stderr
 

@@ -82,10 +82,11 @@ __device__ __forceinline__ uint64_t key_from_regs(const uint32_t (&r)[E_WORDS], 
 
 __device__ __forceinline__ int bitlen64(uint64_t x) { return x ? 64 - __clzll(x) : 0; }
 
-// Block-wide exclusive scan of one value per thread (kThreads threads).
-// `tmp` holds kWarps entries.  Returns the exclusive prefix; *total gets the sum.
-template <typename T>
+// Block-wide exclusive scan of one value per thread (NT threads).
+// `tmp` holds NT / 32 entries.  Returns the exclusive prefix; *total gets the sum.
+template <typename T, int NT = kThreads>
 __device__ __forceinline__ T block_exclusive_scan(T v, T* tmp, T* total) {
+  constexpr int NW = NT / 32;
   const uint32_t lane = lane_id(), w = warp_id();
   T x = v;
 #pragma unroll
@@ -96,18 +97,18 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T* tmp, T* total) {
   if (lane == 31) tmp[w] = x;
   __syncthreads();
   if (w == 0) {
-    T s = lane < (uint32_t)kWarps ? tmp[lane] : T(0);
+    T s = lane < (uint32_t)NW ? tmp[lane] : T(0);
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       T y = __shfl_up_sync(GB_FULL_MASK, s, o);
       if (lane >= (uint32_t)o) s += y;
     }
-    if (lane < (uint32_t)kWarps) tmp[lane] = s;
+    if (lane < (uint32_t)NW) tmp[lane] = s;
   }
   __syncthreads();
   T warp_prefix = w ? tmp[w - 1] : T(0);
   T result = warp_prefix + x - v;
-  if (total) *total = tmp[kWarps - 1];
+  if (total) *total = tmp[NW - 1];
   __syncthreads();
   return result;
 }
@@ -123,11 +124,12 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T* tmp, T* total) {
 // different digits touch different banks.  Items with valid == false must
 // carry the largest digit; they then land after every valid item.
 // ---------------------------------------------------------------------------
-template <int RPT, int DIGIT_BITS>
+template <int RPT, int DIGIT_BITS, int NT = kThreads>
 struct BlockRank {
+  static constexpr int kNW = NT / 32;
   static constexpr int kDigits = 1 << DIGIT_BITS;
-  static constexpr int kCounters = kDigits * kWarps;
-  static constexpr int kDigitsPerThread = (kDigits + kThreads - 1) / kThreads;
+  static constexpr int kCounters = kDigits * kNW;
+  static constexpr int kDigitsPerThread = (kDigits + NT - 1) / NT;
 
   // ranks[r] receives the position of item r; digit_start (optional, kDigits
   // + 1 entries in shared memory) receives the start of every digit's run.
@@ -135,7 +137,7 @@ struct BlockRank {
                                               uint16_t* hist, uint32_t* scan_tmp,
                                               uint32_t* digit_start) {
     const uint32_t lane = lane_id(), w = warp_id();
-    for (int i = threadIdx.x; i < kCounters; i += kThreads) hist[i] = 0;
+    for (int i = threadIdx.x; i < kCounters; i += NT) hist[i] = 0;
     __syncthreads();
     const uint32_t lt = lanemask_lt();
     uint16_t* wh = hist + w * kDigits;
@@ -151,34 +153,71 @@ struct BlockRank {
     }
     __syncthreads();
     // per digit: exclusive prefix over the warps, then over the digits
-    uint32_t tot[kDigitsPerThread];
-    uint32_t sum = 0;
+    uint32_t total;
+    if constexpr (kDigits >= NT) {
+      uint32_t tot[kDigitsPerThread];
+      uint32_t sum = 0;
 #pragma unroll
-    for (int j = 0; j < kDigitsPerThread; ++j) {
-      const int d = threadIdx.x * kDigitsPerThread + j;
+      for (int j = 0; j < kDigitsPerThread; ++j) {
+        const int d = threadIdx.x * kDigitsPerThread + j;
+        uint32_t run = 0;
+        if (d < kDigits) {
+#pragma unroll
+          for (int q = 0; q < kNW; ++q) {
+            uint32_t c = hist[q * kDigits + d];
+            hist[q * kDigits + d] = (uint16_t)run;
+            run += c;
+          }
+        }
+        tot[j] = run;
+        sum += run;
+      }
+      uint32_t base = block_exclusive_scan<uint32_t, NT>(sum, scan_tmp, &total);
+#pragma unroll
+      for (int j = 0; j < kDigitsPerThread; ++j) {
+        const int d = threadIdx.x * kDigitsPerThread + j;
+        if (d < kDigits) {
+#pragma unroll
+          for (int q = 0; q < kNW; ++q) hist[q * kDigits + d] = (uint16_t)(hist[q * kDigits + d] + base);
+          if (digit_start) digit_start[d] = base;
+        }
+        base += tot[j];
+      }
+    } else {
+      // fewer digits than threads: TPD adjacent lanes share a digit, each
+      // summing kNW / TPD warps, combined with shuffles
+      constexpr int TPD = NT / kDigits;
+      constexpr int WPS = kNW / TPD > 0 ? kNW / TPD : 1;
+      static_assert(TPD <= 32 && (32 % TPD) == 0, "digit groups must tile a warp");
+      const int d = threadIdx.x / TPD, qq = threadIdx.x % TPD;
       uint32_t run = 0;
-      if (d < kDigits) {
+      if (qq * WPS < kNW) {
 #pragma unroll
-        for (int q = 0; q < kWarps; ++q) {
-          uint32_t c = hist[q * kDigits + d];
-          hist[q * kDigits + d] = (uint16_t)run;
+        for (int q = 0; q < WPS; ++q) {
+          const int wq = qq * WPS + q;
+          uint32_t c = hist[wq * kDigits + d];
+          hist[wq * kDigits + d] = (uint16_t)run;
           run += c;
         }
       }
-      tot[j] = run;
-      sum += run;
-    }
-    uint32_t total;
-    uint32_t base = block_exclusive_scan<uint32_t>(sum, scan_tmp, &total);
+      uint32_t incl = run;
 #pragma unroll
-    for (int j = 0; j < kDigitsPerThread; ++j) {
-      const int d = threadIdx.x * kDigitsPerThread + j;
-      if (d < kDigits) {
-#pragma unroll
-        for (int q = 0; q < kWarps; ++q) hist[q * kDigits + d] = (uint16_t)(hist[q * kDigits + d] + base);
-        if (digit_start) digit_start[d] = base;
+      for (int o = 1; o < TPD; o <<= 1) {
+        uint32_t y = __shfl_up_sync(GB_FULL_MASK, incl, o);
+        if (qq >= o) incl += y;
       }
-      base += tot[j];
+      const uint32_t excl = incl - run;
+      const uint32_t dtot = __shfl_sync(GB_FULL_MASK, incl, (lane | (TPD - 1)));
+      uint32_t scan = block_exclusive_scan<uint32_t, NT>(qq == 0 ? dtot : 0u, scan_tmp, &total);
+      const uint32_t base = __shfl_sync(GB_FULL_MASK, scan, lane & ~(uint32_t)(TPD - 1)) + excl;
+      if (qq * WPS < kNW) {
+#pragma unroll
+        for (int q = 0; q < WPS; ++q) {
+          const int wq = qq * WPS + q;
+          hist[wq * kDigits + d] = (uint16_t)(hist[wq * kDigits + d] + base);
+        }
+      }
+      if (digit_start && qq == 0) digit_start[d] = base;
     }
     if (digit_start && threadIdx.x == 0) digit_start[kDigits] = total;
     __syncthreads();

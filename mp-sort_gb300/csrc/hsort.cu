@@ -27,7 +27,11 @@ int num_sms();
 namespace {
 
 constexpr int kLocalMax = 4096;        // records a local sort holds in shared memory
-constexpr int kLocalRpt = kLocalMax / kThreads;
+#ifndef GB_LOCAL_THREADS
+#define GB_LOCAL_THREADS 512
+#endif
+constexpr int kLocalThreads = GB_LOCAL_THREADS;  // threads of a local-sort CTA
+constexpr int kLocalCtasPerSm = 2;
 constexpr int kLocalBits = 9;          // digit of the local MSD pass
 constexpr int kInsertMax = 24;         // bins up to this size use insertion sort
 constexpr int kSplitBits = 12;         // bins of a bucket split
@@ -508,18 +512,20 @@ __device__ __forceinline__ void block_copy_ilp(const uint8_t* src, uint8_t* dst,
   }
 }
 
-struct LocalSmem {
+template <int NT>
+struct LocalSmemT {
+  static constexpr int kNW = NT / 32;
   uint64_t keyA[kLocalMax];  // keys in input order (then staging of big bins)
   uint64_t keyB[kLocalMax];  // keys in sorted order
   uint16_t idxA[kLocalMax];
   uint16_t idxB[kLocalMax];
-  uint16_t hist[kWarps << kLocalBits];
+  uint16_t hist[kNW << kLocalBits];
   uint32_t start[(1 << kLocalBits) + 1];
   uint16_t big[kLocalMax / (kInsertMax + 1) + 2];  // start of pending bins
   uint16_t bigsz[kLocalMax / (kInsertMax + 1) + 2];
   uint32_t nbig;
-  uint64_t red[2 * kWarps];
-  uint32_t scan_tmp[kWarps];
+  uint64_t red[2 * kNW];
+  uint32_t scan_tmp[kNW];
   uint32_t task_id;
   SortTask next;
 };
@@ -537,7 +543,9 @@ struct SplitSmem {
   SortTask next;
 };
 
+template <int NT = kThreads>
 __device__ __forceinline__ void block_minmax(uint64_t& mn, uint64_t& mx, uint64_t* red) {
+  constexpr int NW = NT / 32;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     uint64_t a = __shfl_xor_sync(GB_FULL_MASK, mn, o), b = __shfl_xor_sync(GB_FULL_MASK, mx, o);
@@ -546,15 +554,15 @@ __device__ __forceinline__ void block_minmax(uint64_t& mn, uint64_t& mx, uint64_
   }
   if (lane_id() == 0) {
     red[warp_id()] = mn;
-    red[kWarps + warp_id()] = mx;
+    red[NW + warp_id()] = mx;
   }
   __syncthreads();
   mn = red[0];
-  mx = red[kWarps];
+  mx = red[NW];
 #pragma unroll
-  for (int i = 1; i < kWarps; ++i) {
+  for (int i = 1; i < NW; ++i) {
     mn = red[i] < mn ? red[i] : mn;
-    mx = red[kWarps + i] > mx ? red[kWarps + i] : mx;
+    mx = red[NW + i] > mx ? red[NW + i] : mx;
   }
   __syncthreads();
 }
@@ -566,8 +574,10 @@ __device__ __forceinline__ void block_minmax(uint64_t& mn, uint64_t& mx, uint64_
 // step is one element per thread, so a large bin costs its own threads only.
 // Elements of bins above kInsertMax go back unchanged and their bins are
 // queued for another pass.  Keys stay in shared memory (few registers).
-__device__ void local_msd_pass(LocalSmem& sm, uint32_t a, uint32_t s, uint64_t mn, uint64_t mx) {
-  using Rank = BlockRank<kLocalRpt, kLocalBits>;
+template <int NT>
+__device__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint32_t s, uint64_t mn, uint64_t mx) {
+  constexpr int kLocalRpt = kLocalMax / NT;
+  using Rank = BlockRank<kLocalRpt, kLocalBits, NT>;
   const uint32_t w = warp_id(), lane = lane_id();
   const int bits = bitlen64(mx - mn);
   const int shift = bits > kLocalBits ? bits - kLocalBits : 0;
@@ -587,7 +597,7 @@ __device__ void local_msd_pass(LocalSmem& sm, uint32_t a, uint32_t s, uint64_t m
     }
   }
   __syncthreads();
-  for (uint32_t i = threadIdx.x; i < s; i += kThreads) {
+  for (uint32_t i = threadIdx.x; i < s; i += NT) {
     const uint64_t kv = sm.keyB[a + i];
     const uint16_t iv = sm.idxB[a + i];
     const uint32_t d = (uint32_t)((kv - mn) >> shift);
@@ -613,9 +623,10 @@ __device__ void local_msd_pass(LocalSmem& sm, uint32_t a, uint32_t s, uint64_t m
 }
 
 // Stable sort of `m` <= kLocalMax records of src by key into dst (distinct).
-template <int EW>
-__device__ void local_sort(LocalSmem& sm, const uint8_t* src, uint8_t* dst, uint32_t m,
+template <int EW, int NT>
+__device__ void local_sort(LocalSmemT<NT>& sm, const uint8_t* src, uint8_t* dst, uint32_t m,
                            const gbsort_key_word& kw, uint32_t* stats) {
+  constexpr int kLocalRpt = kLocalMax / NT;
   constexpr uint32_t E = EW * 4;
   const uint32_t w = warp_id(), lane = lane_id();
   uint64_t mn = ~0ull, mx = 0;
@@ -638,13 +649,13 @@ __device__ void local_sort(LocalSmem& sm, const uint8_t* src, uint8_t* dst, uint
     }
   }
   if (threadIdx.x == 0) sm.nbig = 0;
-  block_minmax(mn, mx, sm.red);
+  block_minmax<NT>(mn, mx, sm.red);
   if (mn == mx) {  // one key: the input order is the stable order
-    block_copy_ilp<EW>(src, dst, m, kThreads);
+    block_copy_ilp<EW>(src, dst, m, NT);
     __syncthreads();
     return;
   }
-  local_msd_pass(sm, 0, m, mn, mx);
+  local_msd_pass<NT>(sm, 0, m, mn, mx);
   // further passes over bins too large for insertion sort
   for (;;) {
     uint32_t nb = sm.nbig;
@@ -654,15 +665,15 @@ __device__ void local_sort(LocalSmem& sm, const uint8_t* src, uint8_t* dst, uint
     __syncthreads();
     if (threadIdx.x == 0) sm.nbig = nb - 1;
     uint64_t bmn = ~0ull, bmx = 0;
-    for (uint32_t e = threadIdx.x; e < s; e += kThreads) {
+    for (uint32_t e = threadIdx.x; e < s; e += NT) {
       uint64_t kv = sm.keyA[a + e];
       bmn = kv < bmn ? kv : bmn;
       bmx = kv > bmx ? kv : bmx;
     }
-    block_minmax(bmn, bmx, sm.red);
+    block_minmax<NT>(bmn, bmx, sm.red);
     if (bmn == bmx) continue;  // equal keys are already in input order
     if (threadIdx.x == 0) atomicAdd(stats + STAT_BIGBIN, 1u);
-    local_msd_pass(sm, a, s, bmn, bmx);
+    local_msd_pass<NT>(sm, a, s, bmn, bmx);
   }
   // gather the records into dst in sorted order, four loads in flight
   {
@@ -671,16 +682,16 @@ __device__ void local_sort(LocalSmem& sm, const uint8_t* src, uint8_t* dst, uint
     constexpr int VPR = E / sizeof(V);
     constexpr int U = sizeof(V) >= 16 ? 2 : 4;
     const uint32_t nv = m * VPR;
-    for (uint32_t f0 = threadIdx.x; f0 < nv; f0 += kThreads * U) {
+    for (uint32_t f0 = threadIdx.x; f0 < nv; f0 += NT * U) {
       V v[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        uint32_t f = f0 + u * kThreads;
+        uint32_t f = f0 + u * NT;
         if (f < nv) v[u] = reinterpret_cast<const V*>(src + (size_t)sm.idxA[f / VPR] * E)[f % VPR];
       }
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        uint32_t f = f0 + u * kThreads;
+        uint32_t f = f0 + u * NT;
         if (f < nv) reinterpret_cast<V*>(dst + (size_t)(f / VPR) * E)[f % VPR] = v[u];
       }
     }
@@ -880,12 +891,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_split(HsortParams p, TaskLists 
   }
 }
 
-template <int EW>
-__global__ void __launch_bounds__(kThreads, 2) k_local(HsortParams p, const SortTask* __restrict__ tasks,
+template <int EW, int NT = kLocalThreads>
+__global__ void __launch_bounds__(NT, kLocalCtasPerSm) k_local(HsortParams p, const SortTask* __restrict__ tasks,
                                                         const uint32_t* __restrict__ ntasks, uint32_t cap,
                                                         uint32_t* __restrict__ work, uint32_t* __restrict__ stats) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
-  LocalSmem& sm = *reinterpret_cast<LocalSmem*>(smem_raw);
+  LocalSmemT<NT>& sm = *reinterpret_cast<LocalSmemT<NT>*>(smem_raw);
   constexpr uint32_t E = EW * 4;
   const uint32_t nt = min(*ntasks, cap);
   // thread 0 claims the next task while the current one is sorted, so the
@@ -910,11 +921,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_local(HsortParams p, const Sort
     const uint8_t* src = (task.src ? p.bufB : p.bufA) + (size_t)task.start * E;
     uint8_t* out = p.out + (size_t)task.start * E;
     if (task.kind == TASK_COPY || task.count == 1) {
-      block_copy_ilp<EW>(src, out, task.count, kThreads);
+      block_copy_ilp<EW>(src, out, task.count, NT);
       if (threadIdx.x == 0) atomicAdd(stats + STAT_COPY, 1u);
       __syncthreads();
     } else {
-      local_sort<EW>(sm, src, out, task.count, p.key, stats);
+      local_sort<EW, NT>(sm, src, out, task.count, p.key, stats);
       if (threadIdx.x == 0) atomicAdd(stats + STAT_LOCAL, 1u);
     }
     if (threadIdx.x == 0) {
@@ -1062,7 +1073,7 @@ cudaError_t build_tasks(const uint32_t* offsets, int grid, const uint64_t* split
 }
 
 int split_grid() { return num_sms() * 2; }
-int local_grid() { return num_sms() * 2; }
+int local_grid() { return num_sms() * kLocalCtasPerSm; }
 
 cudaError_t run_split_round(const HsortParams& p, const TaskListsHost& lists, uint32_t* work_counter,
                             uint32_t* stats, uint32_t* err, cudaStream_t stream) {
@@ -1087,10 +1098,10 @@ cudaError_t run_local(const HsortParams& p, const SortTask* tasks, const uint32_
   if (e != cudaSuccess) return e;
   bool ok = dispatch_ew(p.elsize, [&](auto ewc) {
     constexpr int EW = decltype(ewc)::value;
-    size_t sm = sizeof(LocalSmem);
+    size_t sm = sizeof(LocalSmemT<kLocalThreads>);
     e = set_smem((const void*)k_local<EW>, sm);
     if (e == cudaSuccess)
-      k_local<EW><<<local_grid(), kThreads, sm, stream>>>(p, tasks, ntasks, cap, work_counter, stats);
+      k_local<EW><<<local_grid(), kLocalThreads, sm, stream>>>(p, tasks, ntasks, cap, work_counter, stats);
     note_launches(1);
   });
   if (!ok) return cudaErrorInvalidValue;
