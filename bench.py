@@ -25,6 +25,7 @@ import time
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(REPO, "mp-sort_gb300"))
 sys.path.insert(0, os.path.join(REPO, "oracle"))
+sys.path.insert(0, REPO)
 
 METRIC = "sorted records/s (1e9 x 16 B u64-keyed records)"
 UNIT = "records/s"
@@ -123,41 +124,12 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_keys(torch, n, dist, device, seed):
-    g = torch.Generator(device=device)
-    g.manual_seed(seed)
-    if dist == "uniform":
-        return torch.randint(-2**63, 2**63 - 1, (n,), dtype=torch.int64, device=device, generator=g)
-    if dist == "sorted1pct":
-        k = torch.arange(n, dtype=torch.int64, device=device)
-        m = n // 100
-        i = torch.randint(0, n, (m,), device=device, generator=g)
-        j = torch.randint(0, n, (m,), device=device, generator=g)
-        ki, kj = k[i].clone(), k[j].clone()
-        k[i] = kj
-        k[j] = ki
-        return k
-    if dist == "zipf":
-        # rank r in [1, 1e6] with P(r) ~ r^-1.2 by inverse transform on a
-        # tabulated CDF, mapped through a seeded permutation of random values
-        import numpy as np
-        rng = np.random.default_rng(seed)
-        ranks = np.arange(1, 10**6 + 1, dtype=np.float64)
-        cdf = np.cumsum(ranks ** -1.2)
-        cdf /= cdf[-1]
-        vals = torch.from_numpy(rng.integers(-2**63, 2**63 - 1, 10**6, dtype=np.int64)).to(device)
-        cdf_t = torch.from_numpy(cdf).to(device)
-        u = torch.rand(n, dtype=torch.float64, device=device, generator=g)
-        r = torch.searchsorted(cdf_t, u).clamp_(max=10**6 - 1)
-        return vals[r]
-    raise ValueError(dist)
-
-
 def run_ours(args):
     import numpy
     import torch
     import mpsort
     from mpsort import device as dev
+    import workloads as W
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -169,7 +141,7 @@ def run_ours(args):
     dt = numpy.dtype(DTYPE_DESC)
     n = args.n
     rec = torch.empty((n, 2), dtype=torch.int64, device="cuda")
-    rec[:, 0] = make_keys(torch, n, args.dist, "cuda", 1234 + rank)
+    rec[:, 0] = W.keys_2(torch, n, args.dist, 1234 + rank)
     rec[:, 1] = torch.arange(n, device="cuda")
     out = torch.empty_like(rec)
     stream = torch.cuda.current_stream()
@@ -325,6 +297,124 @@ def cpu_baseline(args, seconds=None):
             "sample": "%d records of the same 16 B layout, median of 3 sorts" % n}
 
 
+def _u64(t):
+    """uint64 keys held in int64 tensors, mapped to int64 order."""
+    return t ^ (-2**63)
+
+
+def run_config(args):
+    """One JSON line for configurations 1, 3, 4, 5 (parity checked by
+    size-independent properties on the device)."""
+    import numpy
+    import torch
+    import mpsort
+    from mpsort import device as dev
+    import workloads as W
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    st = torch.cuda.current_stream()
+    sp = st.cuda_stream
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    res = {"config_id": args.config, "steps": args.steps, "warmup": args.warmup}
+
+    def timed(fn, steps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        a, b = ev(), ev()
+        a.record(st)
+        for _ in range(steps):
+            fn()
+        b.record(st)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / steps
+
+    if args.config == "1":
+        import oracle as O
+        arr = W.records_1(torch)
+        din = torch.from_numpy(arr.view(numpy.uint8).copy()).cuda()
+        dout = torch.empty_like(din)
+        n = len(arr)
+        for m in ("learned", "plain", "lsd"):
+            ms = timed(lambda: dev.sort(din.data_ptr(), dout.data_ptr(), n, W.DT1, 'key', m, sp), args.steps)
+            res[m + "_records_per_s"] = n / (ms / 1e3)
+        got = dout.cpu().numpy().view(W.DT1)
+        ref = O.ref_sort(arr, 'key', 'omp')
+        exp = ref if ref is not None else O.numpy_sorted(arr, 'key')
+        res.update(value=res["learned_records_per_s"], n=n,
+                   parity={"equals_reference" if ref is not None else "equals_stable_sort": got.tobytes() == exp.tobytes()})
+    elif args.config == "3":
+        buf, dt, offs = W.segments_3(torch)
+        out = torch.empty_like(buf)
+        n = int(offs[-1])
+        ms = timed(lambda: dev.sort_segments(buf.data_ptr(), out.data_ptr(), offs, dt, 'key', 'auto', sp), args.steps)
+        stats = mpsort.last_stats()
+
+        def per_array():
+            for i in range(len(offs) - 1):
+                a, b = int(offs[i]), int(offs[i + 1])
+                dev.sort(buf.data_ptr() + a * 8, out.data_ptr() + a * 8, b - a, dt, 'key', 'plain', sp)
+        ms_loop = timed(per_array, 1)
+        dev.sort_segments(buf.data_ptr(), out.data_ptr(), offs, dt, 'key', 'auto', sp)
+        torch.cuda.synchronize()
+        rec = out.view(torch.int32).view(-1, 2)
+        key, pay = rec[:, 0].to(torch.int64), rec[:, 1].to(torch.int64)
+        seg_start = torch.zeros(n, dtype=torch.bool, device="cuda")
+        seg_start[torch.from_numpy(offs[:-1].astype(numpy.int64)).cuda().clamp_(max=n - 1)] = True
+        ok_sorted = bool(((key[1:] >= key[:-1]) | seg_start[1:]).all().item())
+        ok_stable = bool(((key[1:] != key[:-1]) | seg_start[1:] | (pay[1:] > pay[:-1])).all().item())
+        seg_of_pos = torch.cumsum(seg_start.to(torch.int64), 0)
+        ok_perm = bool((torch.bincount(pay, minlength=n) == 1).all().item()) and \
+            bool((seg_of_pos[pay] == seg_of_pos).all().item())
+        res.update(value=n / (ms / 1e3), n=n, nseg=len(offs) - 1, ms_per_step=ms,
+                   per_array_loop_records_per_s=n / (ms_loop / 1e3), per_array_loop_ms=ms_loop,
+                   parity={"sorted": ok_sorted, "stable": ok_stable, "permutation": ok_perm},
+                   sort_stats=stats)
+    elif args.config == "4":
+        n = args.n if args.n != 10**9 else 5 * 10**8
+        buf, dt = W.particles_4(torch, n)
+        out = torch.empty_like(buf)
+        for m in ("learned", "plain"):
+            ms = timed(lambda: dev.sort(buf.data_ptr(), out.data_ptr(), n, dt, 'key', m, sp), args.steps)
+            stl = mpsort.last_stats()
+            res[m] = {"records_per_s": n / (ms / 1e3), "ms": ms, "stage_ms": stl["stage_ms"],
+                      "bucket_imbalance": stl["max_bucket"] / (n / stl["nbuckets"]),
+                      "resplits": stl["resplits"], "splits": stl["splits"],
+                      "window_misses": stl["window_misses"], "widest_window": stl["widest_window"],
+                      "bigbin_passes": stl["bigbin_passes"]}
+        rec = out.view(torch.int64).view(-1, 5)
+        key, ident = _u64(rec[:, 4]), rec[:, 3]
+        ok_sorted = bool((key[1:] >= key[:-1]).all().item())
+        ok_perm = bool((torch.bincount(ident, minlength=n) == 1).all().item())
+        ok_stable = bool(((key[1:] != key[:-1]) | (ident[1:] > ident[:-1])).all().item())
+        res.update(value=res["learned"]["records_per_s"], n=n,
+                   parity={"sorted": ok_sorted, "permutation": ok_perm, "stable": ok_stable})
+    elif args.config == "5":
+        buf, dt, na, nb, common = W.snapshots_5(torch)
+        out = torch.empty_like(buf)
+        offs = numpy.array([0, na, na + nb], dtype=numpy.uint64)
+        pa = torch.empty(min(na, nb), dtype=torch.int64, device="cuda")
+        pb = torch.empty_like(pa)
+        npairs = torch.zeros(1, dtype=torch.int64, device="cuda")
+
+        def step():
+            dev.sort_segments(buf.data_ptr(), out.data_ptr(), offs, dt, 'id', 'auto', sp)
+            dev.merge_join(out.data_ptr(), na, out.data_ptr() + na * 16, nb, dt, 'id', pa.data_ptr(),
+                           pb.data_ptr(), npairs.data_ptr(), sp)
+        ms = timed(step, args.steps)
+        k = int(npairs.item())
+        ids = out.view(torch.int64).view(-1, 2)[:, 0]
+        ida, idb = ids[:na], ids[na:]
+        ok_pairs = k == common and bool((ida[pa[:k]] == idb[pb[:k]]).all().item()) and \
+            bool((pa[1:k] > pa[:k - 1]).all().item())
+        ok_sorted = bool((ida[1:] > ida[:-1]).all().item()) and bool((idb[1:] > idb[:-1]).all().item())
+        res.update(value=(na + nb) / (ms / 1e3), n=na + nb, ms_per_step=ms, pairs=k, expected_pairs=common,
+                   parity={"pairs": ok_pairs, "sorted_unique": ok_sorted})
+    line = {"metric": "sorted records/s, configuration " + args.config, "unit": UNIT, "n_gpus": 1,
+            "higher_is_better": True, "data": "synthetic (workloads.py, seeded)"}
+    line.update(res)
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -381,11 +471,18 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-compare", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--config", choices=["1", "2a", "2b", "2c", "3", "4", "5"], default="2a",
+                    help="workload; 2a/2b/2c give the contract's bench line (2b = --dist sorted1pct, "
+                         "2c = --dist zipf), the others a JSON line of their own")
     args = ap.parse_args()
+    if args.config in ("2b", "2c"):
+        args.dist = {"2b": "sorted1pct", "2c": "zipf"}[args.config]
     if args.impl == "reference":
         run_reference(args)
-    else:
+    elif args.config in ("2a", "2b", "2c"):
         run_ours(args)
+    else:
+        run_config(args)
 
 
 if __name__ == "__main__":

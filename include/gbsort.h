@@ -65,7 +65,9 @@ typedef struct gbsort_stats {
      * scan, bucket scatter, bucket splits, local sorts */
     float stage_ms[6];
     uint32_t launches;           /* kernels this sort enqueued */
-    uint32_t reserved[3];
+    uint32_t splitter_fallback;  /* 1: the model's splitters failed the sample check and the
+                                    sample quantiles (the plain splitters) were used */
+    uint32_t reserved[2];
 } gbsort_stats;
 
 /* Sort nmemb records of elsize bytes from d_in into d_out (device memory;

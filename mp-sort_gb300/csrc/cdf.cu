@@ -308,6 +308,39 @@ __global__ void k_pack_windows(const uint32_t* __restrict__ lo, const uint32_t* 
   atomicMax(wide, max(lo[l], hi[l]));
 }
 
+// S[i] = x_(C_i), the C_i-th smallest sample key, C_i = s (i+1) / (nsplit+1):
+// the value the reference's bisection converges to (CLT < C <= CLE holds at
+// the C-th order statistic and nowhere else), read directly.
+__global__ void k_quantile_splitters(const uint64_t* __restrict__ x, uint32_t s, int nsplit, uint64_t* __restrict__ S) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsplit) return;
+  uint64_t c = (uint64_t)s * (uint64_t)(i + 1) / (uint64_t)(nsplit + 1);
+  S[i] = x[c > 0 ? c - 1 : 0];
+}
+
+// Judge of a splitter set on the sorted sample: every key with a bucket's
+// worth of sample copies must own a single-key bucket [k, k+1), and no
+// other bucket may hold more than `limit` sample keys.  flags[0] != 0 means
+// rejected; counts (nbuckets) must start at zero.
+__global__ void k_judge_count(const uint64_t* __restrict__ x, uint32_t s, const uint64_t* __restrict__ S, int nbuckets,
+                              uint32_t* __restrict__ counts, uint32_t* __restrict__ flags) {
+  const uint32_t need = (s + nbuckets - 1) / nbuckets;
+  const uint32_t nsplit = (uint32_t)(nbuckets - 1);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s; i += gridDim.x * blockDim.x) {
+    const uint64_t k = x[i];
+    const uint32_t t = upper_bound_in(S, 0, nsplit, k);
+    const bool pure = t > 0 && S[t - 1] == k && (t == nsplit || S[t] == k + 1);
+    if (!pure) atomicAdd(&counts[t], 1u);
+    const bool run_start = i == 0 || x[i - 1] != k;
+    if (run_start && i + need <= s && x[i + need - 1] == k && !pure) atomicOr(flags, 1u);
+  }
+}
+
+__global__ void k_judge_max(const uint32_t* __restrict__ counts, int nbuckets, uint32_t limit, uint32_t* __restrict__ flags) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbuckets; b += gridDim.x * blockDim.x)
+    if (counts[b] > limit) atomicOr(flags, 2u);
+}
+
 unsigned grid_for(uint32_t n, int threads) {
   uint32_t b = (n + threads - 1) / threads;
   return b < 1 ? 1 : (b > 1184 ? 1184 : b);
@@ -382,6 +415,27 @@ cudaError_t cdf_windows(const CdfShape& sh, int nbuckets, const float2* knots, c
   if ((e = cudaMemsetAsync(widest, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
   k_cdf_windows<<<grid_for(nbuckets + nleaf, 128), 128, 0, st>>>(sh, nbuckets, knots, S, tmp_lo, tmp_hi);
   k_pack_windows<<<grid_for(nleaf, 256), 256, 0, st>>>(tmp_lo, tmp_hi, nleaf, win, widest);
+  note_launches(2);
+  return cudaGetLastError();
+}
+
+cudaError_t quantile_splitters(const uint64_t* x, uint32_t s, int nsplit, uint64_t* S, cudaStream_t st) {
+  if (nsplit <= 0) return cudaSuccess;
+  k_quantile_splitters<<<grid_for(nsplit, 256), 256, 0, st>>>(x, s, nsplit, S);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t judge_splitters(const uint64_t* x, uint32_t s, const uint64_t* S, int nbuckets, uint32_t* counts,
+                            uint32_t* flags, cudaStream_t st) {
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(counts, 0, sizeof(uint32_t) * nbuckets, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(flags, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+  // a bucket may hold up to 2.5x its share of the sample before the plain
+  // splitters take over
+  const uint32_t limit = (uint32_t)(2.5 * (double)s / (double)nbuckets) + 8;
+  k_judge_count<<<grid_for(s, 256), 256, 0, st>>>(x, s, S, nbuckets, counts, flags);
+  k_judge_max<<<grid_for(nbuckets, 256), 256, 0, st>>>(counts, nbuckets, limit, flags);
   note_launches(2);
   return cudaGetLastError();
 }

@@ -33,4 +33,11 @@ cudaError_t cdf_windows(const CdfShape& sh, int nbuckets, const float2* knots, c
                         uint32_t* win, uint32_t* tmp_lo, uint32_t* tmp_hi, uint32_t* widest,
                         cudaStream_t st);
 
+// Splitters read directly from the sorted sample at the bisection's targets.
+cudaError_t quantile_splitters(const uint64_t* x, uint32_t s, int nsplit, uint64_t* S, cudaStream_t st);
+// Rejects (flags[0] != 0) a splitter set that leaves a heavy sample key out
+// of a single-key bucket or puts more than 2.5x its share in any bucket.
+cudaError_t judge_splitters(const uint64_t* x, uint32_t s, const uint64_t* S, int nbuckets, uint32_t* counts,
+                            uint32_t* flags, cudaStream_t st);
+
 }  // namespace gb

@@ -25,8 +25,8 @@ cudaError_t join_write(const uint8_t* a, uint32_t na, const uint8_t* b, uint32_t
                        uint64_t* npairs, cudaStream_t st);
 int join_grid(uint32_t na);
 cudaError_t segment_ranges(const uint8_t* rec, uint32_t elsize, gbsort_key_word key, const uint64_t* offsets,
-                           uint32_t nseg, SortTask* tasks, uint32_t* ntasks, uint32_t cap, uint32_t* err,
-                           cudaStream_t st);
+                           uint32_t nseg, uint64_t skip_above, SortTask* tasks, uint32_t* ntasks, uint32_t cap,
+                           uint32_t* err, cudaStream_t st);
 cudaError_t probe_buckets(const uint64_t* keys, uint32_t nkeys, const uint64_t* S, const void* model,
                           uint32_t* learned, uint32_t* search, uint32_t* misses, cudaStream_t st);
 }  // namespace gb
@@ -381,6 +381,7 @@ int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t el
 
   ModelDev model{};
   int lookup = LOOKUP_PLAIN;
+  bool splitter_fallback = false;
   GB_CUDA(cudaEventRecord(c.ev[0], st));
   if (nb > 1) {
     uint64_t* sA = bump.take<uint64_t>(s);
@@ -409,6 +410,20 @@ int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t el
       GB_CUDA(cdf_train(sA, s, sh, epochs, 0.5f, w, st));
       GB_CUDA(cdf_splitters(sA, s, sh, nb, w.knots, S, st));
       GB_CUDA(finalize_splitters(S, nb - 1, st));
+      // the plain splitters judge the model's: if the sample shows a heavy
+      // key outside a single-key bucket or an overfull bucket, the sample's
+      // own quantiles (what the bisection converges to) replace them; the
+      // model still serves the lookup, with windows for the final splitters
+      uint32_t* jcounts = bump.take<uint32_t>(nb);
+      uint32_t* jflag = bump.take<uint32_t>(1);
+      GB_CUDA(judge_splitters(sA, s, S, nb, jcounts, jflag, st));
+      GB_CUDA(cudaMemcpyAsync(&c.hc->err, jflag, 4, cudaMemcpyDeviceToHost, st));
+      GB_CUDA(cudaStreamSynchronize(st));
+      splitter_fallback = c.hc->err != 0;
+      if (splitter_fallback) {
+        GB_CUDA(quantile_splitters(sA, s, nb - 1, S, st));
+        GB_CUDA(finalize_splitters(S, nb - 1, st));
+      }
       GB_CUDA(cdf_windows(sh, nb, w.knots, S, win, wlo, whi, widest, st));
       model.kmin = sh.kmin;
       model.lshift = sh.lshift;
@@ -432,10 +447,17 @@ int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t el
     TaskListsHost L = l2.round(-1);  // appends to split[0]
     GB_CUDA(build_tasks(counts, grid, S, nb, n, L, err, stats, st));
   }
+  static const bool trace = getenv("GBSORT_TRACE") != nullptr;
   for (int r = 0; r < kSplitRounds; ++r) {
     TaskListsHost L = l2.round(r);
     GB_CUDA(cudaMemsetAsync(L.nsplit_out, 0, sizeof(uint32_t), st));
     GB_CUDA(run_split_round(p, L, l2.work, stats, err, st));
+    if (trace) {  // debugging aid: split tasks per round (synchronises)
+      uint32_t h[3];
+      GB_CUDA(cudaMemcpyAsync(h, l2.nsplit, 12, cudaMemcpyDeviceToHost, st));
+      GB_CUDA(cudaStreamSynchronize(st));
+      fprintf(stderr, "gbsort trace: round %d in %u out %u local %u\n", r, h[r & 1], h[(r + 1) & 1], h[2]);
+    }
   }
   GB_CUDA(cudaEventRecord(c.ev[5], st));
   GB_CUDA(run_local(p, l2.local, l2.nlocal, l2.cap_local, l2.work, stats, st));
@@ -470,6 +492,7 @@ int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t el
   g_stats.max_bucket = c.hc->stats[STAT_MAX_BUCKET];
   g_stats.widest_window = c.hc->widest;
   g_stats.model_loss = learned ? c.hc->loss : 0.f;
+  g_stats.splitter_fallback = splitter_fallback ? 1u : 0u;
   for (int i = 0; i < 6; ++i) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c.ev[i], c.ev[i + 1]);
@@ -623,6 +646,19 @@ int gbsort_sort_segments_device(const void* d_in, void* d_out, const uint64_t* s
     }
     return GBSORT_OK;
   }
+  // Segments large enough to fill the GPU on their own go through the full
+  // histogram sort one at a time; the rest share one task pipeline.
+  const uint64_t kBigSegment = 1ull << 22;
+  uint64_t nbig = 0;
+  for (size_t i = 0; i < nseg; ++i) {
+    uint64_t a = seg_offsets[i], b = seg_offsets[i + 1];
+    if (b - a <= kBigSegment) continue;
+    rc = sort_device_locked(*c, (const uint8_t*)d_in + a * E, (uint8_t*)d_out + a * E, b - a, E, key,
+                            method == GBSORT_AUTO ? GBSORT_HISTOGRAM_LEARNED : method, st);
+    if (rc) return rc;
+    nbig += b - a;
+  }
+  if (nbig == n) return GBSORT_OK;
   GB_CUDA(c->A.ensure((size_t)N * E));
   GB_CUDA(c->B.ensure((size_t)N * E));
   const uint32_t cap_split = (uint32_t)nseg * 2 + N / 4096 + 4096;
@@ -638,8 +674,8 @@ int gbsort_sort_segments_device(const void* d_in, void* d_out, const uint64_t* s
   GB_CUDA(cudaMemsetAsync(counters, 0, 64 * sizeof(uint32_t), st));
   GB_CUDA(cudaMemcpyAsync(offs, seg_offsets, (nseg + 1) * 8, cudaMemcpyHostToDevice, st));
   GB_CUDA(cudaMemcpyAsync(c->A.p, d_in, (size_t)N * E, cudaMemcpyDeviceToDevice, st));
-  GB_CUDA(segment_ranges(c->A.as<uint8_t>(), E, key->word[0], offs, (uint32_t)nseg, l2.split[0], l2.nsplit,
-                         cap_split, err, st));
+  GB_CUDA(segment_ranges(c->A.as<uint8_t>(), E, key->word[0], offs, (uint32_t)nseg, kBigSegment, l2.split[0],
+                         l2.nsplit, cap_split, err, st));
   HsortParams p{};
   p.in = (const uint8_t*)d_in;
   p.out = (uint8_t*)d_out;

@@ -27,12 +27,12 @@ constexpr int kJoinWindow = 4096;
 __global__ void __launch_bounds__(kThreads) k_segment_ranges(const uint8_t* __restrict__ rec, uint32_t elsize,
                                                               gbsort_key_word kw,
                                                               const uint64_t* __restrict__ offs, uint32_t nseg,
-                                                              SortTask* __restrict__ tasks, uint32_t* ntasks,
-                                                              uint32_t cap, uint32_t* err) {
+                                                              uint64_t skip_above, SortTask* __restrict__ tasks,
+                                                              uint32_t* ntasks, uint32_t cap, uint32_t* err) {
   __shared__ uint64_t red[2 * kWarps];
   for (uint32_t sg = blockIdx.x; sg < nseg; sg += gridDim.x) {
     const uint64_t a = offs[sg], b = offs[sg + 1];
-    if (b == a) continue;
+    if (b == a || b - a > skip_above) continue;  // empty, or sorted on its own
     uint64_t mn = ~0ull, mx = 0;
     for (uint64_t i = a + threadIdx.x; i < b; i += kThreads) {
       uint64_t k = load_key_aligned4(rec + i * elsize, kw);
@@ -200,10 +200,10 @@ __global__ void k_probe_buckets(const uint64_t* __restrict__ keys, uint32_t nkey
 }  // namespace
 
 cudaError_t segment_ranges(const uint8_t* rec, uint32_t elsize, gbsort_key_word key, const uint64_t* offsets,
-                           uint32_t nseg, SortTask* tasks, uint32_t* ntasks, uint32_t cap, uint32_t* err,
-                           cudaStream_t st) {
+                           uint32_t nseg, uint64_t skip_above, SortTask* tasks, uint32_t* ntasks, uint32_t cap,
+                           uint32_t* err, cudaStream_t st) {
   uint32_t g = nseg < (uint32_t)num_sms() * 8 ? nseg : (uint32_t)num_sms() * 8;
-  k_segment_ranges<<<g, kThreads, 0, st>>>(rec, elsize, key, offsets, nseg, tasks, ntasks, cap, err);
+  k_segment_ranges<<<g, kThreads, 0, st>>>(rec, elsize, key, offsets, nseg, skip_above, tasks, ntasks, cap, err);
   note_launches(1);
   return cudaGetLastError();
 }

@@ -357,11 +357,14 @@ def test_learned_lookup_equals_search(mp, dist):
 
 
 # --------------------------------------------- batched and join paths --
-def test_segments(mp):
+@pytest.mark.parametrize("big", [False, True])
+def test_segments(mp, big):
     import torch
     from mpsort import device
     rng = numpy.random.default_rng(5)
     sizes = numpy.concatenate([[0, 1, 2, 4096, 4097, 70_000], rng.integers(0, 3000, 200)])
+    if big:  # segments above 2^22 records take the whole-grid sort one by one
+        sizes = numpy.concatenate([[5_000_000], sizes[:100], [(1 << 22) + 1, 1 << 22], sizes[100:]])
     offs = numpy.concatenate([[0], numpy.cumsum(sizes)]).astype(numpy.uint64)
     n = int(offs[-1])
     dt = numpy.dtype([('key', 'i4'), ('payload', 'u4')])
@@ -414,3 +417,25 @@ def test_stats_report_method(mp):
         assert st["method"] == m
         if m != "lsd":
             assert st["nbuckets"] > 1 and st["window_misses"] == 0
+
+
+@pytest.mark.parametrize("nvals", [1000, 100_000])
+def test_learned_heavy_keys_balanced(mp, nvals):
+    """Zipf keys put several heavy keys between neighbouring model splitters;
+    the learned path must still sort stably and keep every bucket that holds
+    more than one key near the mean size (else it falls back to the sample
+    quantiles and says so)."""
+    rng = numpy.random.default_rng(nvals)
+    n = 4_000_000
+    dt = numpy.dtype([('key', 'u8'), ('val', 'i8')])
+    a = numpy.zeros(n, dt)
+    vals = rng.integers(0, 2**64, nvals, dtype=numpy.uint64, endpoint=False)
+    a['key'] = vals[numpy.minimum(rng.zipf(1.2, n) - 1, nvals - 1)]
+    a['val'] = numpy.arange(n)
+    check(mp, a, 'key', "learned")
+    st = mp.last_stats()
+    assert st["splitter_fallback"] in (0, 1)
+    keys, counts = numpy.unique(a['key'], return_counts=True)
+    # a bucket is either one key, or at most ~2.5x the mean plus one heavy key
+    limit = 3 * n // st["nbuckets"] + 64
+    assert st["max_bucket"] <= max(limit, int(counts.max()))
