@@ -122,6 +122,17 @@ GBSORT_API int gbsort_debug_buckets(const uint64_t *sample, uint32_t s, int nbuc
                          uint32_t nkeys, uint32_t *bucket_search, uint32_t *bucket_learned,
                          uint64_t *splitters, uint32_t *widest_window);
 
+/* What the trained model gains (host arrays): trains the model on the
+ * sample for `epochs` gradient steps (0 = the initial fit of the empirical
+ * CDF at the knots), looks every key up with the model and with the full
+ * binary search over the same splitters, and reports the final training
+ * loss, the splitters read by each lookup in total (reads[0] learned,
+ * reads[1] full search) and the widest window.  Used by tests. */
+GBSORT_API int gbsort_debug_model(const uint64_t *sample, uint32_t s, int nbuckets, int epochs,
+                       const uint64_t *keys, uint32_t nkeys, uint32_t *bucket_search,
+                       uint32_t *bucket_learned, float *loss, uint64_t *reads,
+                       uint32_t *widest_window);
+
 /* Plain splitter search alone (host arrays): the reference's bisection
  * (internal-parallel.h:128-248) for nsplit splitters over a sorted run of
  * s keys with targets C[i+1] = s*(i+1)/(nsplit+1).  Outputs the splitters
@@ -157,6 +168,31 @@ GBSORT_API int gbsort_device_count(void);
 GBSORT_API int gbsort_release(void);
 /* Version string of this library. */
 GBSORT_API const char *gbsort_version(void);
+
+/* ---- graph plans ----------------------------------------------------------
+ * The whole device pipeline of one sort shape -- sample, splitter search or
+ * model training, bucket count, scan, scatter, bucket splits and local
+ * sorts -- captured once into a CUDA graph and replayed with one graph
+ * launch and no host synchronisation.  No counterpart in the reference
+ * (its sort is a synchronous call).
+ *
+ *   gbsort_plan_create   fixes nmemb, elsize, key and method (GBSORT_AUTO
+ *                        resolves at the first capture); owns its scratch.
+ *   gbsort_plan_sort     enqueues the sort of d_in into d_out on `stream`
+ *                        (NULL: the plan's own stream) and returns at once;
+ *                        the graph is captured on first use and again when
+ *                        the buffers change.  One launch per plan at a time:
+ *                        a second call first waits for the previous one.
+ *   gbsort_plan_wait     waits for the launch, then returns its status (the
+ *                        device error word) and fills gbsort_last_stats
+ *                        (without stage times).
+ *   gbsort_plan_destroy  waits and frees everything. */
+typedef struct gbsort_plan gbsort_plan;
+GBSORT_API int gbsort_plan_create(gbsort_plan **plan, size_t nmemb, size_t elsize,
+                       const gbsort_key_desc *key, int method);
+GBSORT_API int gbsort_plan_sort(gbsort_plan *plan, const void *d_in, void *d_out, void *stream);
+GBSORT_API int gbsort_plan_wait(gbsort_plan *plan);
+GBSORT_API int gbsort_plan_destroy(gbsort_plan *plan);
 
 #ifdef __cplusplus
 }

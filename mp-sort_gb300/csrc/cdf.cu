@@ -46,6 +46,7 @@ __device__ __forceinline__ void features(uint64_t key, uint64_t kmin, int lshift
 
 __global__ void k_cdf_forward(const uint64_t* __restrict__ x, uint32_t s, CdfShape sh,
                               const float* __restrict__ y, float* __restrict__ pred, float* __restrict__ loss) {
+  sh = resolve_shape(sh);
   __shared__ float red[32];
   float acc = 0.f;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s; i += gridDim.x * blockDim.x) {
@@ -73,6 +74,7 @@ __global__ void k_cdf_forward(const uint64_t* __restrict__ x, uint32_t s, CdfSha
 // sorted), so lanes with the same leaf combine before the atomic.
 __global__ void k_cdf_backward(const uint64_t* __restrict__ x, uint32_t s, CdfShape sh,
                                const float* __restrict__ y, float* __restrict__ grad) {
+  sh = resolve_shape(sh);
   for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < s; i0 += gridDim.x * blockDim.x) {
     uint32_t i = i0 + threadIdx.x;
     bool v = i < s;
@@ -102,6 +104,7 @@ __global__ void k_cdf_backward(const uint64_t* __restrict__ x, uint32_t s, CdfSh
 }
 
 __global__ void k_cdf_curvature(const uint64_t* __restrict__ x, uint32_t s, CdfShape sh, float* __restrict__ h) {
+  sh = resolve_shape(sh);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s; i += gridDim.x * blockDim.x) {
     uint32_t leaf;
     float frac;
@@ -120,6 +123,7 @@ __global__ void k_cdf_step(float* __restrict__ y, const float* __restrict__ grad
 
 // Initial knots: the empirical CDF of the sample at every knot.
 __global__ void k_cdf_init(const uint64_t* __restrict__ x, uint32_t s, CdfShape sh, float* __restrict__ y) {
+  sh = resolve_shape(sh);
   const int nk = (1 << sh.lbits) + 1;
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nk; j += gridDim.x * blockDim.x) {
     // knot j sits at key kmin + (j << lshift): count samples below it
@@ -191,6 +195,7 @@ __device__ __forceinline__ uint32_t predict(uint64_t key, const CdfShape& sh, in
 // S_j = least key with predicted bucket >= j + 1 (all keys above if none).
 __global__ void k_cdf_splitters(CdfShape sh, int nbuckets, const float2* __restrict__ knots,
                                 uint64_t* __restrict__ S) {
+  sh = resolve_shape(sh);
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nbuckets - 1) return;
   uint64_t lo = 0, hi = ~0ull;
@@ -270,6 +275,7 @@ __device__ __forceinline__ void window_update(uint32_t* win_lo, uint32_t* win_hi
 __global__ void k_cdf_windows(CdfShape sh, int nbuckets, const float2* __restrict__ knots,
                               const uint64_t* __restrict__ S, uint32_t* __restrict__ win_lo,
                               uint32_t* __restrict__ win_hi) {
+  sh = resolve_shape(sh);
   const int nleaf = 1 << sh.lbits;
   const int nsplit = nbuckets - 1;
   const int total = nsplit + nleaf;
@@ -311,9 +317,10 @@ __global__ void k_pack_windows(const uint32_t* __restrict__ lo, const uint32_t* 
 // S[i] = x_(C_i), the C_i-th smallest sample key, C_i = s (i+1) / (nsplit+1):
 // the value the reference's bisection converges to (CLT < C <= CLE holds at
 // the C-th order statistic and nowhere else), read directly.
-__global__ void k_quantile_splitters(const uint64_t* __restrict__ x, uint32_t s, int nsplit, uint64_t* __restrict__ S) {
+__global__ void k_quantile_splitters(const uint64_t* __restrict__ x, uint32_t s, int nsplit, uint64_t* __restrict__ S,
+                                     const uint32_t* __restrict__ only_if) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nsplit) return;
+  if (i >= nsplit || (only_if && *only_if == 0)) return;
   uint64_t c = (uint64_t)s * (uint64_t)(i + 1) / (uint64_t)(nsplit + 1);
   S[i] = x[c > 0 ? c - 1 : 0];
 }
@@ -341,6 +348,22 @@ __global__ void k_judge_max(const uint32_t* __restrict__ counts, int nbuckets, u
     if (counts[b] > limit) atomicOr(flags, 2u);
 }
 
+// Leaves of 2^lshift keys from kmin, lshift the least that covers kmax.
+__host__ __device__ CdfShape make_shape(uint64_t kmin, uint64_t kmax, int lbits) {
+  CdfShape sh{};
+  sh.kmin = kmin;
+  sh.lbits = lbits;
+  int bits = 0;
+  for (uint64_t d = kmax > kmin ? kmax - kmin : 0; d; d >>= 1) ++bits;
+  sh.lshift = bits > lbits ? bits - lbits : 0;
+  sh.dev = nullptr;
+  return sh;
+}
+
+__global__ void k_cdf_shape(const uint64_t* __restrict__ x, uint32_t s, int lbits, CdfShape* out) {
+  if (threadIdx.x == 0) *out = make_shape(x[0], x[s - 1], lbits);
+}
+
 unsigned grid_for(uint32_t n, int threads) {
   uint32_t b = (n + threads - 1) / threads;
   return b < 1 ? 1 : (b > 1184 ? 1184 : b);
@@ -348,13 +371,19 @@ unsigned grid_for(uint32_t n, int threads) {
 
 }  // namespace
 
-CdfShape cdf_shape(uint64_t kmin, uint64_t kmax, int lbits) {
+CdfShape cdf_shape(uint64_t kmin, uint64_t kmax, int lbits) { return make_shape(kmin, kmax, lbits); }
+
+CdfShape cdf_shape_ref(const CdfShape* dev, int lbits) {
   CdfShape sh{};
-  sh.kmin = kmin;
   sh.lbits = lbits;
-  int bits = kmax > kmin ? 64 - __builtin_clzll(kmax - kmin) : 0;
-  sh.lshift = bits > lbits ? bits - lbits : 0;
+  sh.dev = dev;
   return sh;
+}
+
+cudaError_t cdf_shape_device(const uint64_t* x, uint32_t s, int lbits, CdfShape* out, cudaStream_t st) {
+  k_cdf_shape<<<1, 32, 0, st>>>(x, s, lbits, out);
+  note_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t cdf_forward(const uint64_t* x, uint32_t s, const CdfShape& sh, const float* y, float* pred, float* loss,
@@ -419,9 +448,10 @@ cudaError_t cdf_windows(const CdfShape& sh, int nbuckets, const float2* knots, c
   return cudaGetLastError();
 }
 
-cudaError_t quantile_splitters(const uint64_t* x, uint32_t s, int nsplit, uint64_t* S, cudaStream_t st) {
+cudaError_t quantile_splitters(const uint64_t* x, uint32_t s, int nsplit, uint64_t* S, const uint32_t* only_if,
+                               cudaStream_t st) {
   if (nsplit <= 0) return cudaSuccess;
-  k_quantile_splitters<<<grid_for(nsplit, 256), 256, 0, st>>>(x, s, nsplit, S);
+  k_quantile_splitters<<<grid_for(nsplit, 256), 256, 0, st>>>(x, s, nsplit, S, only_if);
   note_launches(1);
   return cudaGetLastError();
 }

@@ -20,6 +20,7 @@
 // non-decreasing in the key.
 #pragma once
 
+#include "cdf_api.h"
 #include "common.cuh"
 
 namespace gb {
@@ -32,7 +33,26 @@ struct ModelDev {
   int pad;
   const float2* knots; // [leaves]: (y[j], y[j+1])
   const uint32_t* win; // [leaves]: (dlo << 16) | dhi
+  const CdfShape* shape;  // if set, kmin and lshift come from this device copy
 };
+
+// kmin / lshift from the device copy of the shape, when there is one.
+__device__ __forceinline__ CdfShape resolve_shape(CdfShape sh) {
+  if (sh.dev) {
+    const CdfShape d = *sh.dev;
+    sh.kmin = d.kmin;
+    sh.lshift = d.lshift;
+  }
+  return sh;
+}
+__device__ __forceinline__ ModelDev resolve_model(ModelDev m) {
+  if (m.shape) {
+    const CdfShape d = *m.shape;
+    m.kmin = d.kmin;
+    m.lshift = d.lshift;
+  }
+  return m;
+}
 
 // Fraction of the way through the leaf, in [0, 1).
 __device__ __forceinline__ float leaf_frac(uint64_t x, int lshift) {

@@ -10,6 +10,10 @@ struct CdfShape {
   uint64_t kmin;  // key of leaf 0's left edge
   int lshift;     // leaf = (key - kmin) >> lshift
   int lbits;      // 1 << lbits leaves, (1 << lbits) + 1 knots
+  // When set, kmin and lshift are read from this device copy at kernel start
+  // (computed on the device from the sorted sample, so the pipeline never
+  // waits for the host); lbits must match it.
+  const CdfShape* dev;
 };
 
 struct CdfWork {   // device buffers of one training run
@@ -21,6 +25,10 @@ struct CdfWork {   // device buffers of one training run
 };
 
 CdfShape cdf_shape(uint64_t kmin, uint64_t kmax, int lbits);
+// The shape of a sorted sample x[0..s) computed on the device into *out, and
+// a host-side CdfShape that refers to it.
+cudaError_t cdf_shape_device(const uint64_t* x, uint32_t s, int lbits, CdfShape* out, cudaStream_t st);
+CdfShape cdf_shape_ref(const CdfShape* dev, int lbits);
 cudaError_t cdf_forward(const uint64_t* x, uint32_t s, const CdfShape& sh, const float* y, float* pred,
                         float* loss, cudaStream_t st);
 cudaError_t cdf_backward(const uint64_t* x, uint32_t s, const CdfShape& sh, const float* y, float* grad,
@@ -33,8 +41,10 @@ cudaError_t cdf_windows(const CdfShape& sh, int nbuckets, const float2* knots, c
                         uint32_t* win, uint32_t* tmp_lo, uint32_t* tmp_hi, uint32_t* widest,
                         cudaStream_t st);
 
-// Splitters read directly from the sorted sample at the bisection's targets.
-cudaError_t quantile_splitters(const uint64_t* x, uint32_t s, int nsplit, uint64_t* S, cudaStream_t st);
+// Splitters read directly from the sorted sample at the bisection's targets
+// (only when *only_if != 0, if only_if is given).
+cudaError_t quantile_splitters(const uint64_t* x, uint32_t s, int nsplit, uint64_t* S, const uint32_t* only_if,
+                               cudaStream_t st);
 // Rejects (flags[0] != 0) a splitter set that leaves a heavy sample key out
 // of a single-key bucket or puts more than 2.5x its share in any bucket.
 cudaError_t judge_splitters(const uint64_t* x, uint32_t s, const uint64_t* S, int nbuckets, uint32_t* counts,

@@ -28,7 +28,8 @@ cudaError_t segment_ranges(const uint8_t* rec, uint32_t elsize, gbsort_key_word 
                            uint32_t nseg, uint64_t skip_above, SortTask* tasks, uint32_t* ntasks, uint32_t cap,
                            uint32_t* err, cudaStream_t st);
 cudaError_t probe_buckets(const uint64_t* keys, uint32_t nkeys, const uint64_t* S, const void* model,
-                          uint32_t* learned, uint32_t* search, uint32_t* misses, cudaStream_t st);
+                          uint32_t* learned, uint32_t* search, uint32_t* misses, unsigned long long* reads,
+                          cudaStream_t st);
 }  // namespace gb
 
 namespace {
@@ -105,14 +106,19 @@ struct Bump {
   }
 };
 
-struct HostCounters {  // pinned, read back at the end of a run
-  uint32_t stats[STAT_SLOTS];
-  uint32_t err;
-  uint32_t iters;
-  uint32_t widest;
-  float loss;
-  uint32_t ntasks[2];
-  uint64_t kminmax[2];
+// Device counters of a histogram-sort run (one 64-word array), in order.
+enum CounterSlot : int {
+  CNT_ERR = STAT_SLOTS,  // kernels given the statistics find the error word next to them
+  CNT_ITERS = 21,        // bisection rounds
+  CNT_WIDEST = 22,       // widest learned window
+  CNT_LOSS = 23,         // final training loss (float)
+  CNT_L2 = 24,           // level-2 task counters: nsplit[2], nlocal, work
+  CNT_FALLBACK = 28,     // the learned splitters were rejected
+  CNT_WORDS = 64
+};
+
+struct HostCounters {  // pinned: the device counters of the last run are copied here
+  uint32_t c[CNT_WORDS];
 };
 
 struct Context {
@@ -127,10 +133,33 @@ struct Context {
   HostCounters* hc = nullptr;
   cudaEvent_t ev[8] = {};  // stage boundaries of the histogram sort
   std::mutex mu;
+  // shape of the last enqueued histogram sort (for hsort_collect)
+  uint32_t run_nbuckets = 0, run_sample = 0, run_lsd_passes = 0;
+  bool run_learned = false, run_timing = false;
 };
 
 std::mutex g_ctx_mu;
 Context* g_ctx[64] = {};
+
+int ctx_init(Context& c, int dev) {
+  c.device = dev;
+  GB_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  GB_CUDA(cudaMallocHost(&c.hc, sizeof(HostCounters)));
+  for (cudaEvent_t& e : c.ev) GB_CUDA(cudaEventCreate(&e));
+  return GBSORT_OK;
+}
+
+void ctx_destroy(Context& c) {
+  if (c.stream) cudaStreamSynchronize(c.stream);
+  DevBuf* bufs[] = {&c.A, &c.B, &c.hin, &c.hout, &c.keysA, &c.keysB, &c.idxA, &c.idxB, &c.small, &c.radix};
+  for (DevBuf* b : bufs) b->release();
+  for (cudaEvent_t& e : c.ev)
+    if (e) cudaEventDestroy(e);
+  if (c.hc) cudaFreeHost(c.hc);
+  if (c.stream) cudaStreamDestroy(c.stream);
+  c.hc = nullptr;
+  c.stream = nullptr;
+}
 
 int get_ctx(Context** out) {
   int dev = 0;
@@ -150,10 +179,11 @@ int get_ctx(Context** out) {
   std::lock_guard<std::mutex> lk(g_ctx_mu);
   if (!g_ctx[dev]) {
     Context* c = new Context();
-    c->device = dev;
-    GB_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-    GB_CUDA(cudaMallocHost(&c->hc, sizeof(HostCounters)));
-    for (cudaEvent_t& e : c->ev) GB_CUDA(cudaEventCreate(&e));
+    int rc = ctx_init(*c, dev);
+    if (rc) {
+      delete c;
+      return rc;
+    }
     g_ctx[dev] = c;
   }
   *out = g_ctx[dev];
@@ -178,47 +208,50 @@ uint32_t pow2_ceil(uint64_t x) {
 }
 
 // ------------------------------------------------------------ LSD path --
+// Scratch of lsd_sort_keys for n keys of nwords words.
+size_t lsd_scratch_bytes(uint32_t n, int nwords) {
+  return (size_t)2 * 8 * 256 * 4 * nwords + (size_t)lsd_tiles(n) * 256 * 8 + 4096;
+}
+
 // Sorts key words (and idx) in place in keys / idx, ping-ponging through
-// keys2 / idx2.  Digits whose histogram puts every key in one bin are
-// skipped.  Returns the number of passes run (the result is in the first
-// buffer either way).
-int lsd_sort_keys(Context& c, Bump& bump, uint64_t* keys, uint64_t* keys2, uint32_t* idx, uint32_t* idx2,
-                  uint32_t n, int nwords, bool skip_trivial, int* passes_out, cudaStream_t st) {
-  const int g = lsd_grid(n);
-  uint32_t* counts = bump.take<uint32_t>((size_t)256 * g);
-  uint32_t* scan_tmp = bump.take<uint32_t>(scan_tmp_words((size_t)256 * g));
+// keys2 / idx2, one one-sweep pass per 8-bit digit.  With skip_trivial the
+// digit histograms are read back (one synchronisation) and digits whose
+// histogram puts every key in one bin are skipped.  Returns the number of
+// passes run (the result is in the first buffer either way).
+int lsd_sort_keys(Bump& bump, uint64_t* keys, uint64_t* keys2, uint32_t* idx, uint32_t* idx2, uint32_t n,
+                  int nwords, bool skip_trivial, int* passes_out, uint32_t* err, cudaStream_t st) {
+  uint32_t* hist = bump.take<uint32_t>((size_t)8 * 256 * nwords);
+  uint32_t* starts = bump.take<uint32_t>((size_t)8 * 256 * nwords);
+  unsigned long long* status = bump.take<unsigned long long>((size_t)lsd_tiles(n) * 256);
+  uint32_t* ticket = bump.take<uint32_t>(1);
+  GB_CUDA(lsd_digit_histograms(keys, n, nwords, hist, st));
+  GB_CUDA(lsd_digit_starts(hist, nwords, starts, st));
   std::vector<int> pass_word, pass_shift;
+  std::vector<uint32_t> h;
   if (skip_trivial) {
-    uint32_t* hist = bump.take<uint32_t>((size_t)8 * 256 * nwords);
-    GB_CUDA(lsd_digit_histograms(keys, n, nwords, hist, st));
-    std::vector<uint32_t> h((size_t)8 * 256 * nwords);
+    h.resize((size_t)8 * 256 * nwords);
     GB_CUDA(cudaMemcpyAsync(h.data(), hist, h.size() * 4, cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
-    for (int w = 0; w < nwords; ++w)
-      for (int d = 0; d < 8; ++d) {
-        bool trivial = false;
+  }
+  for (int w = 0; w < nwords; ++w)
+    for (int d = 0; d < 8; ++d) {
+      bool trivial = false;
+      if (skip_trivial)
         for (int b = 0; b < 256; ++b)
           if (h[((size_t)w * 8 + d) * 256 + b] == n) trivial = true;
-        if (!trivial) {
-          pass_word.push_back(w);
-          pass_shift.push_back(8 * d);
-        }
-      }
-  } else {
-    for (int w = 0; w < nwords; ++w)
-      for (int d = 0; d < 8; ++d) {
+      if (!trivial) {
         pass_word.push_back(w);
         pass_shift.push_back(8 * d);
       }
-  }
+    }
   uint64_t* kin = keys;
   uint64_t* kout = keys2;
   uint32_t* iin = idx;
   uint32_t* iout = idx2;
   for (size_t p = 0; p < pass_word.size(); ++p) {
-    GB_CUDA(lsd_count(kin + (size_t)pass_word[p] * n, n, pass_shift[p], counts, st));
-    GB_CUDA(exclusive_scan_u32(counts, counts, (size_t)256 * g, scan_tmp, st));
-    GB_CUDA(lsd_scatter(kin, iin, kout, iout, n, nwords, pass_word[p], pass_shift[p], counts, st));
+    const uint32_t* st_d = starts + ((size_t)pass_word[p] * 8 + pass_shift[p] / 8) * 256;
+    GB_CUDA(lsd_onesweep(kin, iin, kout, iout, n, nwords, pass_word[p], pass_shift[p], st_d, status, ticket, err,
+                         st));
     std::swap(kin, kout);
     std::swap(iin, iout);
   }
@@ -231,34 +264,56 @@ int lsd_sort_keys(Context& c, Bump& bump, uint64_t* keys, uint64_t* keys2, uint3
 }
 
 // Generic path over device records: keys from the descriptor (or from radix
-// bytes already on the device), LSD, then one gather into d_out.
-int run_lsd(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize, const gbsort_key_desc* key,
-            const uint8_t* d_radix, uint32_t rsize, cudaStream_t st) {
+// bytes already on the device), LSD, then one gather into d_out.  With
+// skip_trivial, constant digits are found on the host (one synchronisation)
+// and skipped; without, nothing waits for the host (graph capture).
+int lsd_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize, const gbsort_key_desc* key,
+                const uint8_t* d_radix, uint32_t rsize, bool skip_trivial, cudaStream_t st) {
   const int nwords = d_radix ? (int)((rsize + 7) / 8) : (int)key->nwords;
   GB_CUDA(c.keysA.ensure(sizeof(uint64_t) * (size_t)n * nwords));
   GB_CUDA(c.keysB.ensure(sizeof(uint64_t) * (size_t)n * nwords));
   GB_CUDA(c.idxA.ensure(sizeof(uint32_t) * (size_t)n));
   GB_CUDA(c.idxB.ensure(sizeof(uint32_t) * (size_t)n));
-  GB_CUDA(c.small.ensure((size_t)16 << 20));
+  if (d_in == d_out) GB_CUDA(c.A.ensure((size_t)n * elsize));
+  GB_CUDA(c.small.ensure(lsd_scratch_bytes(n, nwords) + CNT_WORDS * 4 + 4096));
   Bump bump{c.small.as<uint8_t>()};
+  uint32_t* counters = bump.take<uint32_t>(CNT_WORDS);
+  uint32_t* err = counters + CNT_ERR;
+  GB_CUDA(cudaMemsetAsync(counters, 0, CNT_WORDS * sizeof(uint32_t), st));
   if (d_radix) GB_CUDA(radix_bytes_to_keys(d_radix, n, rsize, c.keysA.as<uint64_t>(), c.idxA.as<uint32_t>(), st));
   else GB_CUDA(extract_keys(d_in, n, elsize, *key, c.keysA.as<uint64_t>(), c.idxA.as<uint32_t>(), st));
   int passes = 0;
-  int rc = lsd_sort_keys(c, bump, c.keysA.as<uint64_t>(), c.keysB.as<uint64_t>(), c.idxA.as<uint32_t>(),
-                         c.idxB.as<uint32_t>(), n, nwords, true, &passes, st);
+  int rc = lsd_sort_keys(bump, c.keysA.as<uint64_t>(), c.keysB.as<uint64_t>(), c.idxA.as<uint32_t>(),
+                         c.idxB.as<uint32_t>(), n, nwords, skip_trivial, &passes, err, st);
   if (rc) return rc;
   const void* src = d_in;
   if (d_in == d_out) {  // the gather needs an untouched copy of the input
-    GB_CUDA(c.A.ensure((size_t)n * elsize));
     GB_CUDA(cudaMemcpyAsync(c.A.p, d_in, (size_t)n * elsize, cudaMemcpyDeviceToDevice, st));
     src = c.A.p;
   }
   GB_CUDA(gather_records(src, d_out, c.idxA.as<uint32_t>(), n, elsize, st));
-  GB_CUDA(cudaStreamSynchronize(st));
+  GB_CUDA(cudaMemcpyAsync(c.hc->c, counters, CNT_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  c.run_lsd_passes = (uint32_t)passes;
+  return GBSORT_OK;
+}
+
+int lsd_collect(Context& c) {
+  if (c.hc->c[CNT_ERR]) {
+    set_err("device check failed in the LSD path: code %u", c.hc->c[CNT_ERR]);
+    return GBSORT_ERR_INTERNAL;
+  }
   g_stats = gbsort_stats{};
   g_stats.method = GBSORT_LSD;
-  g_stats.lsd_passes = (uint32_t)passes;
+  g_stats.lsd_passes = c.run_lsd_passes;
   return GBSORT_OK;
+}
+
+int run_lsd(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize, const gbsort_key_desc* key,
+            const uint8_t* d_radix, uint32_t rsize, cudaStream_t st) {
+  int rc = lsd_enqueue(c, d_in, d_out, n, elsize, key, d_radix, rsize, true, st);
+  if (rc) return rc;
+  GB_CUDA(cudaStreamSynchronize(st));
+  return lsd_collect(c);
 }
 
 // --------------------------------------------------------- hsort path ----
@@ -328,6 +383,7 @@ struct Level2 {
 };
 
 constexpr int kSplitRounds = 16;  // every round narrows each re-split range; 64-bit keys need few
+constexpr int kCdfEpochs = 8;     // gradient steps of the CDF model
 
 // The split rounds, then one pass over every local task.  The initial tasks
 // must already be in split[0] (count in nsplit[0]).
@@ -341,9 +397,11 @@ int run_level2(const HsortParams& p, const Level2& l2, uint32_t* stats, uint32_t
   return GBSORT_OK;
 }
 
-int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize, const gbsort_key_desc* key,
-              int method, cudaStream_t st) {
-  const bool learned = method == GBSORT_HISTOGRAM_LEARNED;
+// Enqueues the whole histogram sort on `st` without waiting for the host
+// anywhere (so it can be captured into a CUDA graph); the device counters
+// end up in c.hc once the stream reaches the end.  hsort_collect reads them.
+int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize, const gbsort_key_desc* key,
+                  bool learned, bool timing, cudaStream_t st) {
   GB_CUDA(c.A.ensure((size_t)n * elsize));
   GB_CUDA(c.B.ensure((size_t)n * elsize));
   const int nb = choose_buckets(n);
@@ -354,21 +412,23 @@ int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t el
   const int lbits = 11;
   const int nleaf = 1 << lbits;
   size_t small_bytes = (size_t)s * 16 + (size_t)nb * 8 + (size_t)nb * grid * 8 + Level2::bytes(cap_split, cap_local) +
-                       (size_t)256 * lsd_grid(std::max<uint32_t>(s, 1)) * 8 + (size_t)nleaf * 64 + (4 << 20);
+                       lsd_scratch_bytes(std::max<uint32_t>(s, 1), 1) + (size_t)nleaf * 64 + (size_t)nb * 4 +
+                       (4 << 20);
   GB_CUDA(c.small.ensure(small_bytes));
   Bump bump{c.small.as<uint8_t>()};
-  uint32_t* counters = bump.take<uint32_t>(64);  // stats, err, ntasks x2, work, iters, widest
+  uint32_t* counters = bump.take<uint32_t>(CNT_WORDS);
   uint32_t* stats = counters;
-  uint32_t* err = counters + STAT_SLOTS;  // kernels given `stats` also find the error word here
-  uint32_t* iters = counters + 21;
-  uint32_t* widest = counters + 22;
-  float* loss = reinterpret_cast<float*>(counters + 23);
-  GB_CUDA(cudaMemsetAsync(counters, 0, 64 * sizeof(uint32_t), st));
+  uint32_t* err = counters + CNT_ERR;
+  uint32_t* iters = counters + CNT_ITERS;
+  uint32_t* widest = counters + CNT_WIDEST;
+  float* loss = reinterpret_cast<float*>(counters + CNT_LOSS);
+  uint32_t* fallback = counters + CNT_FALLBACK;
+  GB_CUDA(cudaMemsetAsync(counters, 0, CNT_WORDS * sizeof(uint32_t), st));
   uint64_t* S = bump.take<uint64_t>((size_t)std::max(nb, 2));
   uint32_t* counts = bump.take<uint32_t>((size_t)nb * grid);
   uint32_t* scan_tmp = bump.take<uint32_t>(scan_tmp_words((size_t)nb * grid));
   Level2 l2;
-  l2.carve(bump, counters + 24, cap_split, cap_local);
+  l2.carve(bump, counters + CNT_L2, cap_split, cap_local);
 
   HsortParams p{};
   p.in = (const uint8_t*)d_in;
@@ -381,22 +441,20 @@ int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t el
 
   ModelDev model{};
   int lookup = LOOKUP_PLAIN;
-  bool splitter_fallback = false;
-  GB_CUDA(cudaEventRecord(c.ev[0], st));
+  if (timing) GB_CUDA(cudaEventRecord(c.ev[0], st));
   if (nb > 1) {
     uint64_t* sA = bump.take<uint64_t>(s);
     uint64_t* sB = bump.take<uint64_t>(s);
     GB_CUDA(sample_keys(p.in, n, elsize, p.key, s, sA, st));
-    int rc = lsd_sort_keys(c, bump, sA, sB, nullptr, nullptr, s, 1, false, nullptr, st);
+    int rc = lsd_sort_keys(bump, sA, sB, nullptr, nullptr, s, 1, false, nullptr, err, st);
     if (rc) return rc;
     if (!learned) {
       GB_CUDA(plain_splitters(sA, s, nb - 1, S, iters, nullptr, nullptr, st));
       GB_CUDA(finalize_splitters(S, nb - 1, st));
     } else {
-      GB_CUDA(cudaMemcpyAsync(&c.hc->kminmax[0], sA, 8, cudaMemcpyDeviceToHost, st));
-      GB_CUDA(cudaMemcpyAsync(&c.hc->kminmax[1], sA + s - 1, 8, cudaMemcpyDeviceToHost, st));
-      GB_CUDA(cudaStreamSynchronize(st));
-      CdfShape sh = cdf_shape(c.hc->kminmax[0], c.hc->kminmax[1], lbits);
+      CdfShape* dshape = bump.take<CdfShape>(1);
+      GB_CUDA(cdf_shape_device(sA, s, lbits, dshape, st));
+      const CdfShape sh = cdf_shape_ref(dshape, lbits);
       CdfWork w{};
       w.y = bump.take<float>(nleaf + 1);
       w.grad = bump.take<float>(nleaf + 1);
@@ -406,43 +464,34 @@ int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t el
       uint32_t* win = bump.take<uint32_t>(nleaf);
       uint32_t* wlo = bump.take<uint32_t>(nleaf);
       uint32_t* whi = bump.take<uint32_t>(nleaf);
-      const int epochs = 8;
-      GB_CUDA(cdf_train(sA, s, sh, epochs, 0.5f, w, st));
+      GB_CUDA(cdf_train(sA, s, sh, kCdfEpochs, 0.5f, w, st));
       GB_CUDA(cdf_splitters(sA, s, sh, nb, w.knots, S, st));
       GB_CUDA(finalize_splitters(S, nb - 1, st));
       // the plain splitters judge the model's: if the sample shows a heavy
       // key outside a single-key bucket or an overfull bucket, the sample's
-      // own quantiles (what the bisection converges to) replace them; the
-      // model still serves the lookup, with windows for the final splitters
+      // own quantiles (what the bisection converges to) replace them, on the
+      // device; the model still serves the lookup, with windows for the
+      // final splitters
       uint32_t* jcounts = bump.take<uint32_t>(nb);
-      uint32_t* jflag = bump.take<uint32_t>(1);
-      GB_CUDA(judge_splitters(sA, s, S, nb, jcounts, jflag, st));
-      GB_CUDA(cudaMemcpyAsync(&c.hc->err, jflag, 4, cudaMemcpyDeviceToHost, st));
-      GB_CUDA(cudaStreamSynchronize(st));
-      splitter_fallback = c.hc->err != 0;
-      if (splitter_fallback) {
-        GB_CUDA(quantile_splitters(sA, s, nb - 1, S, st));
-        GB_CUDA(finalize_splitters(S, nb - 1, st));
-      }
+      GB_CUDA(judge_splitters(sA, s, S, nb, jcounts, fallback, st));
+      GB_CUDA(quantile_splitters(sA, s, nb - 1, S, fallback, st));
+      GB_CUDA(finalize_splitters(S, nb - 1, st, fallback));
       GB_CUDA(cdf_windows(sh, nb, w.knots, S, win, wlo, whi, widest, st));
-      model.kmin = sh.kmin;
-      model.lshift = sh.lshift;
-      model.lbits = sh.lbits;
+      model.lbits = lbits;
       model.nbuckets = nb;
       model.knots = w.knots;
       model.win = win;
+      model.shape = dshape;
       lookup = LOOKUP_LEARNED;
-      GB_CUDA(cudaMemsetAsync(iters, 0, 4, st));
-      c.hc->iters = epochs;
     }
   }
-  GB_CUDA(cudaEventRecord(c.ev[1], st));
+  if (timing) GB_CUDA(cudaEventRecord(c.ev[1], st));
   GB_CUDA(l1_count(p, lookup, S, nb, lookup == LOOKUP_LEARNED ? &model : nullptr, counts, stats, st));
-  GB_CUDA(cudaEventRecord(c.ev[2], st));
+  if (timing) GB_CUDA(cudaEventRecord(c.ev[2], st));
   GB_CUDA(exclusive_scan_u32(counts, counts, (size_t)nb * grid, scan_tmp, st));
-  GB_CUDA(cudaEventRecord(c.ev[3], st));
+  if (timing) GB_CUDA(cudaEventRecord(c.ev[3], st));
   GB_CUDA(l1_scatter(p, lookup, S, nb, lookup == LOOKUP_LEARNED ? &model : nullptr, counts, stats, st));
-  GB_CUDA(cudaEventRecord(c.ev[4], st));
+  if (timing) GB_CUDA(cudaEventRecord(c.ev[4], st));
   {
     TaskListsHost L = l2.round(-1);  // appends to split[0]
     GB_CUDA(build_tasks(counts, grid, S, nb, n, L, err, stats, st));
@@ -452,53 +501,69 @@ int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t el
     TaskListsHost L = l2.round(r);
     GB_CUDA(cudaMemsetAsync(L.nsplit_out, 0, sizeof(uint32_t), st));
     GB_CUDA(run_split_round(p, L, l2.work, stats, err, st));
-    if (trace) {  // debugging aid: split tasks per round (synchronises)
+    if (trace && timing) {  // debugging aid: split tasks per round (synchronises)
       uint32_t h[3];
       GB_CUDA(cudaMemcpyAsync(h, l2.nsplit, 12, cudaMemcpyDeviceToHost, st));
       GB_CUDA(cudaStreamSynchronize(st));
       fprintf(stderr, "gbsort trace: round %d in %u out %u local %u\n", r, h[r & 1], h[(r + 1) & 1], h[2]);
     }
   }
-  GB_CUDA(cudaEventRecord(c.ev[5], st));
+  if (timing) GB_CUDA(cudaEventRecord(c.ev[5], st));
   GB_CUDA(run_local(p, l2.local, l2.nlocal, l2.cap_local, l2.work, stats, st));
-  GB_CUDA(cudaEventRecord(c.ev[6], st));
-  uint32_t learned_iters = learned ? c.hc->iters : 0;
-  GB_CUDA(cudaMemcpyAsync(c.hc->stats, counters, sizeof(uint32_t) * STAT_SLOTS, cudaMemcpyDeviceToHost, st));
-  GB_CUDA(cudaMemcpyAsync(&c.hc->err, err, 4, cudaMemcpyDeviceToHost, st));
-  GB_CUDA(cudaMemcpyAsync(c.hc->ntasks, l2.nsplit, 8, cudaMemcpyDeviceToHost, st));
-  GB_CUDA(cudaMemcpyAsync(&c.hc->iters, iters, 4, cudaMemcpyDeviceToHost, st));
-  GB_CUDA(cudaMemcpyAsync(&c.hc->widest, widest, 4, cudaMemcpyDeviceToHost, st));
-  GB_CUDA(cudaMemcpyAsync(&c.hc->loss, loss, 4, cudaMemcpyDeviceToHost, st));
-  GB_CUDA(cudaStreamSynchronize(st));
-  if (c.hc->err) {
-    set_err("device check failed: code %u", c.hc->err);
+  if (timing) GB_CUDA(cudaEventRecord(c.ev[6], st));
+  GB_CUDA(cudaMemcpyAsync(c.hc->c, counters, CNT_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  c.run_nbuckets = (uint32_t)nb;
+  c.run_sample = s;
+  c.run_learned = learned;
+  c.run_timing = timing;
+  return GBSORT_OK;
+}
+
+// Status and statistics of the last enqueued histogram sort, once its
+// stream has reached the end.
+int hsort_collect(Context& c) {
+  const uint32_t* h = c.hc->c;
+  if (h[CNT_ERR]) {
+    set_err("device check failed: code %u", h[CNT_ERR]);
     return GBSORT_ERR_INTERNAL;
   }
-  if (c.hc->ntasks[kSplitRounds & 1] != 0) {  // the last round's output list must be empty
-    set_err("split rounds did not finish: %u tasks left", c.hc->ntasks[kSplitRounds & 1]);
+  const uint32_t left = h[CNT_L2 + (kSplitRounds & 1)];  // the last round's output list must be empty
+  if (left != 0) {
+    set_err("split rounds did not finish: %u tasks left", left);
     return GBSORT_ERR_INTERNAL;
   }
   g_stats = gbsort_stats{};
-  g_stats.method = learned ? GBSORT_HISTOGRAM_LEARNED : GBSORT_HISTOGRAM_PLAIN;
-  g_stats.nbuckets = (uint32_t)nb;
-  g_stats.sample = s;
-  g_stats.splitter_rounds = learned ? learned_iters : c.hc->iters;
-  g_stats.local_sorts = c.hc->stats[STAT_LOCAL];
-  g_stats.splits = c.hc->stats[STAT_SPLIT];
-  g_stats.copies = c.hc->stats[STAT_COPY];
-  g_stats.resplits = c.hc->stats[STAT_PUSHED];
-  g_stats.bigbin_passes = c.hc->stats[STAT_BIGBIN];
-  g_stats.window_misses = c.hc->stats[STAT_WINDOW_MISS];
-  g_stats.max_bucket = c.hc->stats[STAT_MAX_BUCKET];
-  g_stats.widest_window = c.hc->widest;
-  g_stats.model_loss = learned ? c.hc->loss : 0.f;
-  g_stats.splitter_fallback = splitter_fallback ? 1u : 0u;
-  for (int i = 0; i < 6; ++i) {
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, c.ev[i], c.ev[i + 1]);
-    g_stats.stage_ms[i] = ms;
-  }
+  g_stats.method = c.run_learned ? GBSORT_HISTOGRAM_LEARNED : GBSORT_HISTOGRAM_PLAIN;
+  g_stats.nbuckets = c.run_nbuckets;
+  g_stats.sample = c.run_sample;
+  g_stats.splitter_rounds = c.run_learned ? (uint32_t)kCdfEpochs : h[CNT_ITERS];
+  g_stats.local_sorts = h[STAT_LOCAL];
+  g_stats.splits = h[STAT_SPLIT];
+  g_stats.copies = h[STAT_COPY];
+  g_stats.resplits = h[STAT_PUSHED];
+  g_stats.bigbin_passes = h[STAT_BIGBIN];
+  g_stats.window_misses = h[STAT_WINDOW_MISS];
+  g_stats.max_bucket = h[STAT_MAX_BUCKET];
+  g_stats.widest_window = h[CNT_WIDEST];
+  float loss;
+  memcpy(&loss, &h[CNT_LOSS], 4);
+  g_stats.model_loss = c.run_learned ? loss : 0.f;
+  g_stats.splitter_fallback = c.run_learned && h[CNT_FALLBACK] ? 1u : 0u;
+  if (c.run_timing)
+    for (int i = 0; i < 6; ++i) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, c.ev[i], c.ev[i + 1]);
+      g_stats.stage_ms[i] = ms;
+    }
   return GBSORT_OK;
+}
+
+int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize, const gbsort_key_desc* key,
+              int method, cudaStream_t st) {
+  int rc = hsort_enqueue(c, d_in, d_out, n, elsize, key, method == GBSORT_HISTOGRAM_LEARNED, true, st);
+  if (rc) return rc;
+  GB_CUDA(cudaStreamSynchronize(st));
+  return hsort_collect(c);
 }
 
 int sort_device_dispatch(Context& c, const void* d_in, void* d_out, size_t nmemb, size_t elsize,
@@ -665,13 +730,13 @@ int gbsort_sort_segments_device(const void* d_in, void* d_out, const uint64_t* s
   const uint32_t cap_local = 4u * (uint32_t)nseg + N / 512 + 65536;
   GB_CUDA(c->small.ensure(Level2::bytes(cap_split, cap_local) + (nseg + 1) * 8 + (1 << 20)));
   Bump bump{c->small.as<uint8_t>()};
-  uint32_t* counters = bump.take<uint32_t>(64);
+  uint32_t* counters = bump.take<uint32_t>(CNT_WORDS);
   uint32_t* stats = counters;
-  uint32_t* err = counters + STAT_SLOTS;
+  uint32_t* err = counters + CNT_ERR;
   uint64_t* offs = bump.take<uint64_t>(nseg + 1);
   Level2 l2;
-  l2.carve(bump, counters + 24, cap_split, cap_local);
-  GB_CUDA(cudaMemsetAsync(counters, 0, 64 * sizeof(uint32_t), st));
+  l2.carve(bump, counters + CNT_L2, cap_split, cap_local);
+  GB_CUDA(cudaMemsetAsync(counters, 0, CNT_WORDS * sizeof(uint32_t), st));
   GB_CUDA(cudaMemcpyAsync(offs, seg_offsets, (nseg + 1) * 8, cudaMemcpyHostToDevice, st));
   GB_CUDA(cudaMemcpyAsync(c->A.p, d_in, (size_t)N * E, cudaMemcpyDeviceToDevice, st));
   GB_CUDA(segment_ranges(c->A.as<uint8_t>(), E, key->word[0], offs, (uint32_t)nseg, kBigSegment, l2.split[0],
@@ -686,23 +751,22 @@ int gbsort_sort_segments_device(const void* d_in, void* d_out, const uint64_t* s
   p.key = key->word[0];
   rc = run_level2(p, l2, stats, err, st);
   if (rc) return rc;
-  GB_CUDA(cudaMemcpyAsync(c->hc->stats, counters, sizeof(uint32_t) * STAT_SLOTS, cudaMemcpyDeviceToHost, st));
-  GB_CUDA(cudaMemcpyAsync(&c->hc->err, err, 4, cudaMemcpyDeviceToHost, st));
-  GB_CUDA(cudaMemcpyAsync(c->hc->ntasks, l2.nsplit, 8, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(c->hc->c, counters, CNT_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaStreamSynchronize(st));
-  if (c->hc->err || c->hc->ntasks[kSplitRounds & 1]) {
-    set_err("segmented sort device check failed: code %u, %u tasks left", c->hc->err,
-            c->hc->ntasks[kSplitRounds & 1]);
+  const uint32_t* h = c->hc->c;
+  if (h[CNT_ERR] || h[CNT_L2 + (kSplitRounds & 1)]) {
+    set_err("segmented sort device check failed: code %u, %u tasks left", h[CNT_ERR],
+            h[CNT_L2 + (kSplitRounds & 1)]);
     return GBSORT_ERR_INTERNAL;
   }
   g_stats = gbsort_stats{};
   g_stats.method = GBSORT_HISTOGRAM_PLAIN;
   g_stats.nbuckets = (uint32_t)nseg;
-  g_stats.local_sorts = c->hc->stats[STAT_LOCAL];
-  g_stats.splits = c->hc->stats[STAT_SPLIT];
-  g_stats.copies = c->hc->stats[STAT_COPY];
-  g_stats.resplits = c->hc->stats[STAT_PUSHED];
-  g_stats.bigbin_passes = c->hc->stats[STAT_BIGBIN];
+  g_stats.local_sorts = h[STAT_LOCAL];
+  g_stats.splits = h[STAT_SPLIT];
+  g_stats.copies = h[STAT_COPY];
+  g_stats.resplits = h[STAT_PUSHED];
+  g_stats.bigbin_passes = h[STAT_BIGBIN];
   return GBSORT_OK;
 }
 
@@ -787,10 +851,15 @@ int gbsort_debug_bisect(const uint64_t* sorted, uint32_t s, int nsplit, uint64_t
   return GBSORT_OK;
 }
 
-int gbsort_debug_buckets(const uint64_t* sample, uint32_t s, int nbuckets, const uint64_t* keys, uint32_t nkeys,
-                         uint32_t* bucket_search, uint32_t* bucket_learned, uint64_t* splitters,
-                         uint32_t* widest_window) {
-  if (!sample || s == 0 || nbuckets < 2 || nbuckets > 8192 || !keys) return GBSORT_ERR_BAD_ARG;
+namespace {
+// Trains the model on the sample for `epochs` steps and looks every key up
+// with the model (window search) and with the full search; see
+// gbsort_debug_buckets and gbsort_debug_model.
+int debug_model(const uint64_t* sample, uint32_t s, int nbuckets, int epochs, const uint64_t* keys, uint32_t nkeys,
+                uint32_t* bucket_search, uint32_t* bucket_learned, uint64_t* splitters, uint32_t* widest_window,
+                float* loss, uint64_t* reads) {
+  if (!sample || s == 0 || nbuckets < 2 || nbuckets > 8192 || !keys || epochs < 0 || epochs > 1000)
+    return GBSORT_ERR_BAD_ARG;
   Context* c = nullptr;
   int rc = get_ctx(&c);
   if (rc) return rc;
@@ -805,11 +874,13 @@ int gbsort_debug_buckets(const uint64_t* sample, uint32_t s, int nbuckets, const
   uint32_t* ds = bump.take<uint32_t>(nkeys);
   uint64_t* S = bump.take<uint64_t>(nbuckets);
   uint32_t* misc = bump.take<uint32_t>(4);
+  unsigned long long* dreads = bump.take<unsigned long long>(2);
   CdfWork w{};
   w.y = bump.take<float>(nleaf + 1);
   w.grad = bump.take<float>(nleaf + 1);
   w.h = bump.take<float>(nleaf + 1);
   w.knots = bump.take<float2>(nleaf);
+  w.loss = bump.take<float>(1);
   uint32_t* win = bump.take<uint32_t>(nleaf);
   uint32_t* wlo = bump.take<uint32_t>(nleaf);
   uint32_t* whi = bump.take<uint32_t>(nleaf);
@@ -819,8 +890,9 @@ int gbsort_debug_buckets(const uint64_t* sample, uint32_t s, int nbuckets, const
   GB_CUDA(cudaMemcpyAsync(dx, hs.data(), (size_t)s * 8, cudaMemcpyHostToDevice, st));
   GB_CUDA(cudaMemcpyAsync(dk, keys, (size_t)nkeys * 8, cudaMemcpyHostToDevice, st));
   GB_CUDA(cudaMemsetAsync(misc, 0, 16, st));
+  GB_CUDA(cudaMemsetAsync(dreads, 0, 16, st));
   CdfShape sh = cdf_shape(hs.front(), hs.back(), lbits);
-  GB_CUDA(cdf_train(dx, s, sh, 8, 0.5f, w, st));
+  GB_CUDA(cdf_train(dx, s, sh, epochs, 0.5f, w, st));
   GB_CUDA(cdf_splitters(dx, s, sh, nbuckets, w.knots, S, st));
   GB_CUDA(finalize_splitters(S, nbuckets - 1, st));
   GB_CUDA(cdf_windows(sh, nbuckets, w.knots, S, win, wlo, whi, misc, st));
@@ -831,16 +903,40 @@ int gbsort_debug_buckets(const uint64_t* sample, uint32_t s, int nbuckets, const
   m.nbuckets = nbuckets;
   m.knots = w.knots;
   m.win = win;
-  GB_CUDA(probe_buckets(dk, nkeys, S, &m, dl, ds, misc + 1, st));
+  GB_CUDA(probe_buckets(dk, nkeys, S, &m, dl, ds, misc + 1, dreads, st));
   if (bucket_learned) GB_CUDA(cudaMemcpyAsync(bucket_learned, dl, (size_t)nkeys * 4, cudaMemcpyDeviceToHost, st));
   if (bucket_search) GB_CUDA(cudaMemcpyAsync(bucket_search, ds, (size_t)nkeys * 4, cudaMemcpyDeviceToHost, st));
   if (splitters) GB_CUDA(cudaMemcpyAsync(splitters, S, (size_t)(nbuckets - 1) * 8, cudaMemcpyDeviceToHost, st));
   uint32_t hm[2] = {0, 0};
+  unsigned long long hr[2] = {0, 0};
+  float hl = 0.f;
   GB_CUDA(cudaMemcpyAsync(hm, misc, 8, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(hr, dreads, 16, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(&hl, w.loss, 4, cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaStreamSynchronize(st));
   if (widest_window) *widest_window = hm[0];
+  if (loss) *loss = hl;
+  if (reads) {
+    reads[0] = hr[0];
+    reads[1] = hr[1];
+  }
   g_stats.window_misses = hm[1];
   return GBSORT_OK;
+}
+}  // namespace
+
+int gbsort_debug_buckets(const uint64_t* sample, uint32_t s, int nbuckets, const uint64_t* keys, uint32_t nkeys,
+                         uint32_t* bucket_search, uint32_t* bucket_learned, uint64_t* splitters,
+                         uint32_t* widest_window) {
+  return debug_model(sample, s, nbuckets, 8, keys, nkeys, bucket_search, bucket_learned, splitters, widest_window,
+                     nullptr, nullptr);
+}
+
+int gbsort_debug_model(const uint64_t* sample, uint32_t s, int nbuckets, int epochs, const uint64_t* keys,
+                       uint32_t nkeys, uint32_t* bucket_search, uint32_t* bucket_learned, float* loss,
+                       uint64_t* reads, uint32_t* widest_window) {
+  return debug_model(sample, s, nbuckets, epochs, keys, nkeys, bucket_search, bucket_learned, nullptr,
+                     widest_window, loss, reads);
 }
 
 int gbsort_last_stats(gbsort_stats* out) {
@@ -885,6 +981,141 @@ int gbsort_release(void) {
 }
 
 const char* gbsort_version(void) { return "gbsort 0.1.0 (sm_103a)"; }
+
+// ------------------------------------------------------- graph plans ----
+struct gbsort_plan {
+  Context ctx;                       // the plan's own scratch, counters and capture stream
+  size_t nmemb = 0, elsize = 0;
+  gbsort_key_desc key{};
+  int method = GBSORT_AUTO;          // as requested; resolved per capture
+  int resolved = GBSORT_AUTO;
+  const void* in = nullptr;          // buffers the graph was captured with
+  void* out = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t done = nullptr;
+  uint32_t kernels = 0;              // kernel launches in the graph
+  bool pending = false;
+};
+
+int gbsort_plan_create(gbsort_plan** plan, size_t nmemb, size_t elsize, const gbsort_key_desc* key, int method) {
+  if (!plan) return GBSORT_ERR_BAD_ARG;
+  *plan = nullptr;
+  if (nmemb == 0 || nmemb >= 0xffffffffull || elsize == 0 || elsize > (1u << 20) || !key_ok(key, elsize) ||
+      method < GBSORT_AUTO || method > GBSORT_LSD) {
+    set_err("bad plan arguments");
+    return GBSORT_ERR_BAD_ARG;
+  }
+  Context* probe = nullptr;
+  int rc = get_ctx(&probe);  // checks for a device
+  if (rc) return rc;
+  gbsort_plan* p = new gbsort_plan();
+  rc = ctx_init(p->ctx, probe->device);
+  if (rc == GBSORT_OK && cudaEventCreateWithFlags(&p->done, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    rc = GBSORT_ERR_CUDA;
+  }
+  if (rc) {
+    ctx_destroy(p->ctx);
+    delete p;
+    return rc;
+  }
+  p->nmemb = nmemb;
+  p->elsize = elsize;
+  p->key = *key;
+  p->method = method;
+  *plan = p;
+  return GBSORT_OK;
+}
+
+// Captures the pipeline for (in, out) into the plan's graph.
+static int plan_capture(gbsort_plan* p, const void* in, void* out) {
+  Context& c = p->ctx;
+  const uint32_t n = (uint32_t)p->nmemb, E = (uint32_t)p->elsize;
+  const bool hs_ok = hsort_layout_ok(in, out, E, &p->key);
+  int m = p->method == GBSORT_AUTO ? (hs_ok ? GBSORT_HISTOGRAM_LEARNED : GBSORT_LSD) : p->method;
+  if (m != GBSORT_LSD && !hs_ok) {
+    set_err("histogram sort needs a one-word key at a 4-byte offset and a record size of 8-64 bytes");
+    return GBSORT_ERR_UNSUPPORTED;
+  }
+  // relaxed capture: buffer growth (cudaMalloc) may happen while capturing
+  GB_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeRelaxed));
+  const unsigned long long l0 = launch_count();
+  int rc = m == GBSORT_LSD ? lsd_enqueue(c, in, out, n, E, &p->key, nullptr, 0, false, c.stream)
+                           : hsort_enqueue(c, in, out, n, E, &p->key, m == GBSORT_HISTOGRAM_LEARNED, false, c.stream);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c.stream, &g);
+  if (rc || e != cudaSuccess) {
+    cudaGetLastError();
+    if (g) cudaGraphDestroy(g);
+    if (!rc) set_err("graph capture failed: %s", cudaGetErrorString(e));
+    return rc ? rc : GBSORT_ERR_CUDA;
+  }
+  p->kernels = (uint32_t)(launch_count() - l0);
+  if (p->exec) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(p->exec, g, &info) != cudaSuccess) {
+      cudaGetLastError();
+      cudaGraphExecDestroy(p->exec);
+      p->exec = nullptr;
+    }
+  }
+  if (!p->exec) {
+    e = cudaGraphInstantiate(&p->exec, g, 0);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      cudaGraphDestroy(g);
+      p->exec = nullptr;
+      set_err("graph instantiation failed: %s", cudaGetErrorString(e));
+      return GBSORT_ERR_CUDA;
+    }
+  }
+  if (p->graph) cudaGraphDestroy(p->graph);
+  p->graph = g;
+  p->in = in;
+  p->out = out;
+  p->resolved = m;
+  return GBSORT_OK;
+}
+
+int gbsort_plan_sort(gbsort_plan* p, const void* d_in, void* d_out, void* stream) {
+  if (!p || !d_in || !d_out) return GBSORT_ERR_BAD_ARG;
+  if (p->pending) {  // the previous launch must be collected first
+    int rc = gbsort_plan_wait(p);
+    if (rc) return rc;
+  }
+  if (!p->exec || d_in != p->in || d_out != p->out) {
+    int rc = plan_capture(p, d_in, d_out);
+    if (rc) return rc;
+  }
+  cudaStream_t st = stream ? (cudaStream_t)stream : p->ctx.stream;
+  GB_CUDA(cudaGraphLaunch(p->exec, st));
+  GB_CUDA(cudaEventRecord(p->done, st));
+  note_launches(p->kernels);
+  p->pending = true;
+  return GBSORT_OK;
+}
+
+int gbsort_plan_wait(gbsort_plan* p) {
+  if (!p) return GBSORT_ERR_BAD_ARG;
+  if (!p->pending) return GBSORT_OK;
+  p->pending = false;
+  GB_CUDA(cudaEventSynchronize(p->done));
+  int rc = p->resolved == GBSORT_LSD ? lsd_collect(p->ctx) : hsort_collect(p->ctx);
+  if (rc == GBSORT_OK) g_stats.launches = p->kernels;
+  return rc;
+}
+
+int gbsort_plan_destroy(gbsort_plan* p) {
+  if (!p) return GBSORT_OK;
+  if (p->pending) cudaEventSynchronize(p->done);
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  if (p->done) cudaEventDestroy(p->done);
+  ctx_destroy(p->ctx);
+  delete p;
+  return GBSORT_OK;
+}
 
 // ---------------------------------------------------------- drop-ins ----
 void mpsort_radix_desc(const void* ptr, void* radix, void* arg) {

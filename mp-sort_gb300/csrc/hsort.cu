@@ -191,8 +191,9 @@ __global__ void k_plain_splitters(const uint64_t* __restrict__ sample, uint32_t 
 // Runs of equal splitters become single-key buckets: [.., k, k, k, ..] ->
 // [.., k, k+1, k+1, ..], so every record of a heavy key k lands in the bucket
 // [k, k+1) and needs no sort at all.
-__global__ void __launch_bounds__(1024) k_finalize_splitters(uint64_t* S, int nsplit) {
+__global__ void __launch_bounds__(1024) k_finalize_splitters(uint64_t* S, int nsplit, const uint32_t* only_if) {
   constexpr int PER = 8;  // nsplit <= 8192
+  if (only_if && *only_if == 0) return;
   uint64_t cur[PER], prev[PER];
 #pragma unroll
   for (int j = 0; j < PER; ++j) {
@@ -262,6 +263,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_count(HsortParams p, const u
                                                         int nbuckets, ModelDev model,
                                                         uint32_t* __restrict__ counts,
                                                         uint32_t* __restrict__ stats) {
+  model = resolve_model(model);
   extern __shared__ __align__(16) uint8_t smem[];
   LookupSmem L;
   uint32_t* hist = reinterpret_cast<uint32_t*>(load_lookup<LK>(smem, S, nbuckets, model, L));
@@ -314,6 +316,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
                                                              int nbuckets, ModelDev model,
                                                              const uint32_t* __restrict__ offsets,
                                                              int nchunks, uint32_t* __restrict__ stats) {
+  model = resolve_model(model);
   uint32_t* err = stats + STAT_SLOTS;  // the error word follows the statistics
   constexpr int RPT = Tile<EW>::kRpt, T = Tile<EW>::kSize;
   using Rank = BlockRank<RPT, 7>;
@@ -990,10 +993,10 @@ cudaError_t plain_splitters(const uint64_t* sorted_sample, uint32_t s, int nspli
   return cudaGetLastError();
 }
 
-cudaError_t finalize_splitters(uint64_t* splitters, int nsplit, cudaStream_t stream) {
+cudaError_t finalize_splitters(uint64_t* splitters, int nsplit, cudaStream_t stream, const uint32_t* only_if) {
   if (nsplit <= 1) return cudaSuccess;
   if (nsplit > 8192) return cudaErrorInvalidValue;
-  k_finalize_splitters<<<1, 1024, 0, stream>>>(splitters, nsplit);
+  k_finalize_splitters<<<1, 1024, 0, stream>>>(splitters, nsplit, only_if);
   note_launches(1);
   return cudaGetLastError();
 }

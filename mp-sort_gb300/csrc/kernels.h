@@ -36,16 +36,17 @@ cudaError_t radix_bytes_to_keys(const uint8_t* radix, uint32_t n, uint32_t rsize
 // 256-bin histograms of all 8 * nwords digits in one read ([digit][256]).
 cudaError_t lsd_digit_histograms(const uint64_t* keys, uint32_t n, int nwords, uint32_t* hist,
                                  cudaStream_t stream);
-// Grid size used by lsd_count / lsd_scatter.
-int lsd_grid(uint32_t n);
-// One LSD pass on digit (word, shift): per-chunk counts, then stable scatter
-// of all key words (and idx, if not null) using offsets = exclusive scan of
-// counts ([256][grid]).
-cudaError_t lsd_count(const uint64_t* keys_word, uint32_t n, int shift, uint32_t* counts,
-                      cudaStream_t stream);
-cudaError_t lsd_scatter(const uint64_t* keys_in, const uint32_t* idx_in, uint64_t* keys_out,
-                        uint32_t* idx_out, uint32_t n, int nwords, int word, int shift,
-                        const uint32_t* offsets, cudaStream_t stream);
+// Exclusive scans of those histograms: the first output slot of every bin.
+cudaError_t lsd_digit_starts(const uint32_t* hist, int nwords, uint32_t* starts, cudaStream_t stream);
+// Tiles of one LSD pass over n keys (status words needed: 256 per tile).
+uint32_t lsd_tiles(uint32_t n);
+// One one-sweep LSD pass on digit (word, shift): stable scatter of all key
+// words (and idx, if not null) with offsets from starts (256 entries of this
+// digit) plus a decoupled look-back over the tiles; status and ticket are
+// scratch (zeroed here); err receives DEV_ERR_TIMEOUT if a wait gave up.
+cudaError_t lsd_onesweep(const uint64_t* keys_in, const uint32_t* idx_in, uint64_t* keys_out, uint32_t* idx_out,
+                         uint32_t n, int nwords, int word, int shift, const uint32_t* starts,
+                         unsigned long long* status, uint32_t* ticket, uint32_t* err, cudaStream_t stream);
 // out[i] = in[idx[i]] for records of elsize bytes.
 cudaError_t gather_records(const void* in, void* out, const uint32_t* idx, uint32_t n,
                            uint32_t elsize, cudaStream_t stream);
@@ -94,7 +95,7 @@ cudaError_t sample_keys(const uint8_t* rec, uint32_t n, uint32_t elsize, gbsort_
 cudaError_t plain_splitters(const uint64_t* sorted_sample, uint32_t s, int nsplit,
                             uint64_t* splitters, uint32_t* iters, int64_t* clt, int64_t* cle,
                             cudaStream_t stream);
-cudaError_t finalize_splitters(uint64_t* splitters, int nsplit, cudaStream_t stream);
+cudaError_t finalize_splitters(uint64_t* splitters, int nsplit, cudaStream_t stream, const uint32_t* only_if = nullptr);
 // Level-1 bucket counts per chunk ([nbuckets][grid]) and the stable scatter.
 // `model` points to a host copy of the ModelDev (cdf.cuh) for the learned
 // lookup, else null.  `stats` is the device statistics array (Stat indices).

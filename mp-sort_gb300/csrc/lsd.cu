@@ -6,13 +6,16 @@
 // host radix() callback) and sorts the sample of the histogram sort.  It
 // reproduces the reference's ordering -- a stable sort by the radix as a
 // little-endian unsigned integer (radixsort.c:19-44, stdlib/msort.c:52-174)
-// -- with 8-bit digit passes:
-//   * one read of the keys builds the histograms of every digit, so passes
-//     whose digit is constant are skipped by the host;
-//   * per pass, each CTA counts digits over its contiguous chunk, the
-//     (digit x chunk) matrix is scanned, and each CTA re-reads its chunk and
-//     scatters stably: tile ranks come from warp match ranking, chunk order
-//     from the scanned offsets.
+// -- with 8-bit digit passes in a one-sweep design:
+//   * one read of the keys builds the histograms of every digit; their
+//     exclusive scans give each digit's first output slot in every pass
+//     (and passes whose digit is constant can be skipped by the host);
+//   * each pass is then ONE kernel: a CTA takes the next tile by ticket,
+//     ranks its digits stably (warp match ranking), publishes the tile's
+//     per-digit counts and looks back over the previous tiles' published
+//     counts for its global offsets (decoupled look-back, bounded spins),
+//     stages the tile in digit order in shared memory and writes it out in
+//     runs, so every key is read once and written once per pass.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -22,13 +25,6 @@ namespace {
 
 constexpr int kLsdRpt = 8;                      // items per thread per tile
 constexpr int kLsdTile = kThreads * kLsdRpt;    // 4096
-
-__host__ __device__ __forceinline__ uint32_t chunk_begin(uint32_t n, uint32_t c, uint32_t g) {
-  return (uint32_t)(((uint64_t)n * c / g) & ~(uint64_t)31);
-}
-__host__ __device__ __forceinline__ uint32_t chunk_end(uint32_t n, uint32_t c, uint32_t g) {
-  return c + 1 == g ? n : chunk_begin(n, c + 1, g);
-}
 
 __global__ void k_extract_keys(const uint8_t* __restrict__ rec, uint32_t n, uint32_t elsize,
                                gbsort_key_desc key, int aligned4, uint64_t* __restrict__ keys,
@@ -73,77 +69,124 @@ __global__ void __launch_bounds__(kThreads) k_digit_hist(const uint64_t* __restr
     if (h[i]) atomicAdd(&hist[i], h[i]);
 }
 
-__global__ void __launch_bounds__(kThreads) k_lsd_count(const uint64_t* __restrict__ keys, uint32_t n,
-                                                         int shift, uint32_t* __restrict__ counts) {
-  __shared__ uint32_t h[256];
-  const uint32_t c = blockIdx.x, g = gridDim.x;
-  const uint32_t b = chunk_begin(n, c, g), e = chunk_end(n, c, g);
-  for (int i = threadIdx.x; i < 256; i += kThreads) h[i] = 0;
-  __syncthreads();
-  for (uint32_t i0 = b; i0 < e; i0 += kThreads) {
-    uint32_t i = i0 + threadIdx.x;
-    bool v = i < e;
-    uint32_t d = v ? (uint32_t)(keys[i] >> shift) & 255u : 0xffffffffu;
-    uint32_t peers = __match_any_sync(GB_FULL_MASK, d);
-    if (v && (peers & lanemask_lt()) == 0) atomicAdd(&h[d], (uint32_t)__popc(peers));
-  }
-  __syncthreads();
-  for (int d = threadIdx.x; d < 256; d += kThreads) counts[(size_t)d * g + c] = h[d];
+// Exclusive scans of the 256-bin histograms: one block per (word, digit).
+__global__ void __launch_bounds__(256) k_digit_starts(const uint32_t* __restrict__ hist,
+                                                      uint32_t* __restrict__ starts) {
+  __shared__ uint32_t tmp[8];
+  const uint32_t v = hist[blockIdx.x * 256 + threadIdx.x];
+  starts[blockIdx.x * 256 + threadIdx.x] = block_exclusive_scan<uint32_t, 256>(v, tmp, nullptr);
 }
 
+// Look-back status word of (tile, digit): a 2-bit flag over a 62-bit count.
+constexpr unsigned long long kStatAgg = 1ull << 62;     // the tile's own count
+constexpr unsigned long long kStatPrefix = 2ull << 62;  // count of every tile up to this one
+constexpr unsigned long long kStatValue = (1ull << 62) - 1;
+constexpr uint32_t kLookbackSpins = 1u << 22;           // ~1 s of polling, then an error
+
+__device__ __forceinline__ void st_relaxed(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// One LSD pass on digit (word, shift).  starts[d] = first output slot of
+// digit d; status holds ntiles * 256 zeroed words; *ticket starts at 0.
 template <int NW, bool IDX>
-__global__ void __launch_bounds__(kThreads) k_lsd_scatter(const uint64_t* __restrict__ keys_in,
-                                                           const uint32_t* __restrict__ idx_in,
-                                                           uint64_t* __restrict__ keys_out,
-                                                           uint32_t* __restrict__ idx_out, uint32_t n,
-                                                           int word, int shift,
-                                                           const uint32_t* __restrict__ offsets) {
+__global__ void __launch_bounds__(kThreads) k_lsd_onesweep(const uint64_t* __restrict__ keys_in,
+                                                            const uint32_t* __restrict__ idx_in,
+                                                            uint64_t* __restrict__ keys_out,
+                                                            uint32_t* __restrict__ idx_out, uint32_t n, int word,
+                                                            int shift, const uint32_t* __restrict__ starts,
+                                                            unsigned long long* status, uint32_t* ticket,
+                                                            uint32_t* err) {
   using Rank = BlockRank<kLsdRpt, 8>;
   __shared__ uint16_t hist[Rank::kCounters];
   __shared__ uint32_t scan_tmp[kWarps];
   __shared__ uint32_t start[257];
-  __shared__ uint32_t cursor[256];
-  const uint32_t c = blockIdx.x, g = gridDim.x;
-  const uint32_t cb = chunk_begin(n, c, g), ce = chunk_end(n, c, g);
-  for (int d = threadIdx.x; d < 256; d += kThreads) cursor[d] = offsets[(size_t)d * g + c];
+  __shared__ uint32_t base[256];
+  __shared__ uint32_t tile_s;
+  extern __shared__ __align__(16) uint8_t smem[];
+  uint64_t* skeys = reinterpret_cast<uint64_t*>(smem);  // [NW][kLsdTile], digit order
+  uint32_t* sidx = reinterpret_cast<uint32_t*>(skeys + NW * kLsdTile);
+
+  // tiles go out in ticket order, so every tile a CTA looks back at belongs
+  // to a CTA that is already running
+  if (threadIdx.x == 0) tile_s = atomicAdd(ticket, 1u);
   __syncthreads();
+  const uint32_t tile = tile_s;
+  const uint32_t t = tile * (uint32_t)kLsdTile;
+  const uint32_t nvalid = min((uint32_t)kLsdTile, n - t);
   const uint32_t w = warp_id(), lane = lane_id();
-  for (uint32_t t = cb; t < ce; t += kLsdTile) {
-    uint64_t k[NW][kLsdRpt];
-    uint32_t ix[kLsdRpt];
-    uint32_t digit[kLsdRpt], pos[kLsdRpt];
-    uint32_t nvalid = min((uint32_t)kLsdTile, ce - t);
+  // only the digit's word stays in registers across the ranking; the other
+  // words (and the index) are read after it, straight into place
+  const uint64_t* kdig = keys_in + (size_t)word * n + t;
+  uint64_t k[kLsdRpt];
+  uint32_t digit[kLsdRpt], pos[kLsdRpt];
 #pragma unroll
-    for (int r = 0; r < kLsdRpt; ++r) {
-      uint32_t e = w * 32 * kLsdRpt + r * 32 + lane;
-      bool valid = e < nvalid;
+  for (int r = 0; r < kLsdRpt; ++r) {
+    uint32_t e = w * 32 * kLsdRpt + r * 32 + lane;
+    bool valid = e < nvalid;
+    k[r] = valid ? kdig[e] : 0;
+    // padding items take the last digit and, being last in the tile, rank
+    // after every real item
+    digit[r] = valid ? (uint32_t)(k[r] >> shift) & 255u : 255u;
+  }
+  Rank::rank(digit, pos, hist, scan_tmp, start);
 #pragma unroll
-      for (int q = 0; q < NW; ++q) k[q][r] = valid ? keys_in[(size_t)q * n + t + e] : 0;
-      if (IDX) ix[r] = valid ? idx_in[t + e] : 0;
-      uint64_t kw = 0;
+  for (int r = 0; r < kLsdRpt; ++r) {
+    const uint32_t e = w * 32 * kLsdRpt + r * 32 + lane;
+    if (pos[r] < nvalid) {
 #pragma unroll
-      for (int q = 0; q < NW; ++q) kw = (q == word) ? k[q][r] : kw;
-      digit[r] = valid ? (uint32_t)(kw >> shift) & 255u : 255u;
+      for (int q = 0; q < NW; ++q)
+        skeys[q * kLsdTile + pos[r]] = q == word ? k[r] : keys_in[(size_t)q * n + t + e];
+      if (IDX) sidx[pos[r]] = idx_in[t + e];
     }
-    Rank::rank(digit, pos, hist, scan_tmp, start);
-#pragma unroll
-    for (int r = 0; r < kLsdRpt; ++r) {
-      uint32_t e = w * 32 * kLsdRpt + r * 32 + lane;
-      if (e < nvalid) {
-        uint32_t d = digit[r];
-        uint32_t dest = cursor[d] + pos[r] - start[d];
-#pragma unroll
-        for (int q = 0; q < NW; ++q) keys_out[(size_t)q * n + dest] = k[q][r];
-        if (IDX) idx_out[dest] = ix[r];
+  }
+  if (threadIdx.x < 256) {
+    const uint32_t d = threadIdx.x;
+    uint32_t cnt = start[d + 1] - start[d];
+    if (d == 255) cnt -= (uint32_t)kLsdTile - nvalid;
+    unsigned long long* mine = status + (size_t)tile * 256 + d;
+    unsigned long long excl = 0;
+    if (tile == 0) {
+      st_relaxed(mine, kStatPrefix | cnt);
+    } else {
+      st_relaxed(mine, kStatAgg | cnt);
+      uint32_t j = tile - 1, spins = 0;
+      for (;;) {
+        const unsigned long long v = ld_relaxed(status + (size_t)j * 256 + d);
+        const unsigned long long f = v & ~kStatValue;
+        if (f == 0) {  // tile j has not published yet
+          if (++spins > kLookbackSpins) {
+            set_error(err, DEV_ERR_TIMEOUT);
+            break;
+          }
+          __nanosleep(spins < 32 ? 32 : 256);
+          continue;
+        }
+        excl += v & kStatValue;
+        if (f == kStatPrefix || j == 0) break;
+        --j;
       }
+      st_relaxed(mine, kStatPrefix | (excl + cnt));
     }
-    __syncthreads();
-    for (int d = threadIdx.x; d < 256; d += kThreads) {
-      uint32_t cnt = start[d + 1] - start[d];
-      if (d == 255) cnt -= (uint32_t)kLsdTile - nvalid;  // the padding items sit at the end
-      cursor[d] += cnt;
+    base[d] = starts[d] + (uint32_t)excl - start[d];
+  }
+  __syncthreads();
+  // runs of equal digits go to consecutive output slots
+  for (uint32_t i = threadIdx.x; i < nvalid; i += kThreads) {
+    const uint32_t d = (uint32_t)(skeys[word * kLsdTile + i] >> shift) & 255u;
+    const uint32_t dest = base[d] + i;
+    if (dest >= n) {
+      set_error(err, DEV_ERR_COUNT_MISMATCH);
+      continue;
     }
-    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NW; ++q) keys_out[(size_t)q * n + dest] = skeys[q * kLsdTile + i];
+    if (IDX) idx_out[dest] = sidx[i];
   }
 }
 
@@ -213,31 +256,41 @@ cudaError_t lsd_digit_histograms(const uint64_t* keys, uint32_t n, int nwords, u
   return cudaGetLastError();
 }
 
-int lsd_grid(uint32_t n) {
-  uint64_t g = ((uint64_t)n + kLsdTile - 1) / kLsdTile;
-  uint64_t cap = (uint64_t)num_sms() * 2;
-  return (int)(g < 1 ? 1 : (g > cap ? cap : g));
-}
-
-cudaError_t lsd_count(const uint64_t* keys_word, uint32_t n, int shift, uint32_t* counts,
-                      cudaStream_t stream) {
-  k_lsd_count<<<lsd_grid(n), kThreads, 0, stream>>>(keys_word, n, shift, counts);
+cudaError_t lsd_digit_starts(const uint32_t* hist, int nwords, uint32_t* starts, cudaStream_t stream) {
+  k_digit_starts<<<8 * nwords, 256, 0, stream>>>(hist, starts);
   note_launches(1);
   return cudaGetLastError();
 }
 
-cudaError_t lsd_scatter(const uint64_t* keys_in, const uint32_t* idx_in, uint64_t* keys_out,
-                        uint32_t* idx_out, uint32_t n, int nwords, int word, int shift,
-                        const uint32_t* offsets, cudaStream_t stream) {
-  int g = lsd_grid(n);
-#define GB_LSD_CASE(NWV)                                                                            \
-  case NWV:                                                                                         \
-    if (idx_in)                                                                                     \
-      k_lsd_scatter<NWV, true><<<g, kThreads, 0, stream>>>(keys_in, idx_in, keys_out, idx_out, n,   \
-                                                           word, shift, offsets);                   \
-    else                                                                                            \
-      k_lsd_scatter<NWV, false><<<g, kThreads, 0, stream>>>(keys_in, idx_in, keys_out, idx_out, n,  \
-                                                            word, shift, offsets);                  \
+uint32_t lsd_tiles(uint32_t n) { return (uint32_t)(((uint64_t)n + kLsdTile - 1) / kLsdTile); }
+
+template <int NW, bool IDX>
+static cudaError_t launch_onesweep(const uint64_t* keys_in, const uint32_t* idx_in, uint64_t* keys_out,
+                                   uint32_t* idx_out, uint32_t n, int word, int shift, const uint32_t* starts,
+                                   unsigned long long* status, uint32_t* ticket, uint32_t* err,
+                                   cudaStream_t stream) {
+  const size_t smem = (size_t)NW * kLsdTile * 8 + (IDX ? (size_t)kLsdTile * 4 : 0);
+  cudaError_t e = cudaFuncSetAttribute(k_lsd_onesweep<NW, IDX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  k_lsd_onesweep<NW, IDX><<<lsd_tiles(n), kThreads, smem, stream>>>(keys_in, idx_in, keys_out, idx_out, n, word,
+                                                                     shift, starts, status, ticket, err);
+  return cudaGetLastError();
+}
+
+cudaError_t lsd_onesweep(const uint64_t* keys_in, const uint32_t* idx_in, uint64_t* keys_out, uint32_t* idx_out,
+                         uint32_t n, int nwords, int word, int shift, const uint32_t* starts,
+                         unsigned long long* status, uint32_t* ticket, uint32_t* err, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(status, 0, sizeof(unsigned long long) * 256 * (size_t)lsd_tiles(n), stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ticket, 0, sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return e;
+#define GB_LSD_CASE(NWV)                                                                                       \
+  case NWV:                                                                                                    \
+    e = idx_in ? launch_onesweep<NWV, true>(keys_in, idx_in, keys_out, idx_out, n, word, shift, starts, status,  \
+                                            ticket, err, stream)                                               \
+               : launch_onesweep<NWV, false>(keys_in, idx_in, keys_out, idx_out, n, word, shift, starts,       \
+                                             status, ticket, err, stream);                                     \
     break;
   switch (nwords) {
     GB_LSD_CASE(1)
@@ -249,7 +302,7 @@ cudaError_t lsd_scatter(const uint64_t* keys_in, const uint32_t* idx_in, uint64_
   }
 #undef GB_LSD_CASE
   note_launches(1);
-  return cudaGetLastError();
+  return e;
 }
 
 cudaError_t gather_records(const void* in, void* out, const uint32_t* idx, uint32_t n, uint32_t elsize,

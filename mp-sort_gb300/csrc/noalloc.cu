@@ -137,11 +137,12 @@ extern "C" GBSORT_API int gbsort_sort_device_noalloc(const void* d_in, void* d_o
   SortTask* split0 = cv.take<SortTask>(cap_split);
   SortTask* split1 = cv.take<SortTask>(cap_split);
   SortTask* local = cv.take<SortTask>(cap_local);
-  const int lg = lsd_grid(s_eff > 0 ? s_eff : 1);
   uint64_t* sA = cv.take<uint64_t>(s_eff);
   uint64_t* sB = cv.take<uint64_t>(s_eff);
-  uint32_t* scounts = cv.take<uint32_t>((size_t)256 * lg);
-  uint32_t* sscan = cv.take<uint32_t>(scan_tmp_words((size_t)256 * lg));
+  uint32_t* shist = cv.take<uint32_t>(8 * 256);
+  uint32_t* sstarts = cv.take<uint32_t>(8 * 256);
+  unsigned long long* sstatus = cv.take<unsigned long long>((size_t)lsd_tiles(s_eff > 0 ? s_eff : 1) * 256);
+  uint32_t* sticket = cv.take<uint32_t>(1);
   if (!cv.ok()) {
     fprintf(stderr, "gbsort_sort_device_noalloc: scratch layout exceeds the static array\n");
     return GBSORT_ERR_BAD_ARG;
@@ -168,10 +169,11 @@ extern "C" GBSORT_API int gbsort_sort_device_noalloc(const void* d_in, void* d_o
     NA_CUDA(sample_keys(p.in, n, E, p.key, s_eff, sA, st));
     uint64_t* kin = sA;
     uint64_t* kout = sB;
-    for (int d = 0; d < 8; ++d) {  // LSD sort of the sample, 8 digit passes
-      NA_CUDA(lsd_count(kin, s_eff, 8 * d, scounts, st));
-      NA_CUDA(exclusive_scan_u32(scounts, scounts, (size_t)256 * lg, sscan, st));
-      NA_CUDA(lsd_scatter(kin, nullptr, kout, nullptr, s_eff, 1, 0, 8 * d, scounts, st));
+    NA_CUDA(lsd_digit_histograms(sA, s_eff, 1, shist, st));
+    NA_CUDA(lsd_digit_starts(shist, 1, sstarts, st));
+    for (int d = 0; d < 8; ++d) {  // LSD sort of the sample, 8 one-sweep digit passes
+      NA_CUDA(lsd_onesweep(kin, nullptr, kout, nullptr, s_eff, 1, 0, 8 * d, sstarts + 256 * d, sstatus, sticket,
+                           err, st));
       uint64_t* t = kin;
       kin = kout;
       kout = t;

@@ -188,12 +188,47 @@ __global__ void __launch_bounds__(kThreads) k_join_write(const uint8_t* a, uint3
   if (blockIdx.x == 0 && threadIdx.x == 0) *npairs = offsets[gridDim.x];
 }
 
+// Splitter reads of upper_bound_in(S, lo, hi, key): one per halving step.
+__device__ __forceinline__ uint32_t search_reads(const uint64_t* S, uint32_t lo, uint32_t hi, uint64_t key) {
+  uint32_t r = 0;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi) >> 1;
+    ++r;
+    if (S[mid] <= key) lo = mid + 1;
+    else hi = mid;
+  }
+  return r;
+}
+
 __global__ void k_probe_buckets(const uint64_t* __restrict__ keys, uint32_t nkeys, const uint64_t* __restrict__ S,
                                 ModelDev m, uint32_t* __restrict__ learned, uint32_t* __restrict__ search,
-                                uint32_t* misses) {
+                                uint32_t* misses, unsigned long long* reads) {
+  m = resolve_model(m);
+  const uint32_t nsplit = (uint32_t)(m.nbuckets - 1);
+  unsigned long long rl = 0, rp = 0;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nkeys; i += gridDim.x * blockDim.x) {
-    learned[i] = bucket_learned(S, m, m.knots, m.win, keys[i], misses);
-    search[i] = bucket_plain(S, m.nbuckets, keys[i]);
+    const uint64_t k = keys[i];
+    const uint32_t bl = bucket_learned(S, m, m.knots, m.win, k, misses);
+    const uint32_t bs = bucket_plain(S, m.nbuckets, k);
+    learned[i] = bl;
+    search[i] = bs;
+    if (reads) {
+      // splitters the learned lookup reads: none for a zero window, else the
+      // two window bounds and the search inside the window
+      uint32_t leaf, g;
+      model_predict(k, m.kmin, m.lshift, m.lbits, m.nbuckets, m.knots, leaf, g);
+      const uint32_t w = m.win[leaf];
+      if (w != 0) {
+        uint32_t lo = g > (w >> 16) ? g - (w >> 16) : 0u;
+        uint32_t hi = min(g + (w & 0xffffu), nsplit);
+        rl += (lo > 0) + (hi < nsplit) + search_reads(S, lo, hi, k);
+      }
+      rp += search_reads(S, 0, nsplit, k);
+    }
+  }
+  if (reads) {
+    atomicAdd(reads, rl);
+    atomicAdd(reads + 1, rp);
   }
 }
 
@@ -230,12 +265,13 @@ cudaError_t join_write(const uint8_t* a, uint32_t na, const uint8_t* b, uint32_t
 }
 
 cudaError_t probe_buckets(const uint64_t* keys, uint32_t nkeys, const uint64_t* S, const void* model,
-                          uint32_t* learned, uint32_t* search, uint32_t* misses, cudaStream_t st) {
+                          uint32_t* learned, uint32_t* search, uint32_t* misses, unsigned long long* reads,
+                          cudaStream_t st) {
   const ModelDev m = *(const ModelDev*)model;
   unsigned g = (nkeys + 255) / 256;
   if (g > 4096) g = 4096;
   if (g == 0) return cudaSuccess;
-  k_probe_buckets<<<g, 256, 0, st>>>(keys, nkeys, S, m, learned, search, misses);
+  k_probe_buckets<<<g, 256, 0, st>>>(keys, nkeys, S, m, learned, search, misses, reads);
   note_launches(1);
   return cudaGetLastError();
 }

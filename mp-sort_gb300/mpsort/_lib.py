@@ -73,7 +73,12 @@ SIGNATURES = {
     "gbsort_merge_join_device": (_I, [_P, _SZ, _P, _SZ, _SZ, _P, _P, _P, _P, _P]),
     "gbsort_cdf_forward_backward": (_I, [_P, _U32, _U64, _U64, _I, _P, _P, _P, _P]),
     "gbsort_debug_buckets": (_I, [_P, _U32, _I, _P, _U32, _P, _P, _P, _P]),
+    "gbsort_debug_model": (_I, [_P, _U32, _I, _I, _P, _U32, _P, _P, _P, _P, _P]),
     "gbsort_debug_bisect": (_I, [_P, _U32, _I, _P, _P, _P, _P]),
+    "gbsort_plan_create": (_I, [_P, _SZ, _SZ, _P, _I]),
+    "gbsort_plan_sort": (_I, [_P, _P, _P, _P]),
+    "gbsort_plan_wait": (_I, [_P]),
+    "gbsort_plan_destroy": (_I, [_P]),
     "gbsort_last_stats": (_I, [_P]),
     "gbsort_status_string": (ctypes.c_char_p, [_I]),
     "gbsort_last_error": (ctypes.c_char_p, []),

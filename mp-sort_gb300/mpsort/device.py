@@ -24,6 +24,37 @@ def sort(d_in, d_out, n, dtype, orderby, method="auto", stream=0):
                                              _lib.METHODS[method], stream or None))
 
 
+class Plan:
+    """The sort of n records of `dtype` by `orderby` captured as one CUDA
+    graph: ``plan.sort(d_in, d_out, stream)`` enqueues it (one graph launch,
+    no host synchronisation), ``plan.wait()`` waits and raises on a device
+    error.  The graph is re-captured when the buffers change."""
+
+    def __init__(self, n, dtype, orderby, method="auto"):
+        dtype = numpy.dtype(dtype)
+        self._desc = _desc(dtype, orderby)
+        self._h = ctypes.c_void_p()
+        _lib.check(_lib.lib().gbsort_plan_create(ctypes.byref(self._h), n, dtype.itemsize,
+                                                 ctypes.byref(self._desc), _lib.METHODS[method]))
+
+    def sort(self, d_in, d_out, stream=0):
+        _lib.check(_lib.lib().gbsort_plan_sort(self._h, d_in, d_out, stream or None))
+
+    def wait(self):
+        _lib.check(_lib.lib().gbsort_plan_wait(self._h))
+
+    def close(self):
+        if self._h:
+            _lib.lib().gbsort_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def sort_segments(d_in, d_out, offsets, dtype, orderby, method="auto", stream=0):
     """Sort every segment [offsets[i], offsets[i+1]) of d_in independently."""
     dtype = numpy.dtype(dtype)
@@ -79,6 +110,23 @@ def debug_buckets(sample, nbuckets, keys):
                                                len(keys), bs.ctypes.data, bl.ctypes.data, S.ctypes.data,
                                                ctypes.byref(w)))
     return bs, bl, S, w.value
+
+
+def debug_model(sample, nbuckets, keys, epochs):
+    """Model trained for `epochs` steps: (full-search buckets, learned
+    buckets, final loss, splitters read by the learned lookups, splitters read
+    by the full searches, widest window)."""
+    sample = numpy.ascontiguousarray(sample, dtype=numpy.uint64)
+    keys = numpy.ascontiguousarray(keys, dtype=numpy.uint64)
+    bs = numpy.zeros(len(keys), numpy.uint32)
+    bl = numpy.zeros(len(keys), numpy.uint32)
+    loss = ctypes.c_float(0)
+    reads = numpy.zeros(2, numpy.uint64)
+    w = ctypes.c_uint32(0)
+    _lib.check(_lib.lib().gbsort_debug_model(sample.ctypes.data, len(sample), nbuckets, epochs, keys.ctypes.data,
+                                             len(keys), bs.ctypes.data, bl.ctypes.data, ctypes.byref(loss),
+                                             reads.ctypes.data, ctypes.byref(w)))
+    return bs, bl, loss.value, int(reads[0]), int(reads[1]), w.value
 
 
 def debug_bisect(sorted_keys, nsplit):

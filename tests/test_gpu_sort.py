@@ -356,6 +356,39 @@ def test_learned_lookup_equals_search(mp, dist):
         assert (numpy.diff(S.astype(object)) >= 0).all()
 
 
+@pytest.mark.parametrize("dist", ["lognormal", "mixture", "uniform"])
+def test_trained_model_gain(mp, dist):
+    """What the trained model gains over the full splitter search: the same
+    bucket for every key while reading a fraction of the splitters (none at
+    all where the splitters come from the model itself), and gradient steps
+    that lower the fit's loss below the initial empirical-CDF knots."""
+    from mpsort import device
+    rng = numpy.random.default_rng(21)
+    n = 1_000_000
+    if dist == "lognormal":
+        keys = (rng.lognormal(0.0, 2.0, n) * 1e9).astype(numpy.uint64)
+    elif dist == "mixture":
+        c = rng.uniform(0, 2**50, 300)
+        sd = numpy.exp(rng.uniform(numpy.log(2**30), numpy.log(2**40), 300))
+        i = rng.integers(0, 300, n)
+        keys = numpy.abs(rng.normal(c[i], sd[i])).astype(numpy.uint64)
+    else:
+        keys = rng.integers(0, 2**64, n, dtype=numpy.uint64, endpoint=False)
+    sample = keys[rng.integers(0, n, 262_144)]
+    probe = keys[:200_000]
+    res = {}
+    for epochs in (0, 8):
+        bs, bl, loss, rl, rp, widest = device.debug_model(sample, 2048, probe, epochs)
+        assert (bs == bl).all(), (dist, epochs)
+        res[epochs] = (loss, rl / len(probe), rp / len(probe), widest)
+    (l0, r0, p0, w0), (l8, r8, p8, w8) = res[0], res[8]
+    print(dist, "loss %.3g -> %.3g, splitter reads per key: full search %.2f, learned %.2f (untrained %.2f)"
+          % (l0, l8, p8, r8, r0))
+    assert p8 >= 10.0                      # 2047 splitters: ~11 reads per full search
+    assert r8 <= 0.4 * p8                  # the model reads a fraction of them
+    assert l8 < l0                         # the gradient steps improve on the initial fit
+
+
 # --------------------------------------------- batched and join paths --
 @pytest.mark.parametrize("big", [False, True])
 def test_segments(mp, big):
@@ -439,3 +472,50 @@ def test_learned_heavy_keys_balanced(mp, nvals):
     # a bucket is either one key, or at most ~2.5x the mean plus one heavy key
     limit = 3 * n // st["nbuckets"] + 64
     assert st["max_bucket"] <= max(limit, int(counts.max()))
+
+
+# ------------------------------------------------------------ graph plans --
+@pytest.mark.parametrize("method", ["auto"] + METHODS)
+def test_plan_graph_replay(mp, method):
+    """A plan replays the captured pipeline on new contents of the same
+    buffers, re-captures for new buffers, and matches the stable sort."""
+    import torch
+    from mpsort import device
+    rng = numpy.random.default_rng(31)
+    dt = numpy.dtype([('key', 'u8'), ('val', 'i8')])
+    n = 300_001
+    plan = device.Plan(n, dt, 'key', method)
+    din = torch.empty(n * dt.itemsize, dtype=torch.uint8, device='cuda')
+    dout = torch.empty_like(din)
+    for rep, dist in enumerate(("uniform", "dups", "zipf", "sorted")):
+        a = make(dt, 'key', n, dist, rng)
+        din.copy_(torch.from_numpy(a.view(numpy.uint8)))
+        plan.sort(din.data_ptr(), dout.data_ptr())
+        plan.wait()
+        got = dout.cpu().numpy().view(dt)
+        assert got.tobytes() == O.numpy_sorted(a, 'key').tobytes(), (method, dist)
+        st = mp.last_stats()
+        assert st["launches"] > 0
+    # new output buffer: re-captured
+    dout2 = torch.empty_like(din)
+    plan.sort(din.data_ptr(), dout2.data_ptr())
+    plan.wait()
+    assert torch.equal(dout2, dout)
+    plan.close()
+
+
+def test_plan_on_torch_stream(mp):
+    import torch
+    from mpsort import device
+    rng = numpy.random.default_rng(32)
+    dt = numpy.dtype([('key', 'i4'), ('payload', 'u4')])
+    n = 70_000
+    a = make(dt, 'key', n, "uniform", rng)
+    din = torch.from_numpy(a.view(numpy.uint8).copy()).cuda()
+    dout = torch.empty_like(din)
+    s = torch.cuda.Stream()
+    plan = device.Plan(n, dt, 'key', "learned")
+    for _ in range(3):
+        plan.sort(din.data_ptr(), dout.data_ptr(), s.cuda_stream)
+    plan.wait()
+    assert dout.cpu().numpy().view(dt).tobytes() == O.numpy_sorted(a, 'key').tobytes()
