@@ -331,7 +331,7 @@ struct HsortRun {
 };
 
 // Level-1 bucket count: about 2048 records per bucket, at most 2048 (or
-// GBSORT_MAX_BUCKETS, a power of two up to 8192, when set).  Fewer, larger
+// GBSORT_MAX_BUCKETS, a power of two up to 4096, when set).  Fewer, larger
 // buckets keep the scatter's runs long enough to fill whole DRAM sectors;
 // the bucket splits then carry more of the work.
 int choose_buckets(uint32_t n) {
@@ -340,7 +340,7 @@ int choose_buckets(uint32_t n) {
   if (cap < 0) {
     const char* e = getenv("GBSORT_MAX_BUCKETS");
     int v = e ? atoi(e) : 0;
-    cap = (v >= 2 && v <= 8192 && (v & (v - 1)) == 0) ? v : 2048;
+    cap = (v >= 2 && v <= 4096 && (v & (v - 1)) == 0) ? v : 2048;
   }
   uint64_t want = ((uint64_t)n + 2047) / 2048;
   uint32_t nb = pow2_ceil(want);

@@ -26,17 +26,24 @@ int num_sms();
 
 namespace {
 
-constexpr int kLocalMax = 4096;        // records a local sort holds in shared memory
-#ifndef GB_LOCAL_THREADS
-#define GB_LOCAL_THREADS 512
+// Local-sort shape (overridable at build time for tuning sweeps).
+#ifndef GB_LOCAL_MAX
+#define GB_LOCAL_MAX 2048
 #endif
+#ifndef GB_LOCAL_THREADS
+#define GB_LOCAL_THREADS 256
+#endif
+#ifndef GB_LOCAL_CTAS
+#define GB_LOCAL_CTAS 4
+#endif
+constexpr int kLocalMax = GB_LOCAL_MAX;          // records a local sort holds in shared memory
 constexpr int kLocalThreads = GB_LOCAL_THREADS;  // threads of a local-sort CTA
-constexpr int kLocalCtasPerSm = 2;
+constexpr int kLocalCtasPerSm = GB_LOCAL_CTAS;
 constexpr int kLocalBits = 9;          // digit of the local MSD pass
 constexpr int kInsertMax = 24;         // bins up to this size use insertion sort
 constexpr int kSplitBits = 12;         // bins of a bucket split
 constexpr int kSplitBins = 1 << kSplitBits;
-constexpr int kMaxGroups = 256;        // sub-buckets per split
+constexpr int kMaxGroups = 512;        // sub-buckets per split
 constexpr uint32_t kCopyPiece = 1u << 16;
 
 __host__ __device__ __forceinline__ uint32_t chunk_begin(uint32_t n, uint32_t c, uint32_t g) {
@@ -299,6 +306,68 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_count(HsortParams p, const u
   for (int b = threadIdx.x; b < nbuckets; b += kThreads) counts[(size_t)b * g + c] = hist[b];
 }
 
+// --------------------------------------------------- warp-row ranking ---
+// Stable ranking of a tile by a bucket id without a block-wide sort.  Items
+// are in warp-chunk order (item r of lane l in warp w is element
+// w * 32 * RPT + r * 32 + l); cnt is a shared [buckets][kWarps] uint16 table,
+// all zero on entry.
+//   warp_ranks (then a barrier):  each warp ranks its items with warp
+//       matches and adds its per-bucket counts to its column of cnt;
+//   tile_rank (then a barrier):   an item's rank in its bucket's run of the
+//       tile is the counts of the warps before its own plus its rank in its
+//       warp; `all` is the run's length;
+//   clear_rows (then a barrier):  the warps zero the entries they touched.
+// kNoBucket marks padding items.
+constexpr uint32_t kNoBucket = 0xffffffffu;
+
+template <int RPT>
+__device__ __forceinline__ void warp_ranks(const uint32_t (&bkt)[RPT], uint32_t (&rank)[RPT], uint32_t (&lead)[RPT],
+                                           uint16_t* cnt) {
+  const uint32_t w = warp_id(), lane = lane_id();
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) {
+    const uint32_t peers = __match_any_sync(GB_FULL_MASK, bkt[r]);
+    const uint32_t leader = __ffs(peers) - 1;
+    uint32_t old = 0;
+    if (lane == leader && bkt[r] != kNoBucket) {
+      uint16_t* slot = cnt + (size_t)bkt[r] * kWarps + w;
+      old = *slot;
+      *slot = (uint16_t)(old + __popc(peers));
+    }
+    old = __shfl_sync(GB_FULL_MASK, old, leader);
+    rank[r] = old + __popc(peers & lanemask_lt());
+    lead[r] = lane == leader;
+    __syncwarp();
+  }
+}
+
+__device__ __forceinline__ uint32_t tile_rank(uint32_t b, uint32_t rank, const uint16_t* cnt, uint32_t& all) {
+  const uint32_t w = warp_id();
+  const uint4* row = reinterpret_cast<const uint4*>(cnt + (size_t)b * kWarps);
+  uint32_t before = 0;
+  all = 0;
+#pragma unroll
+  for (int v = 0; v < kWarps / 8; ++v) {
+    const uint4 x = row[v];
+    const uint32_t pr[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      const uint32_t j = (uint32_t)(v * 8 + h * 2);
+      const uint32_t lo = pr[h] & 0xffffu, hi = pr[h] >> 16;
+      before += (j < w ? lo : 0u) + (j + 1 < w ? hi : 0u);
+      all += lo + hi;
+    }
+  }
+  return before + rank;
+}
+
+template <int RPT>
+__device__ __forceinline__ void clear_rows(const uint32_t (&bkt)[RPT], const uint32_t (&lead)[RPT], uint16_t* cnt) {
+#pragma unroll
+  for (int r = 0; r < RPT; ++r)
+    if (lead[r] && bkt[r] != kNoBucket) cnt[(size_t)bkt[r] * kWarps + warp_id()] = 0;
+}
+
 // --------------------------------------------------- level-1 scatter ------
 template <int EW>
 struct Tile {
@@ -306,11 +375,18 @@ struct Tile {
   static constexpr int kSize = kThreads * kRpt;
 };
 
-// Stable scatter of each chunk into its buckets.  Per tile: records in
-// registers, bucket ids ranked stably in two 7-bit passes (low bits, then
-// high bits), then each record goes to cursor[bucket] + its rank in the
-// bucket's run of the tile; cursors start at the scanned (bucket, chunk)
-// offsets, so chunk order and tile order are both preserved.
+// Stable scatter of each chunk into its buckets.  Per tile of T records
+// (RPT per thread, in warp-chunk order), without a block-wide sort:
+//   1. each warp ranks its own records by bucket with warp matches, keeping
+//      per-(bucket, warp) counts in a shared table cnt[bucket][warp];
+//   2. after one barrier, every record reads its bucket's row of the table:
+//      the counts of the warps before its own plus its rank in its warp are
+//      its rank in the tile's run of that bucket, so it goes straight to
+//      cursor[bucket] + that rank;
+//   3. after a second barrier, the last record of each bucket's run advances
+//      the cursor and each warp clears the rows it touched.
+// Cursors start at the scanned (bucket, chunk) offsets, so chunk order and
+// tile order are both preserved.
 template <int EW, int LK>
 __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const uint64_t* __restrict__ S,
                                                              int nbuckets, ModelDev model,
@@ -319,26 +395,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
   model = resolve_model(model);
   uint32_t* err = stats + STAT_SLOTS;  // the error word follows the statistics
   constexpr int RPT = Tile<EW>::kRpt, T = Tile<EW>::kSize;
-  using Rank = BlockRank<RPT, 7>;
-  using Rank8 = BlockRank<RPT, 8>;
   extern __shared__ __align__(16) uint8_t smem[];
   LookupSmem L;
   uint8_t* q = load_lookup<LK>(smem, S, nbuckets, model, L);
   uint32_t* cursor = reinterpret_cast<uint32_t*>(q);
   q += 4 * (size_t)((nbuckets + 3) & ~3);
-  uint16_t* hist = reinterpret_cast<uint16_t*>(q);
-  q += 2 * Rank8::kCounters;
-  uint16_t* bsorted = reinterpret_cast<uint16_t*>(q);
-  q += 2 * T;
-  uint16_t* fpos = reinterpret_cast<uint16_t*>(q);
-  q += 2 * T;
-  uint16_t* bfinal = reinterpret_cast<uint16_t*>(q);
-  q += 2 * T;
-  __shared__ uint32_t scan_tmp[kWarps];
+  uint16_t* cnt = reinterpret_cast<uint16_t*>(q);  // [nbuckets][kWarps]
+  for (int i = threadIdx.x; i < nbuckets * kWarps / 8; i += kThreads)
+    reinterpret_cast<uint4*>(cnt)[i] = make_uint4(0, 0, 0, 0);
 
   const uint32_t w = warp_id(), lane = lane_id();
   const uint32_t E = EW * 4;
-  const bool two_pass = nbuckets > 256;
   // the count kernel's chunks, several per CTA
   for (uint32_t c = blockIdx.x; c < (uint32_t)nchunks; c += gridDim.x) {
   const uint32_t g = (uint32_t)nchunks;
@@ -357,7 +424,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
   for (uint32_t t0 = cb; t0 < ce; t0 += T) {
     const uint32_t nvalid = min((uint32_t)T, ce - t0);
     uint32_t rec[RPT][EW];
-    uint32_t bkt[RPT], dig[RPT], pos[RPT];
+    uint32_t bkt[RPT], rank[RPT];
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
 #pragma unroll
@@ -368,65 +435,35 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
       uint32_t e = w * 32 * RPT + r * 32 + lane;
+      bkt[r] = kNoBucket;
       if (e < nvalid) {
         uint64_t k = key_from_regs<EW>(rec[r], p.key);
         bkt[r] = lookup<LK>(L, model, nbuckets, k, stats + STAT_WINDOW_MISS);
-      } else {
-        bkt[r] = 0x3fffu;  // sorts after every real bucket in both passes
       }
-      dig[r] = bkt[r] & 127u;
     }
-    if (!two_pass) {
-#pragma unroll
-      for (int r = 0; r < RPT; ++r) dig[r] = bkt[r] > 255u ? 255u : bkt[r];
-      Rank8::rank(dig, pos, hist, scan_tmp, nullptr);
-#pragma unroll
-      for (int r = 0; r < RPT; ++r) bfinal[pos[r]] = (uint16_t)bkt[r];
-      __syncthreads();
-    } else {
-      Rank::rank(dig, pos, hist, scan_tmp, nullptr);
-#pragma unroll
-      for (int r = 0; r < RPT; ++r) bsorted[pos[r]] = (uint16_t)bkt[r];
-      __syncthreads();
-      uint32_t kb[RPT], pos2[RPT];
-#pragma unroll
-      for (int r = 0; r < RPT; ++r) {
-        uint32_t k = w * 32 * RPT + r * 32 + lane;
-        kb[r] = bsorted[k];
-        dig[r] = kb[r] >> 7;
-      }
-      Rank::rank(dig, pos2, hist, scan_tmp, nullptr);
-#pragma unroll
-      for (int r = 0; r < RPT; ++r) {
-        uint32_t k = w * 32 * RPT + r * 32 + lane;
-        fpos[k] = (uint16_t)pos2[r];
-        bfinal[pos2[r]] = (uint16_t)kb[r];
-      }
-      __syncthreads();
-#pragma unroll
-      for (int r = 0; r < RPT; ++r) pos[r] = fpos[pos[r]];
-    }
-    // run heads turn cursor[b] into cursor[b] - head_position
-    for (uint32_t i = threadIdx.x; i < nvalid; i += kThreads) {
-      uint32_t b = bfinal[i];
-      if (i == 0 || bfinal[i - 1] != b) cursor[b] -= i;
-    }
+    // 1. ranks within the warp, in (r, lane) order
+    uint32_t lead[RPT];
+    warp_ranks<RPT>(bkt, rank, lead, cnt);
     __syncthreads();
+    // 2. rank in the tile = counts of the earlier warps + rank in the warp
+    uint32_t tot[RPT];
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
-      uint32_t e = w * 32 * RPT + r * 32 + lane;
-      if (e < nvalid) {
-        uint32_t dest = cursor[bkt[r]] + pos[r];
-        if (dest < p.n) RecIO<EW>::store(p.bufA + (size_t)dest * E, rec[r]);
-        else set_error(err, DEV_ERR_COUNT_MISMATCH);
-      }
+      tot[r] = 0;
+      if (bkt[r] == kNoBucket) continue;
+      uint32_t all;
+      const uint32_t at = tile_rank(bkt[r], rank[r], cnt, all);
+      const uint32_t dest = cursor[bkt[r]] + at;
+      if (dest < p.n) RecIO<EW>::store(p.bufA + (size_t)dest * E, rec[r]);
+      else set_error(err, DEV_ERR_COUNT_MISMATCH);
+      tot[r] = at + 1 == all ? all : 0;  // the run's last record advances the cursor
     }
     __syncthreads();
-    // run tails advance the cursors past the tile's records
-    for (uint32_t i = threadIdx.x; i < nvalid; i += kThreads) {
-      uint32_t b = bfinal[i];
-      if (i + 1 == nvalid || bfinal[i + 1] != b) cursor[b] += i + 1;
-    }
+    // 3. advance the cursors, clear the rows
+#pragma unroll
+    for (int r = 0; r < RPT; ++r)
+      if (tot[r]) cursor[bkt[r]] += tot[r];
+    clear_rows<RPT>(bkt, lead, cnt);
     __syncthreads();
   }
   }
@@ -434,9 +471,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
 
 template <int EW, int LK>
 size_t l1_scatter_smem(int nbuckets, const ModelDev* m) {
-  using Rank8 = BlockRank<Tile<EW>::kRpt, 8>;
-  return lookup_smem_bytes<LK>(nbuckets, m) + 4 * (size_t)((nbuckets + 3) & ~3) +
-         2 * Rank8::kCounters + 3 * 2 * (size_t)Tile<EW>::kSize;
+  return lookup_smem_bytes<LK>(nbuckets, m) + 4 * (size_t)((nbuckets + 3) & ~3) + 2 * (size_t)nbuckets * kWarps;
 }
 
 // ------------------------------------------------------------- tasks -----
@@ -534,10 +569,9 @@ struct LocalSmemT {
 };
 struct SplitSmem {
   uint32_t hist[kSplitBins];
-  uint8_t gmap[kSplitBins];
+  uint16_t gmap[kSplitBins];
   uint32_t cursor[kMaxGroups];
-  uint32_t dstart[kMaxGroups + 1];
-  uint16_t rhist[kWarps * kMaxGroups];
+  __align__(16) uint16_t gcnt[kMaxGroups * kWarps];  // warp-row ranking table, zero between tiles
   uint64_t red[2 * kWarps];
   uint32_t gstart[kMaxGroups + 1];
   uint32_t gfirst[kMaxGroups + 1];
@@ -710,7 +744,6 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
                            uint32_t* stats, uint32_t* err) {
   constexpr uint32_t E = EW * 4;
   constexpr int RPT = Tile<EW>::kRpt, T = Tile<EW>::kSize;
-  using Rank = BlockRank<RPT, 8>;
   const uint8_t* src = (task.src ? p.bufB : p.bufA) + (size_t)task.start * E;
   uint8_t* oth = (task.src ? p.bufA : p.bufB) + (size_t)task.start * E;
   const uint32_t m = task.count;
@@ -789,7 +822,7 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
       unsigned long long mid2 = (unsigned long long)sm.hist[b] + incl;
       gb_ = (uint32_t)min(mid2 / (2ull * target), (unsigned long long)(kMaxGroups - 1));
     }
-    sm.gmap[b] = (uint8_t)gb_;
+    sm.gmap[b] = (uint16_t)gb_;
   }
   __syncthreads();
   for (uint32_t b = threadIdx.x; b < nbins; b += kThreads) {
@@ -809,41 +842,41 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
   __syncthreads();
   for (int g = threadIdx.x; g < kMaxGroups; g += kThreads) sm.cursor[g] = sm.gstart[g];
   __syncthreads();
-  // stable scatter src -> other by group
+  // stable scatter src -> other by group (warp-row ranking)
   for (uint32_t t0 = 0; t0 < m; t0 += T) {
     const uint32_t nvalid = min((uint32_t)T, m - t0);
     uint32_t rec[RPT][EW];
-    uint32_t dig[RPT], pos[RPT];
+    uint32_t grp[RPT], rank[RPT], lead[RPT], tot[RPT];
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
       uint32_t e = w * 32 * RPT + r * 32 + lane;
+      grp[r] = kNoBucket;
       if (e < nvalid) {
         RecIO<EW>::load(src + (size_t)(t0 + e) * E, rec[r]);
         uint64_t key = key_from_regs<EW>(rec[r], p.key);
         uint64_t x = key > blo ? key - blo : 0;
         uint32_t bin = (uint32_t)min(x >> shift, (uint64_t)(nbins - 1));
-        dig[r] = sm.gmap[bin];
-      } else {
-        dig[r] = kMaxGroups - 1;
+        grp[r] = sm.gmap[bin];
       }
     }
-    Rank::rank(dig, pos, sm.rhist, sm.scan_tmp, sm.dstart);
+    warp_ranks<RPT>(grp, rank, lead, sm.gcnt);
+    __syncthreads();
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
-      uint32_t e = w * 32 * RPT + r * 32 + lane;
-      if (e < nvalid) {
-        uint32_t d = dig[r];
-        uint32_t dest = sm.cursor[d] + pos[r] - sm.dstart[d];
-        if (dest < m) RecIO<EW>::store(oth + (size_t)dest * E, rec[r]);
-        else set_error(err, DEV_ERR_COUNT_MISMATCH);
-      }
+      tot[r] = 0;
+      if (grp[r] == kNoBucket) continue;
+      uint32_t all;
+      const uint32_t at = tile_rank(grp[r], rank[r], sm.gcnt, all);
+      const uint32_t dest = sm.cursor[grp[r]] + at;
+      if (dest < m) RecIO<EW>::store(oth + (size_t)dest * E, rec[r]);
+      else set_error(err, DEV_ERR_COUNT_MISMATCH);
+      tot[r] = at + 1 == all ? all : 0;
     }
     __syncthreads();
-    for (int d = threadIdx.x; d < kMaxGroups; d += kThreads) {
-      uint32_t cnt = sm.dstart[d + 1] - sm.dstart[d];
-      if (d == kMaxGroups - 1) cnt -= (uint32_t)T - nvalid;
-      sm.cursor[d] += cnt;
-    }
+#pragma unroll
+    for (int r = 0; r < RPT; ++r)
+      if (tot[r]) sm.cursor[grp[r]] += tot[r];
+    clear_rows<RPT>(grp, lead, sm.gcnt);
     __syncthreads();
   }
   __threadfence_block();
@@ -874,6 +907,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split(HsortParams p, TaskLists 
   extern __shared__ __align__(16) uint8_t smem_raw[];
   SplitSmem& sm = *reinterpret_cast<SplitSmem*>(smem_raw);
   const uint32_t nt = min(*L.nsplit_in, L.cap_split);
+  for (int i = threadIdx.x; i < kMaxGroups * kWarps; i += kThreads) sm.gcnt[i] = 0;
   for (;;) {
     if (threadIdx.x == 0) {
       uint32_t id = atomicAdd(work, 1u);

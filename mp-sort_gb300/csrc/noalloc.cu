@@ -120,7 +120,7 @@ extern "C" GBSORT_API int gbsort_sort_device_noalloc(const void* d_in, void* d_o
   int nb = 1;
   if (n > 4096) {
     uint64_t want = ((uint64_t)n + 2047) / 2048;
-    while ((uint64_t)nb < want && nb < 8192) nb <<= 1;
+    while ((uint64_t)nb < want && nb < 4096) nb <<= 1;
   }
   const int grid = hsort_grid(n);
   const uint32_t s_eff = nb > 1 ? (uint32_t)std::min<uint64_t>(n, std::max<uint64_t>(4096, (uint64_t)nb * 128)) : 0;
