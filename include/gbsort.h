@@ -169,6 +169,35 @@ GBSORT_API int gbsort_release(void);
 /* Version string of this library. */
 GBSORT_API const char *gbsort_version(void);
 
+/* ---- autotuner --------------------------------------------------------------
+ * gbsort_autotune times every candidate configuration -- the LSD path, and
+ * the plain and learned histogram sorts at level-1 bucket caps of 512, 1024,
+ * 2048 and 4096 -- on nmemb records of this layout (the caller's device
+ * records, read only, or pseudo-random ones when d_records is NULL), returns
+ * the fastest and stores it in the tuning table under (elsize, key width,
+ * size class = bit length of nmemb).  Sorts with GBSORT_AUTO use the table
+ * entry of the nearest size class within a factor of 4.  The table can be
+ * set by hand, saved to and loaded from a text file (one entry per line:
+ * elsize key_width size_class method max_buckets sample_per_bucket ms).
+ * No counterpart in the reference. */
+typedef struct gbsort_tuning {
+    int32_t method;              /* GBSORT_HISTOGRAM_PLAIN, _LEARNED or GBSORT_LSD */
+    uint32_t max_buckets;        /* level-1 bucket cap: a power of two, 2..4096 (0: default) */
+    uint32_t sample_per_bucket;  /* sampled keys per level-1 bucket, 16..1024 (0: 128) */
+    float ms;                    /* measured time of this configuration */
+    uint32_t reserved[4];
+} gbsort_tuning;
+GBSORT_API int gbsort_autotune(size_t nmemb, size_t elsize, const gbsort_key_desc *key,
+                    const void *d_records, gbsort_tuning *best);
+GBSORT_API int gbsort_tuning_set(size_t nmemb, size_t elsize, const gbsort_key_desc *key,
+                      const gbsort_tuning *t);
+/* GBSORT_ERR_UNSUPPORTED when the table has no entry for this shape. */
+GBSORT_API int gbsort_tuning_get(size_t nmemb, size_t elsize, const gbsort_key_desc *key,
+                      gbsort_tuning *t);
+GBSORT_API int gbsort_tuning_clear(void);
+GBSORT_API int gbsort_tuning_save(const char *path);
+GBSORT_API int gbsort_tuning_load(const char *path);
+
 /* ---- graph plans ----------------------------------------------------------
  * The whole device pipeline of one sort shape -- sample, splitter search or
  * model training, bucket count, scan, scatter, bucket splits and local

@@ -7,6 +7,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <map>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -330,21 +331,71 @@ struct HsortRun {
   uint32_t sample = 0;
 };
 
-// Level-1 bucket count: about 2048 records per bucket, at most 2048 (or
-// GBSORT_MAX_BUCKETS, a power of two up to 4096, when set).  Fewer, larger
-// buckets keep the scatter's runs long enough to fill whole DRAM sectors;
-// the bucket splits then carry more of the work.
-int choose_buckets(uint32_t n) {
+// Run-time shape of a histogram sort (the autotuner's choices).
+struct Knobs {
+  int max_buckets = 0;        // level-1 bucket cap, a power of two up to 4096 (0: default)
+  int sample_per_bucket = 0;  // sampled keys per level-1 bucket (0: 128)
+};
+
+// Level-1 bucket count: about 2048 records per bucket, at most the cap --
+// the knob, else GBSORT_MAX_BUCKETS (a power of two up to 4096), else 2048.
+// Fewer, larger buckets keep the scatter's runs long enough to fill whole
+// DRAM sectors; the bucket splits then carry more of the work.
+int choose_buckets(uint32_t n, const Knobs& k) {
   if (n <= 4096) return 1;
-  static int cap = -1;
-  if (cap < 0) {
+  static int env_cap = -1;
+  if (env_cap < 0) {
     const char* e = getenv("GBSORT_MAX_BUCKETS");
     int v = e ? atoi(e) : 0;
-    cap = (v >= 2 && v <= 4096 && (v & (v - 1)) == 0) ? v : 2048;
+    env_cap = (v >= 2 && v <= 4096 && (v & (v - 1)) == 0) ? v : 2048;
   }
+  const int cap = k.max_buckets ? k.max_buckets : env_cap;
   uint64_t want = ((uint64_t)n + 2047) / 2048;
   uint32_t nb = pow2_ceil(want);
   return (int)std::min<uint32_t>(nb, (uint32_t)cap);
+}
+
+// ------------------------------------------------------ tuning table ----
+// Winning configurations of gbsort_autotune per (record size, key width,
+// size class = bit length of n); sorts with GBSORT_AUTO look here first.
+std::mutex g_tune_mu;
+std::map<uint64_t, gbsort_tuning> g_tune;
+
+uint64_t tune_key(uint32_t elsize, uint32_t width, uint32_t cls) {
+  return ((uint64_t)elsize << 16) | ((uint64_t)width << 8) | cls;
+}
+uint32_t size_class(uint64_t n) {
+  uint32_t b = 0;
+  while (n) {
+    ++b;
+    n >>= 1;
+  }
+  return b;
+}
+bool tuning_ok(const gbsort_tuning& t) {
+  if (t.method != GBSORT_HISTOGRAM_PLAIN && t.method != GBSORT_HISTOGRAM_LEARNED && t.method != GBSORT_LSD)
+    return false;
+  if (t.max_buckets && (t.max_buckets < 2 || t.max_buckets > 4096 || (t.max_buckets & (t.max_buckets - 1))))
+    return false;
+  return t.sample_per_bucket == 0 || (t.sample_per_bucket >= 16 && t.sample_per_bucket <= 1024);
+}
+// The entry of the nearest size class (within a factor of 4) for this layout.
+bool tune_lookup(uint32_t elsize, uint32_t width, uint64_t n, gbsort_tuning* out) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (g_tune.empty()) return false;
+  const uint32_t cls = size_class(n);
+  for (uint32_t d = 0; d <= 2; ++d)
+    for (int sgn = 0; sgn < 2; ++sgn) {
+      if (d == 0 && sgn) continue;
+      uint32_t c = sgn ? cls + d : cls - d;
+      if (c > 64) continue;
+      auto it = g_tune.find(tune_key(elsize, width, c));
+      if (it != g_tune.end()) {
+        *out = it->second;
+        return true;
+      }
+    }
+  return false;
 }
 
 // Device task lists of level 2 and their counters.
@@ -401,12 +452,13 @@ int run_level2(const HsortParams& p, const Level2& l2, uint32_t* stats, uint32_t
 // anywhere (so it can be captured into a CUDA graph); the device counters
 // end up in c.hc once the stream reaches the end.  hsort_collect reads them.
 int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize, const gbsort_key_desc* key,
-                  bool learned, bool timing, cudaStream_t st) {
+                  bool learned, bool timing, const Knobs& knobs, cudaStream_t st) {
   GB_CUDA(c.A.ensure((size_t)n * elsize));
   GB_CUDA(c.B.ensure((size_t)n * elsize));
-  const int nb = choose_buckets(n);
+  const int nb = choose_buckets(n, knobs);
   const int grid = hsort_grid(n);
-  const uint32_t s = nb > 1 ? (uint32_t)std::min<uint64_t>(n, std::max<uint64_t>(4096, (uint64_t)nb * 128)) : 0;
+  const uint64_t spb = knobs.sample_per_bucket ? (uint64_t)knobs.sample_per_bucket : 128;
+  const uint32_t s = nb > 1 ? (uint32_t)std::min<uint64_t>(n, std::max<uint64_t>(4096, (uint64_t)nb * spb)) : 0;
   const uint32_t cap_split = (uint32_t)nb + n / 4096 + 4096;
   const uint32_t cap_local = 4u * (uint32_t)nb + n / 512 + 65536;
   const int lbits = 11;
@@ -559,8 +611,8 @@ int hsort_collect(Context& c) {
 }
 
 int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize, const gbsort_key_desc* key,
-              int method, cudaStream_t st) {
-  int rc = hsort_enqueue(c, d_in, d_out, n, elsize, key, method == GBSORT_HISTOGRAM_LEARNED, true, st);
+              int method, const Knobs& knobs, cudaStream_t st) {
+  int rc = hsort_enqueue(c, d_in, d_out, n, elsize, key, method == GBSORT_HISTOGRAM_LEARNED, true, knobs, st);
   if (rc) return rc;
   GB_CUDA(cudaStreamSynchronize(st));
   return hsort_collect(c);
@@ -568,6 +620,22 @@ int run_hsort(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t el
 
 int sort_device_dispatch(Context& c, const void* d_in, void* d_out, size_t nmemb, size_t elsize,
                          const gbsort_key_desc* key, int method, cudaStream_t st);
+
+// GBSORT_AUTO: the tuned configuration for this layout and size when there
+// is one (a histogram method only where the layout allows it), else the
+// learned histogram sort where possible and LSD otherwise.
+int resolve_auto(uint32_t elsize, const gbsort_key_desc* key, uint64_t n, bool hs_ok, Knobs* knobs) {
+  gbsort_tuning t;
+  if (key->nwords == 1 && tune_lookup(elsize, key->word[0].width, n, &t)) {
+    if (t.method == GBSORT_LSD) return GBSORT_LSD;
+    if (hs_ok) {
+      knobs->max_buckets = (int)t.max_buckets;
+      knobs->sample_per_bucket = (int)t.sample_per_bucket;
+      return t.method;
+    }
+  }
+  return hs_ok ? GBSORT_HISTOGRAM_LEARNED : GBSORT_LSD;
+}
 
 int sort_device_locked(Context& c, const void* d_in, void* d_out, size_t nmemb, size_t elsize,
                        const gbsort_key_desc* key, int method, cudaStream_t st) {
@@ -593,13 +661,14 @@ int sort_device_dispatch(Context& c, const void* d_in, void* d_out, size_t nmemb
   }
   const uint32_t n = (uint32_t)nmemb, E = (uint32_t)elsize;
   bool hs_ok = hsort_layout_ok(d_in, d_out, E, key);
-  if (method == GBSORT_AUTO) method = hs_ok ? GBSORT_HISTOGRAM_LEARNED : GBSORT_LSD;
+  Knobs knobs;
+  if (method == GBSORT_AUTO) method = resolve_auto(E, key, n, hs_ok, &knobs);
   if (method == GBSORT_HISTOGRAM_PLAIN || method == GBSORT_HISTOGRAM_LEARNED) {
     if (!hs_ok) {
       set_err("histogram sort needs a one-word key at a 4-byte offset and a record size of 8-64 bytes");
       return GBSORT_ERR_UNSUPPORTED;
     }
-    return run_hsort(c, d_in, d_out, n, E, key, method, st);
+    return run_hsort(c, d_in, d_out, n, E, key, method, knobs, st);
   }
   if (method == GBSORT_LSD) return run_lsd(c, d_in, d_out, n, E, key, nullptr, 0, st);
   set_err("unknown method %d", method);
@@ -982,6 +1051,156 @@ int gbsort_release(void) {
 
 const char* gbsort_version(void) { return "gbsort 0.1.0 (sm_103a)"; }
 
+// ----------------------------------------------------------- autotuner --
+int gbsort_autotune(size_t nmemb, size_t elsize, const gbsort_key_desc* key, const void* d_records,
+                    gbsort_tuning* best) {
+  if (!best || nmemb < 2 || nmemb >= 0xffffffffull || elsize == 0 || elsize > (1u << 20) || !key_ok(key, elsize))
+    return GBSORT_ERR_BAD_ARG;
+  Context* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaStream_t st = c->stream;
+  const uint32_t n = (uint32_t)nmemb, E = (uint32_t)elsize;
+  const size_t bytes = (size_t)n * E;
+  // inputs: the caller's records, or pseudo-random ones; the sorts write to
+  // the host-staging buffer so the caller's data is never modified
+  GB_CUDA(c->hout.ensure(bytes));
+  const void* in = d_records;
+  if (!in) {
+    GB_CUDA(c->hin.ensure(bytes));
+    GB_CUDA(fill_hash(c->hin.p, bytes, 0x5eed5eedull, st));
+    in = c->hin.p;
+  }
+  void* out = c->hout.p;
+  const bool hs_ok = hsort_layout_ok(in, out, E, key);
+  struct Cand {
+    int method;
+    int cap;
+  };
+  std::vector<Cand> cands;
+  cands.push_back({GBSORT_LSD, 0});
+  if (hs_ok)
+    for (int m : {GBSORT_HISTOGRAM_LEARNED, GBSORT_HISTOGRAM_PLAIN})
+      for (int cap : {512, 1024, 2048, 4096}) cands.push_back({m, cap});
+  gbsort_tuning win{};
+  win.ms = -1.f;
+  for (const Cand& cd : cands) {
+    Knobs k;
+    k.max_buckets = cd.cap;
+    float ms_best = -1.f;
+    for (int rep = 0; rep < 3; ++rep) {  // a warm-up, then the best of two
+      GB_CUDA(cudaEventRecord(c->ev[7], st));
+      int r = cd.method == GBSORT_LSD ? run_lsd(*c, in, out, n, E, key, nullptr, 0, st)
+                                      : run_hsort(*c, in, out, n, E, key, cd.method, k, st);
+      if (r) {
+        ms_best = -1.f;
+        break;
+      }
+      // run_* returned after synchronising, so the end event is already due
+      GB_CUDA(cudaEventRecord(c->ev[6], st));
+      GB_CUDA(cudaEventSynchronize(c->ev[6]));
+      float ms = 0.f;
+      GB_CUDA(cudaEventElapsedTime(&ms, c->ev[7], c->ev[6]));
+      if (rep > 0 && (ms_best < 0.f || ms < ms_best)) ms_best = ms;
+    }
+    if (ms_best >= 0.f && (win.ms < 0.f || ms_best < win.ms)) {
+      win.method = cd.method;
+      win.max_buckets = (uint32_t)cd.cap;
+      win.sample_per_bucket = 0;
+      win.ms = ms_best;
+    }
+  }
+  if (win.ms < 0.f) {
+    set_err("autotune: no candidate ran");
+    return GBSORT_ERR_INTERNAL;
+  }
+  *best = win;
+  if (key->nwords == 1) {
+    std::lock_guard<std::mutex> tl(g_tune_mu);
+    g_tune[tune_key(E, key->word[0].width, size_class(n))] = win;
+  }
+  return GBSORT_OK;
+}
+
+int gbsort_tuning_set(size_t nmemb, size_t elsize, const gbsort_key_desc* key, const gbsort_tuning* t) {
+  if (!t || !key_ok(key, elsize) || key->nwords != 1 || !tuning_ok(*t)) return GBSORT_ERR_BAD_ARG;
+  std::lock_guard<std::mutex> tl(g_tune_mu);
+  g_tune[tune_key((uint32_t)elsize, key->word[0].width, size_class(nmemb))] = *t;
+  return GBSORT_OK;
+}
+
+int gbsort_tuning_get(size_t nmemb, size_t elsize, const gbsort_key_desc* key, gbsort_tuning* t) {
+  if (!t || !key_ok(key, elsize)) return GBSORT_ERR_BAD_ARG;
+  if (key->nwords != 1 || !tune_lookup((uint32_t)elsize, key->word[0].width, nmemb, t)) return GBSORT_ERR_UNSUPPORTED;
+  return GBSORT_OK;
+}
+
+int gbsort_tuning_clear(void) {
+  std::lock_guard<std::mutex> tl(g_tune_mu);
+  g_tune.clear();
+  return GBSORT_OK;
+}
+
+// One line per entry: elsize width class method max_buckets sample_per_bucket ms
+int gbsort_tuning_save(const char* path) {
+  if (!path) return GBSORT_ERR_BAD_ARG;
+  FILE* f = fopen(path, "w");
+  if (!f) {
+    set_err("cannot write %s", path);
+    return GBSORT_ERR_BAD_ARG;
+  }
+  std::lock_guard<std::mutex> tl(g_tune_mu);
+  fprintf(f, "# gbsort tuning: elsize key_width size_class method max_buckets sample_per_bucket ms\n");
+  for (const auto& kv : g_tune)
+    fprintf(f, "%u %u %u %d %u %u %.4f\n", (unsigned)(kv.first >> 16), (unsigned)((kv.first >> 8) & 0xff),
+            (unsigned)(kv.first & 0xff), kv.second.method, kv.second.max_buckets, kv.second.sample_per_bucket,
+            kv.second.ms);
+  fclose(f);
+  return GBSORT_OK;
+}
+
+int gbsort_tuning_load(const char* path) {
+  if (!path) return GBSORT_ERR_BAD_ARG;
+  FILE* f = fopen(path, "r");
+  if (!f) {
+    set_err("cannot read %s", path);
+    return GBSORT_ERR_BAD_ARG;
+  }
+  char line[256];
+  std::map<uint64_t, gbsort_tuning> loaded;
+  int rc = GBSORT_OK;
+  while (fgets(line, sizeof line, f)) {
+    if (line[0] == '#' || line[0] == '\n') continue;
+    unsigned el, wd, cls, mb, spb;
+    int m;
+    float ms;
+    if (sscanf(line, "%u %u %u %d %u %u %f", &el, &wd, &cls, &m, &mb, &spb, &ms) != 7 || (wd != 4 && wd != 8) ||
+        cls > 64 || el == 0 || el > (1u << 20)) {
+      rc = GBSORT_ERR_BAD_ARG;
+      break;
+    }
+    gbsort_tuning t{};
+    t.method = m;
+    t.max_buckets = mb;
+    t.sample_per_bucket = spb;
+    t.ms = ms;
+    if (!tuning_ok(t)) {
+      rc = GBSORT_ERR_BAD_ARG;
+      break;
+    }
+    loaded[tune_key(el, wd, cls)] = t;
+  }
+  fclose(f);
+  if (rc) {
+    set_err("malformed tuning file %s", path);
+    return rc;
+  }
+  std::lock_guard<std::mutex> tl(g_tune_mu);
+  for (const auto& kv : loaded) g_tune[kv.first] = kv.second;
+  return GBSORT_OK;
+}
+
 // ------------------------------------------------------- graph plans ----
 struct gbsort_plan {
   Context ctx;                       // the plan's own scratch, counters and capture stream
@@ -1033,7 +1252,8 @@ static int plan_capture(gbsort_plan* p, const void* in, void* out) {
   Context& c = p->ctx;
   const uint32_t n = (uint32_t)p->nmemb, E = (uint32_t)p->elsize;
   const bool hs_ok = hsort_layout_ok(in, out, E, &p->key);
-  int m = p->method == GBSORT_AUTO ? (hs_ok ? GBSORT_HISTOGRAM_LEARNED : GBSORT_LSD) : p->method;
+  Knobs knobs;
+  int m = p->method == GBSORT_AUTO ? resolve_auto(E, &p->key, n, hs_ok, &knobs) : p->method;
   if (m != GBSORT_LSD && !hs_ok) {
     set_err("histogram sort needs a one-word key at a 4-byte offset and a record size of 8-64 bytes");
     return GBSORT_ERR_UNSUPPORTED;
@@ -1042,7 +1262,8 @@ static int plan_capture(gbsort_plan* p, const void* in, void* out) {
   GB_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeRelaxed));
   const unsigned long long l0 = launch_count();
   int rc = m == GBSORT_LSD ? lsd_enqueue(c, in, out, n, E, &p->key, nullptr, 0, false, c.stream)
-                           : hsort_enqueue(c, in, out, n, E, &p->key, m == GBSORT_HISTOGRAM_LEARNED, false, c.stream);
+                           : hsort_enqueue(c, in, out, n, E, &p->key, m == GBSORT_HISTOGRAM_LEARNED, false, knobs,
+                                           c.stream);
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(c.stream, &g);
   if (rc || e != cudaSuccess) {

@@ -47,6 +47,9 @@ uint32_t lsd_tiles(uint32_t n);
 cudaError_t lsd_onesweep(const uint64_t* keys_in, const uint32_t* idx_in, uint64_t* keys_out, uint32_t* idx_out,
                          uint32_t n, int nwords, int word, int shift, const uint32_t* starts,
                          unsigned long long* status, uint32_t* ticket, uint32_t* err, cudaStream_t stream);
+// Pseudo-random contents for the first nbytes / 4 words of p (synthetic
+// inputs of the autotuner).
+cudaError_t fill_hash(void* p, size_t nbytes, uint64_t seed, cudaStream_t stream);
 // out[i] = in[idx[i]] for records of elsize bytes.
 cudaError_t gather_records(const void* in, void* out, const uint32_t* idx, uint32_t n,
                            uint32_t elsize, cudaStream_t stream);

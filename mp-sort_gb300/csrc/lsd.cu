@@ -190,6 +190,17 @@ __global__ void __launch_bounds__(kThreads) k_lsd_onesweep(const uint64_t* __res
   }
 }
 
+// Pseudo-random bytes: word i of the buffer is a 64-bit mix of (i, seed).
+__global__ void k_fill_hash(uint32_t* __restrict__ p, uint64_t nwords, uint64_t seed) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nwords;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t z = (i + 1) * 0x9E3779B97F4A7C15ull ^ seed;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    p[i] = (uint32_t)((z ^ (z >> 31)) >> 16);
+  }
+}
+
 // out[i] = in[idx[i]], copied in units of VB bytes (VB divides elsize and
 // both base addresses are VB-aligned).
 template <typename V>
@@ -303,6 +314,14 @@ cudaError_t lsd_onesweep(const uint64_t* keys_in, const uint32_t* idx_in, uint64
 #undef GB_LSD_CASE
   note_launches(1);
   return e;
+}
+
+cudaError_t fill_hash(void* p, size_t nbytes, uint64_t seed, cudaStream_t stream) {
+  const uint64_t nw = nbytes / 4;
+  if (nw == 0) return cudaSuccess;
+  k_fill_hash<<<blocks_for(nw, 256), 256, 0, stream>>>((uint32_t*)p, nw, seed);
+  note_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t gather_records(const void* in, void* out, const uint32_t* idx, uint32_t n, uint32_t elsize,

@@ -63,6 +63,16 @@ _U32 = ctypes.c_uint32
 _U64 = ctypes.c_uint64
 _I = ctypes.c_int
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_int32), ("max_buckets", ctypes.c_uint32),
+                ("sample_per_bucket", ctypes.c_uint32), ("ms", ctypes.c_float),
+                ("reserved", ctypes.c_uint32 * 4)]
+
+    def as_dict(self):
+        return {"method": METHOD_NAMES.get(self.method, self.method), "max_buckets": self.max_buckets,
+                "sample_per_bucket": self.sample_per_bucket, "ms": self.ms}
+
+
 # name: (restype, argtypes)
 SIGNATURES = {
     "gbsort_sort_device": (_I, [_P, _P, _SZ, _SZ, _P, _I, _P]),
@@ -79,6 +89,12 @@ SIGNATURES = {
     "gbsort_plan_sort": (_I, [_P, _P, _P, _P]),
     "gbsort_plan_wait": (_I, [_P]),
     "gbsort_plan_destroy": (_I, [_P]),
+    "gbsort_autotune": (_I, [_SZ, _SZ, _P, _P, _P]),
+    "gbsort_tuning_set": (_I, [_SZ, _SZ, _P, _P]),
+    "gbsort_tuning_get": (_I, [_SZ, _SZ, _P, _P]),
+    "gbsort_tuning_clear": (_I, []),
+    "gbsort_tuning_save": (_I, [ctypes.c_char_p]),
+    "gbsort_tuning_load": (_I, [ctypes.c_char_p]),
     "gbsort_last_stats": (_I, [_P]),
     "gbsort_status_string": (ctypes.c_char_p, [_I]),
     "gbsort_last_error": (ctypes.c_char_p, []),

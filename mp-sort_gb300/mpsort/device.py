@@ -55,6 +55,49 @@ class Plan:
             pass
 
 
+def autotune(n, dtype, orderby, d_records=0):
+    """Time the candidate configurations on n records of `dtype` (the device
+    records at d_records, read only, or pseudo-random ones) and store the
+    fastest in the tuning table used by method='auto'.  Returns it as a dict."""
+    dtype = numpy.dtype(dtype)
+    desc = _desc(dtype, orderby)
+    t = _lib.Tuning()
+    _lib.check(_lib.lib().gbsort_autotune(n, dtype.itemsize, ctypes.byref(desc), d_records or None,
+                                          ctypes.byref(t)))
+    return t.as_dict()
+
+
+def tuning_set(n, dtype, orderby, method, max_buckets=0, sample_per_bucket=0):
+    dtype = numpy.dtype(dtype)
+    desc = _desc(dtype, orderby)
+    t = _lib.Tuning(_lib.METHODS[method], max_buckets, sample_per_bucket, 0.0)
+    _lib.check(_lib.lib().gbsort_tuning_set(n, dtype.itemsize, ctypes.byref(desc), ctypes.byref(t)))
+
+
+def tuning_get(n, dtype, orderby):
+    """The table entry used for this shape, or None."""
+    dtype = numpy.dtype(dtype)
+    desc = _desc(dtype, orderby)
+    t = _lib.Tuning()
+    rc = _lib.lib().gbsort_tuning_get(n, dtype.itemsize, ctypes.byref(desc), ctypes.byref(t))
+    if rc == 6:  # GBSORT_ERR_UNSUPPORTED: no entry
+        return None
+    _lib.check(rc)
+    return t.as_dict()
+
+
+def tuning_clear():
+    _lib.check(_lib.lib().gbsort_tuning_clear())
+
+
+def tuning_save(path):
+    _lib.check(_lib.lib().gbsort_tuning_save(str(path).encode()))
+
+
+def tuning_load(path):
+    _lib.check(_lib.lib().gbsort_tuning_load(str(path).encode()))
+
+
 def sort_segments(d_in, d_out, offsets, dtype, orderby, method="auto", stream=0):
     """Sort every segment [offsets[i], offsets[i+1]) of d_in independently."""
     dtype = numpy.dtype(dtype)

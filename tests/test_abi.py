@@ -50,6 +50,7 @@ def test_key_descriptor_layout_matches_header(lib):
     import mpsort._lib as L
     assert ctypes.sizeof(L.KeyDesc) == 8 + 16 * 4
     assert ctypes.sizeof(L.Stats) == 4 * 24
+    assert ctypes.sizeof(L.Tuning) == 4 * 8
 
 
 def test_key_desc_follows_binding_rules():
@@ -132,3 +133,34 @@ def test_tuning_flags_are_stored(lib):
     mpsort.sort(a, tuning=['DISABLE_GATHER_SORT', 'REQUIRE_SPARSE_ALLTOALLV'])
     assert lib.mpsort_mpi_has_options((1 << 3) | (1 << 6))
     assert not lib.mpsort_mpi_has_options(1 << 4)
+
+
+def test_tuning_table_roundtrip_without_gpu(lib, tmp_path):
+    """The autotuner's table: set, look up by nearest size class, save,
+    clear, load -- host logic only, no device call."""
+    from mpsort import device
+    dt = numpy.dtype([('key', 'u8'), ('val', 'i8')])
+    device.tuning_clear()
+    assert device.tuning_get(10**6, dt, 'key') is None
+    device.tuning_set(10**6, dt, 'key', 'plain', max_buckets=1024, sample_per_bucket=64)
+    got = device.tuning_get(10**6, dt, 'key')
+    assert got["method"] == "plain" and got["max_buckets"] == 1024 and got["sample_per_bucket"] == 64
+    assert device.tuning_get(3 * 10**6, dt, 'key')["method"] == "plain"   # nearest size class
+    assert device.tuning_get(10**9, dt, 'key') is None                     # too far away
+    dt4 = numpy.dtype([('key', 'i4'), ('payload', 'u4')])
+    assert device.tuning_get(10**6, dt4, 'key') is None                    # other layout
+    device.tuning_set(10**8, dt4, 'key', 'lsd')
+    path = tmp_path / "tune.txt"
+    device.tuning_save(path)
+    device.tuning_clear()
+    assert device.tuning_get(10**6, dt, 'key') is None
+    device.tuning_load(path)
+    assert device.tuning_get(10**6, dt, 'key')["max_buckets"] == 1024
+    assert device.tuning_get(10**8, dt4, 'key')["method"] == "lsd"
+    bad = tmp_path / "bad.txt"
+    bad.write_text("16 8 20 2 3000 128 1.0\n")                             # cap not a power of two
+    with pytest.raises(Exception):
+        device.tuning_load(bad)
+    with pytest.raises(Exception):
+        device.tuning_set(10**6, dt, 'key', 'plain', max_buckets=8192)
+    device.tuning_clear()

@@ -519,3 +519,29 @@ def test_plan_on_torch_stream(mp):
         plan.sort(din.data_ptr(), dout.data_ptr(), s.cuda_stream)
     plan.wait()
     assert dout.cpu().numpy().view(dt).tobytes() == O.numpy_sorted(a, 'key').tobytes()
+
+
+# -------------------------------------------------------------- autotuner --
+@pytest.mark.parametrize("given", [False, True])
+def test_autotune_feeds_auto(mp, given):
+    """The autotuner times its candidates, stores the winner, and sorts with
+    method='auto' then run that configuration (same stable result)."""
+    import torch
+    from mpsort import device
+    rng = numpy.random.default_rng(41)
+    dt = numpy.dtype([('key', 'u8'), ('val', 'i8')])
+    n = 2_000_000
+    a = make(dt, 'key', n, "uniform", rng)
+    din = torch.from_numpy(a.view(numpy.uint8).copy()).cuda()
+    before = din.clone()
+    device.tuning_clear()
+    best = device.autotune(n, dt, 'key', din.data_ptr() if given else 0)
+    assert torch.equal(din, before)                    # the caller's records are read only
+    assert best["method"] in ("plain", "learned", "lsd") and best["ms"] > 0
+    assert device.tuning_get(n, dt, 'key')["method"] == best["method"]
+    check(mp, a, 'key', "auto")
+    st = mp.last_stats()
+    assert st["method"] == best["method"]
+    if best["method"] != "lsd":
+        assert st["nbuckets"] <= best["max_buckets"]
+    device.tuning_clear()
