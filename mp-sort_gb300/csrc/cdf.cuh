@@ -54,11 +54,20 @@ __device__ __forceinline__ ModelDev resolve_model(ModelDev m) {
   return m;
 }
 
-// Fraction of the way through the leaf, in [0, 1).
+// Fraction of the way through the leaf, in [0, 1): the top 23 bits of the
+// offset in the leaf placed in a float's mantissa (1.m - 1 = m / 2^23), so
+// no integer-to-float conversion (those run on the slow 64-bit pipe here).
 __device__ __forceinline__ float leaf_frac(uint64_t x, int lshift) {
   if (lshift == 0) return 0.f;
-  uint64_t m = x & ((1ull << lshift) - 1ull);
-  return __ull2float_rz(m) * __int_as_float((127 - lshift) << 23);  // exact power of two
+  const uint64_t m = x & ((1ull << lshift) - 1ull);
+  const uint32_t top = lshift >= 23 ? (uint32_t)(m >> (lshift - 23)) : (uint32_t)(m << (23 - lshift));
+  return __int_as_float(0x3f800000 | top) - 1.0f;
+}
+
+// floor(v) for v in [0, 2^23): adding 2^23 with round-toward-zero leaves
+// the integer part in the low mantissa bits.
+__device__ __forceinline__ int floor_small(float v) {
+  return __float_as_int(__fadd_rz(v, 8388608.0f)) - 0x4b000000;
 }
 
 // (leaf, predicted bucket) for a key.
@@ -83,8 +92,9 @@ __device__ __forceinline__ void model_predict(uint64_t key, uint64_t kmin, int l
       f = fminf(fmaxf(f, k.x), k.y);
     }
   }
-  int b = (int)(f * (float)nbuckets);
-  g = (uint32_t)min(max(b, 0), nbuckets - 1);
+  const float v = fmaxf(f * (float)nbuckets, 0.f);
+  const int b = floor_small(fminf(v, 8388607.f));
+  g = (uint32_t)min(b, nbuckets - 1);
 }
 
 // t = #{ j in [lo, hi) : S[j] <= key } + lo, valid when S[lo-1] <= key < S[hi].

@@ -38,6 +38,31 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   return m;
 }
 
+// Lanes of the warp whose label has the same low `bits` bits as this lane's:
+// one ballot per bit.  Runs on the integer pipes at a fixed cost, where the
+// native match instruction serialises over the distinct values in the warp
+// (and ranking tiles of thousands of buckets has up to 32 of them).
+template <int BITS>
+__device__ __forceinline__ uint32_t match_bits(uint32_t label) {
+  uint32_t m = GB_FULL_MASK;
+#pragma unroll
+  for (int b = 0; b < BITS; ++b) {
+    const uint32_t bit = (label >> b) & 1u;
+    const uint32_t v = __ballot_sync(GB_FULL_MASK, bit);
+    m &= bit ? v : ~v;
+  }
+  return m;
+}
+__device__ __forceinline__ uint32_t match_bits_rt(uint32_t label, int bits) {
+  uint32_t m = GB_FULL_MASK;
+  for (int b = 0; b < bits; ++b) {
+    const uint32_t bit = (label >> b) & 1u;
+    const uint32_t v = __ballot_sync(GB_FULL_MASK, bit);
+    m &= bit ? v : ~v;
+  }
+  return m;
+}
+
 // Order-preserving 64-bit word of a key field held as raw bits (binding.pyx
 // radix_func_*: u8 as is, u4 zero-extended, i8/i4 sign-extended plus 2^63).
 __device__ __forceinline__ uint64_t map_key(uint64_t raw, uint32_t width, uint32_t is_signed) {
@@ -144,7 +169,7 @@ struct BlockRank {
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
       const uint32_t d = digit[r];
-      const uint32_t peers = __match_any_sync(GB_FULL_MASK, d);
+      const uint32_t peers = match_bits<DIGIT_BITS>(d);
       const uint32_t before = wh[d];
       ranks[r] = before + __popc(peers & lt);
       __syncwarp();

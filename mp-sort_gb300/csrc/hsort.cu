@@ -297,9 +297,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_count(HsortParams p, const u
     for (int u = 0; u < U; ++u) {
       uint32_t i = base + u * kThreads + threadIdx.x;
       bool v = i < ce;
-      uint32_t b = v ? lookup<LK>(L, model, nbuckets, k[u], stats + STAT_WINDOW_MISS) : 0xffffffffu;
-      uint32_t peers = __match_any_sync(GB_FULL_MASK, b);
-      if (v && (peers & lanemask_lt()) == 0) atomicAdd(&hist[b], (uint32_t)__popc(peers));
+      if (v) atomicAdd(&hist[lookup<LK>(L, model, nbuckets, k[u], stats + STAT_WINDOW_MISS)], 1u);
     }
   }
   __syncthreads();
@@ -309,9 +307,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_count(HsortParams p, const u
 // --------------------------------------------------- warp-row ranking ---
 // Stable ranking of a tile by a bucket id without a block-wide sort.  Items
 // are in warp-chunk order (item r of lane l in warp w is element
-// w * 32 * RPT + r * 32 + l); cnt is a shared [buckets][kWarps] uint16 table,
-// all zero on entry.
-//   warp_ranks (then a barrier):  each warp ranks its items with warp
+// w * 32 * RPT + r * 32 + l); cnt is a shared [buckets][kWarps] byte table
+// (a warp holds at most 32 * RPT <= 128 items of one bucket), all zero on
+// entry.
+//   warp_ranks (then a barrier):  each warp ranks its items with ballot
 //       matches and adds its per-bucket counts to its column of cnt;
 //   tile_rank (then a barrier):   an item's rank in its bucket's run of the
 //       tile is the counts of the warps before its own plus its rank in its
@@ -319,20 +318,25 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_count(HsortParams p, const u
 //   clear_rows (then a barrier):  the warps zero the entries they touched.
 // kNoBucket marks padding items.
 constexpr uint32_t kNoBucket = 0xffffffffu;
+static_assert(kWarps == 16, "a table row is one 16-byte vector");
 
+// `nbuckets` bounds the ids; padding items match each other under the label
+// nbuckets, so labels need bitlen(nbuckets) bits.
 template <int RPT>
 __device__ __forceinline__ void warp_ranks(const uint32_t (&bkt)[RPT], uint32_t (&rank)[RPT], uint32_t (&lead)[RPT],
-                                           uint16_t* cnt) {
+                                           uint8_t* cnt, uint32_t nbuckets) {
+  static_assert(RPT <= 7, "per-warp counts must fit a byte");
   const uint32_t w = warp_id(), lane = lane_id();
+  const int bits = 32 - __clz(nbuckets);
 #pragma unroll
   for (int r = 0; r < RPT; ++r) {
-    const uint32_t peers = __match_any_sync(GB_FULL_MASK, bkt[r]);
+    const uint32_t peers = match_bits_rt(bkt[r] == kNoBucket ? nbuckets : bkt[r], bits);
     const uint32_t leader = __ffs(peers) - 1;
     uint32_t old = 0;
     if (lane == leader && bkt[r] != kNoBucket) {
-      uint16_t* slot = cnt + (size_t)bkt[r] * kWarps + w;
+      uint8_t* slot = cnt + (size_t)bkt[r] * kWarps + w;
       old = *slot;
-      *slot = (uint16_t)(old + __popc(peers));
+      *slot = (uint8_t)(old + __popc(peers));
     }
     old = __shfl_sync(GB_FULL_MASK, old, leader);
     rank[r] = old + __popc(peers & lanemask_lt());
@@ -341,28 +345,32 @@ __device__ __forceinline__ void warp_ranks(const uint32_t (&bkt)[RPT], uint32_t 
   }
 }
 
-__device__ __forceinline__ uint32_t tile_rank(uint32_t b, uint32_t rank, const uint16_t* cnt, uint32_t& all) {
+__device__ __forceinline__ uint32_t tile_rank(uint32_t b, uint32_t rank, const uint8_t* cnt, uint32_t& all) {
   const uint32_t w = warp_id();
-  const uint4* row = reinterpret_cast<const uint4*>(cnt + (size_t)b * kWarps);
+  const uint4 x = *reinterpret_cast<const uint4*>(cnt + (size_t)b * kWarps);
+  const uint32_t wd[4] = {x.x, x.y, x.z, x.w};
+  // byte j of the row (warp j's count) counts when j < w
   uint32_t before = 0;
   all = 0;
 #pragma unroll
-  for (int v = 0; v < kWarps / 8; ++v) {
-    const uint4 x = row[v];
-    const uint32_t pr[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-    for (int h = 0; h < 4; ++h) {
-      const uint32_t j = (uint32_t)(v * 8 + h * 2);
-      const uint32_t lo = pr[h] & 0xffffu, hi = pr[h] >> 16;
-      before += (j < w ? lo : 0u) + (j + 1 < w ? hi : 0u);
-      all += lo + hi;
-    }
+  for (int v = 0; v < 4; ++v) {
+    const uint32_t lo = wd[v] & 0x00ff00ffu, hi = (wd[v] >> 8) & 0x00ff00ffu;  // bytes 0,2 and 1,3
+    const uint32_t pair = lo + hi;                                           // (b0+b1) | (b2+b3) << 16
+    all += (pair & 0xffffu) + (pair >> 16);
+    const int j0 = v * 4;
+    uint32_t keep = 0;  // bytes of this word below warp w
+    if (j0 + 4 <= (int)w) keep = 0xffffffffu;
+    else if (j0 < (int)w) keep = 0xffffffffu >> (8 * (4 - ((int)w - j0)));
+    const uint32_t m = wd[v] & keep;
+    const uint32_t mlo = m & 0x00ff00ffu, mhi = (m >> 8) & 0x00ff00ffu;
+    const uint32_t mp = mlo + mhi;
+    before += (mp & 0xffffu) + (mp >> 16);
   }
   return before + rank;
 }
 
 template <int RPT>
-__device__ __forceinline__ void clear_rows(const uint32_t (&bkt)[RPT], const uint32_t (&lead)[RPT], uint16_t* cnt) {
+__device__ __forceinline__ void clear_rows(const uint32_t (&bkt)[RPT], const uint32_t (&lead)[RPT], uint8_t* cnt) {
 #pragma unroll
   for (int r = 0; r < RPT; ++r)
     if (lead[r] && bkt[r] != kNoBucket) cnt[(size_t)bkt[r] * kWarps + warp_id()] = 0;
@@ -374,19 +382,46 @@ struct Tile {
   static constexpr int kRpt = (16 / EW) < 1 ? 1 : ((16 / EW) > 4 ? 4 : (16 / EW));
   static constexpr int kSize = kThreads * kRpt;
 };
+#ifndef GB_SCATTER_RPT
+#define GB_SCATTER_RPT 16
+#endif
+#ifndef GB_SCATTER_PREFETCH
+#define GB_SCATTER_PREFETCH 1
+#endif
+// Tile of the level-1 scatter: up to GB_SCATTER_RPT / EW records per thread.
+template <int EW>
+struct ScatterTile {
+  static constexpr int kRpt = (GB_SCATTER_RPT / EW) < 1 ? 1 : ((GB_SCATTER_RPT / EW) > 7 ? 7 : (GB_SCATTER_RPT / EW));
+  static constexpr int kSize = kThreads * kRpt;
+  static constexpr bool kPrefetch = GB_SCATTER_PREFETCH != 0;
+};
+
+// One 32-byte store (a whole DRAM sector, one memory request; two 16-byte
+// stores to scattered places cost a request each).  p is 32-byte aligned.
+__device__ __forceinline__ void store_sector(uint8_t* p, const uint4& a, const uint4& b) {
+  asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "r"(a.x), "r"(a.y), "r"(a.z),
+               "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w)
+               : "memory");
+}
 
 // Stable scatter of each chunk into its buckets.  Per tile of T records
 // (RPT per thread, in warp-chunk order), without a block-wide sort:
-//   1. each warp ranks its own records by bucket with warp matches, keeping
-//      per-(bucket, warp) counts in a shared table cnt[bucket][warp];
-//   2. after one barrier, every record reads its bucket's row of the table:
-//      the counts of the warps before its own plus its rank in its warp are
-//      its rank in the tile's run of that bucket, so it goes straight to
-//      cursor[bucket] + that rank;
-//   3. after a second barrier, the last record of each bucket's run advances
-//      the cursor and each warp clears the rows it touched.
+//   1. each warp ranks its own records by bucket (warp_ranks);
+//   2. after one barrier, every record's rank in its bucket's run of the
+//      tile gives its destination cursor[bucket] + rank (tile_rank);
+//   3. after a second barrier, the last record of each run advances the
+//      cursor and each warp clears the table entries it touched.
 // Cursors start at the scanned (bucket, chunk) offsets, so chunk order and
 // tile order are both preserved.
+//
+// Write combining (16-byte records): a 32-byte DRAM sector holds two
+// records.  Two neighbours in the same run are written in the same phase
+// and meet in L2; but a run usually has one record, and its sector partner
+// comes a tile later -- a half-written sector that L2 may evict, costing
+// an ECC read-modify-write in DRAM.  So the last record of a run whose
+// destination starts a sector is held in shared memory (one slot per
+// bucket) and written together with its partner, the next tile's first
+// record of that bucket; slots still held at the chunk's end are flushed.
 template <int EW, int LK>
 __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const uint64_t* __restrict__ S,
                                                              int nbuckets, ModelDev model,
@@ -394,14 +429,21 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
                                                              int nchunks, uint32_t* __restrict__ stats) {
   model = resolve_model(model);
   uint32_t* err = stats + STAT_SLOTS;  // the error word follows the statistics
-  constexpr int RPT = Tile<EW>::kRpt, T = Tile<EW>::kSize;
+  constexpr int RPT = ScatterTile<EW>::kRpt, T = ScatterTile<EW>::kSize;
+  constexpr bool kPre = ScatterTile<EW>::kPrefetch;
+  constexpr bool kCombine = EW == 4;
+  constexpr uint32_t kNoSlot = 0xffffffffu;
   extern __shared__ __align__(16) uint8_t smem[];
   LookupSmem L;
   uint8_t* q = load_lookup<LK>(smem, S, nbuckets, model, L);
   uint32_t* cursor = reinterpret_cast<uint32_t*>(q);
   q += 4 * (size_t)((nbuckets + 3) & ~3);
-  uint16_t* cnt = reinterpret_cast<uint16_t*>(q);  // [nbuckets][kWarps]
-  for (int i = threadIdx.x; i < nbuckets * kWarps / 8; i += kThreads)
+  uint32_t* held_at = reinterpret_cast<uint32_t*>(q);  // destination of the held record, or kNoSlot
+  if (kCombine) q += 4 * (size_t)((nbuckets + 3) & ~3);
+  uint4* held = reinterpret_cast<uint4*>(q);  // the held record of each bucket
+  if (kCombine) q += 16 * (size_t)nbuckets;
+  uint8_t* cnt = q;  // [nbuckets][kWarps]
+  for (int i = threadIdx.x; i < nbuckets * kWarps / 16; i += kThreads)
     reinterpret_cast<uint4*>(cnt)[i] = make_uint4(0, 0, 0, 0);
 
   const uint32_t w = warp_id(), lane = lane_id();
@@ -411,15 +453,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
   const uint32_t g = (uint32_t)nchunks;
   const uint32_t cb = chunk_begin(p.n, c, g), ce = chunk_end(p.n, c, g);
   __syncthreads();
-  for (int b = threadIdx.x; b < nbuckets; b += kThreads) cursor[b] = offsets[(size_t)b * g + c];
+  for (int b = threadIdx.x; b < nbuckets; b += kThreads) {
+    cursor[b] = offsets[(size_t)b * g + c];
+    if (kCombine) held_at[b] = kNoSlot;
+  }
   __syncthreads();
 
   // the next tile's records are loaded while the current tile is ranked
-  uint32_t nxt[RPT][EW];
+  uint32_t nxt[kPre ? RPT : 1][EW];
+  if constexpr (kPre) {
 #pragma unroll
-  for (int r = 0; r < RPT; ++r) {
-    uint32_t e = w * 32 * RPT + r * 32 + lane;
-    if (cb + e < ce) RecIO<EW>::load_stream(p.in + (size_t)(cb + e) * E, nxt[r]);
+    for (int r = 0; r < RPT; ++r) {
+      uint32_t e = w * 32 * RPT + r * 32 + lane;
+      if (cb + e < ce) RecIO<EW>::load_stream(p.in + (size_t)(cb + e) * E, nxt[r]);
+    }
   }
   for (uint32_t t0 = cb; t0 < ce; t0 += T) {
     const uint32_t nvalid = min((uint32_t)T, ce - t0);
@@ -427,10 +474,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
     uint32_t bkt[RPT], rank[RPT];
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
+      if constexpr (kPre) {
 #pragma unroll
-      for (int q2 = 0; q2 < EW; ++q2) rec[r][q2] = nxt[r][q2];
-      uint32_t e = t0 + T + w * 32 * RPT + r * 32 + lane;
-      if (e < ce) RecIO<EW>::load_stream(p.in + (size_t)e * E, nxt[r]);
+        for (int q2 = 0; q2 < EW; ++q2) rec[r][q2] = nxt[r][q2];
+        uint32_t e = t0 + T + w * 32 * RPT + r * 32 + lane;
+        if (e < ce) RecIO<EW>::load_stream(p.in + (size_t)e * E, nxt[r]);
+      } else {
+        uint32_t e = t0 + w * 32 * RPT + r * 32 + lane;
+        if (e < ce) RecIO<EW>::load_stream(p.in + (size_t)e * E, rec[r]);
+      }
     }
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
@@ -443,35 +495,65 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
     }
     // 1. ranks within the warp, in (r, lane) order
     uint32_t lead[RPT];
-    warp_ranks<RPT>(bkt, rank, lead, cnt);
+    warp_ranks<RPT>(bkt, rank, lead, cnt, (uint32_t)nbuckets);
     __syncthreads();
     // 2. rank in the tile = counts of the earlier warps + rank in the warp
-    uint32_t tot[RPT];
+    uint32_t tot[RPT], hold[RPT];
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
       tot[r] = 0;
+      hold[r] = kNoSlot;
       if (bkt[r] == kNoBucket) continue;
       uint32_t all;
       const uint32_t at = tile_rank(bkt[r], rank[r], cnt, all);
       const uint32_t dest = cursor[bkt[r]] + at;
-      if (dest < p.n) RecIO<EW>::store(p.bufA + (size_t)dest * E, rec[r]);
-      else set_error(err, DEV_ERR_COUNT_MISMATCH);
       tot[r] = at + 1 == all ? all : 0;  // the run's last record advances the cursor
+      if (dest >= p.n) {
+        set_error(err, DEV_ERR_COUNT_MISMATCH);
+        continue;
+      }
+      uint8_t* to = p.bufA + (size_t)dest * E;
+      if constexpr (kCombine) {
+        if ((dest & 1u) == 0 && at + 1 == all) {  // starts a sector whose partner comes later
+          hold[r] = dest;
+          continue;
+        }
+        if ((dest & 1u) && at == 0 && held_at[bkt[r]] == dest - 1) {  // completes a held sector
+          store_sector(to - 16, held[bkt[r]], make_uint4(rec[r][0], rec[r][1], rec[r][2], rec[r][3]));
+          continue;
+        }
+      }
+      RecIO<EW>::store(to, rec[r]);
     }
     __syncthreads();
-    // 3. advance the cursors, clear the rows
+    // 3. advance the cursors, hold the open sectors, clear the rows
 #pragma unroll
-    for (int r = 0; r < RPT; ++r)
+    for (int r = 0; r < RPT; ++r) {
       if (tot[r]) cursor[bkt[r]] += tot[r];
+      if constexpr (kCombine) {
+        if (hold[r] != kNoSlot) {
+          held[bkt[r]] = make_uint4(rec[r][0], rec[r][1], rec[r][2], rec[r][3]);
+          held_at[bkt[r]] = hold[r];
+        } else if (bkt[r] != kNoBucket && tot[r]) {
+          held_at[bkt[r]] = kNoSlot;  // the run ended on a completed sector
+        }
+      }
+    }
     clear_rows<RPT>(bkt, lead, cnt);
     __syncthreads();
+  }
+  if constexpr (kCombine) {  // the chunk's open sectors
+    for (int b = threadIdx.x; b < nbuckets; b += kThreads)
+      if (held_at[b] != kNoSlot) reinterpret_cast<uint4*>(p.bufA)[held_at[b]] = held[b];
   }
   }
 }
 
 template <int EW, int LK>
 size_t l1_scatter_smem(int nbuckets, const ModelDev* m) {
-  return lookup_smem_bytes<LK>(nbuckets, m) + 4 * (size_t)((nbuckets + 3) & ~3) + 2 * (size_t)nbuckets * kWarps;
+  const size_t words = 4 * (size_t)((nbuckets + 3) & ~3);
+  const size_t combine = EW == 4 ? words + 16 * (size_t)nbuckets : 0;
+  return lookup_smem_bytes<LK>(nbuckets, m) + words + combine + (size_t)nbuckets * kWarps;
 }
 
 // ------------------------------------------------------------- tasks -----
@@ -571,7 +653,7 @@ struct SplitSmem {
   uint32_t hist[kSplitBins];
   uint16_t gmap[kSplitBins];
   uint32_t cursor[kMaxGroups];
-  __align__(16) uint16_t gcnt[kMaxGroups * kWarps];  // warp-row ranking table, zero between tiles
+  __align__(16) uint8_t gcnt[kMaxGroups * kWarps];  // warp-row ranking table, zero between tiles
   uint64_t red[2 * kWarps];
   uint32_t gstart[kMaxGroups + 1];
   uint32_t gfirst[kMaxGroups + 1];
@@ -780,8 +862,7 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
           uint64_t x = key > blo ? key - blo : 0;
           bin = (uint32_t)min(x >> shift, (uint64_t)(nbins - 1));
         }
-        uint32_t peers = __match_any_sync(GB_FULL_MASK, bin);
-        if (v && (peers & lanemask_lt()) == 0) atomicAdd(&sm.hist[bin], (uint32_t)__popc(peers));
+        if (v) atomicAdd(&sm.hist[bin], 1u);
       }
     }
     block_minmax(mn, mx, sm.red);
@@ -859,7 +940,7 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
         grp[r] = sm.gmap[bin];
       }
     }
-    warp_ranks<RPT>(grp, rank, lead, sm.gcnt);
+    warp_ranks<RPT>(grp, rank, lead, sm.gcnt, (uint32_t)kMaxGroups);
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
