@@ -39,7 +39,7 @@ namespace {
 constexpr int kLocalMax = GB_LOCAL_MAX;          // records a local sort holds in shared memory
 constexpr int kLocalThreads = GB_LOCAL_THREADS;  // threads of a local-sort CTA
 constexpr int kLocalCtasPerSm = GB_LOCAL_CTAS;
-constexpr int kLocalBits = 9;          // digit of the local MSD pass
+constexpr int kLocalBits = 11;         // bins of the local counting pass (about one record each)
 constexpr int kInsertMax = 24;         // bins up to this size use insertion sort
 constexpr int kSplitBits = 12;         // bins of a bucket split
 constexpr int kSplitBins = 1 << kSplitBits;
@@ -639,7 +639,7 @@ struct LocalSmemT {
   uint64_t keyB[kLocalMax];  // keys in sorted order
   uint16_t idxA[kLocalMax];
   uint16_t idxB[kLocalMax];
-  uint16_t hist[kNW << kLocalBits];
+  uint32_t cnt[1 << kLocalBits];          // bin counts, then bin cursors
   uint32_t start[(1 << kLocalBits) + 1];
   uint16_t big[kLocalMax / (kInsertMax + 1) + 2];  // start of pending bins
   uint16_t bigsz[kLocalMax / (kInsertMax + 1) + 2];
@@ -649,7 +649,11 @@ struct LocalSmemT {
   uint32_t task_id;
   SortTask next;
 };
+constexpr int kSplitTileBytes = kThreads * 64;  // a scatter tile: kThreads * RPT records of <= 16 / RPT words
 struct SplitSmem {
+  __align__(16) uint8_t stage[kSplitTileBytes];  // the tile in group order
+  uint16_t sgrp[kThreads * 4];                   // group of each staged record
+  uint32_t goff[kMaxGroups];                     // first staged slot of each group
   uint32_t hist[kSplitBins];
   uint16_t gmap[kSplitBins];
   uint32_t cursor[kMaxGroups];
@@ -686,41 +690,67 @@ __device__ __forceinline__ void block_minmax(uint64_t& mn, uint64_t& mx, uint64_
   __syncthreads();
 }
 
-// One MSD counting pass over positions [a, a+s) of keyA / idxA, in place:
-// a stable counting sort by (key - mn) >> shift into keyB / idxB, then every
-// element of a small bin takes its place by counting the bin's members with
-// a smaller (key, input index) and is written back to keyA / idxA.  That
-// step is one element per thread, so a large bin costs its own threads only.
-// Elements of bins above kInsertMax go back unchanged and their bins are
-// queued for another pass.  Keys stay in shared memory (few registers).
+// One counting pass over positions [a, a+s) of keyA / idxA, in place: every
+// element takes a slot in its bin, (key - mn) >> shift, by a shared-memory
+// atomic (the order inside a bin is arbitrary), lands in keyB / idxB at its
+// bin's start plus that slot, and then -- in a small bin -- takes its final
+// place by counting the bin's members with a smaller (key, input index):
+// that comparison, not the pass, makes the result stable.  Bins above
+// kInsertMax go back unchanged and are queued for another pass.  With
+// by_idx the bins are the input indices themselves (a bin of equal keys is
+// put back in input order; indices are distinct and below kLocalMax).
 template <int NT>
-__device__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint32_t s, uint64_t mn, uint64_t mx) {
-  constexpr int kLocalRpt = kLocalMax / NT;
-  using Rank = BlockRank<kLocalRpt, kLocalBits, NT>;
-  const uint32_t w = warp_id(), lane = lane_id();
+__device__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint32_t s, uint64_t mn, uint64_t mx,
+                               bool by_idx) {
+  constexpr int kBins = 1 << kLocalBits;
+  constexpr int PER = kLocalMax / NT;
+  static_assert(kLocalMax <= kBins, "input indices must fit the bins");
   const int bits = bitlen64(mx - mn);
   const int shift = bits > kLocalBits ? bits - kLocalBits : 0;
-  uint32_t dig[kLocalRpt], pos[kLocalRpt];
+  for (int i = threadIdx.x; i < kBins; i += NT) sm.cnt[i] = 0;
+  __syncthreads();
+  uint32_t bin[PER], slot[PER];
 #pragma unroll
-  for (int r = 0; r < kLocalRpt; ++r) {
-    uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
-    dig[r] = e < s ? (uint32_t)((sm.keyA[a + e] - mn) >> shift) : ((1u << kLocalBits) - 1);
-  }
-  Rank::rank(dig, pos, sm.hist, sm.scan_tmp, sm.start);
-#pragma unroll
-  for (int r = 0; r < kLocalRpt; ++r) {
-    uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
+  for (int r = 0; r < PER; ++r) {
+    const uint32_t e = r * NT + threadIdx.x;
     if (e < s) {
-      sm.keyB[a + pos[r]] = sm.keyA[a + e];
-      sm.idxB[a + pos[r]] = sm.idxA[a + e];
+      bin[r] = by_idx ? (uint32_t)sm.idxA[a + e] : (uint32_t)((sm.keyA[a + e] - mn) >> shift);
+      slot[r] = atomicAdd(&sm.cnt[bin[r]], 1u);
+    }
+  }
+  __syncthreads();
+  {  // exclusive scan of the bin counts
+    constexpr int BPT = kBins / NT;
+    uint32_t loc[BPT], sum = 0;
+#pragma unroll
+    for (int i = 0; i < BPT; ++i) {
+      loc[i] = sm.cnt[threadIdx.x * BPT + i];
+      sum += loc[i];
+    }
+    uint32_t pre = block_exclusive_scan<uint32_t, NT>(sum, sm.scan_tmp, nullptr);
+#pragma unroll
+    for (int i = 0; i < BPT; ++i) {
+      sm.start[threadIdx.x * BPT + i] = pre;
+      pre += loc[i];
+    }
+    if (threadIdx.x == NT - 1) sm.start[kBins] = pre;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < PER; ++r) {
+    const uint32_t e = r * NT + threadIdx.x;
+    if (e < s) {
+      const uint32_t pos = sm.start[bin[r]] + slot[r];
+      sm.keyB[a + pos] = sm.keyA[a + e];
+      sm.idxB[a + pos] = sm.idxA[a + e];
     }
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < s; i += NT) {
     const uint64_t kv = sm.keyB[a + i];
     const uint16_t iv = sm.idxB[a + i];
-    const uint32_t d = (uint32_t)((kv - mn) >> shift);
-    const uint32_t b0 = sm.start[d], b1 = min(sm.start[d + 1], s);
+    const uint32_t d = by_idx ? (uint32_t)iv : (uint32_t)((kv - mn) >> shift);
+    const uint32_t b0 = sm.start[d], b1 = sm.start[d + 1];
     const uint32_t sz = b1 - b0;
     uint32_t at = i;
     if (sz <= (uint32_t)kInsertMax) {
@@ -774,7 +804,7 @@ __device__ void local_sort(LocalSmemT<NT>& sm, const uint8_t* src, uint8_t* dst,
     __syncthreads();
     return;
   }
-  local_msd_pass<NT>(sm, 0, m, mn, mx);
+  local_msd_pass<NT>(sm, 0, m, mn, mx, false);
   // further passes over bins too large for insertion sort
   for (;;) {
     uint32_t nb = sm.nbig;
@@ -790,9 +820,9 @@ __device__ void local_sort(LocalSmemT<NT>& sm, const uint8_t* src, uint8_t* dst,
       bmx = kv > bmx ? kv : bmx;
     }
     block_minmax<NT>(bmn, bmx, sm.red);
-    if (bmn == bmx) continue;  // equal keys are already in input order
     if (threadIdx.x == 0) atomicAdd(stats + STAT_BIGBIN, 1u);
-    local_msd_pass<NT>(sm, a, s, bmn, bmx);
+    // equal keys: back into input order (their bin filled in any order)
+    local_msd_pass<NT>(sm, a, s, bmn, bmx, bmn == bmx);
   }
   // gather the records into dst in sorted order, four loads in flight
   {
@@ -923,11 +953,17 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
   __syncthreads();
   for (int g = threadIdx.x; g < kMaxGroups; g += kThreads) sm.cursor[g] = sm.gstart[g];
   __syncthreads();
-  // stable scatter src -> other by group (warp-row ranking)
+  // stable scatter src -> other by group: each tile is ranked by group
+  // (warp-row ranking), placed in shared memory in group order and written
+  // out by consecutive threads, so the runs of a group leave as coalesced
+  // stores rather than one memory request per record
+  static_assert(kMaxGroups == kThreads, "one group per thread in the tile scan");
+  static_assert(T <= kThreads * 4 && T * E <= kSplitTileBytes, "tile staging size");
+  const uint32_t g_me = threadIdx.x;
   for (uint32_t t0 = 0; t0 < m; t0 += T) {
     const uint32_t nvalid = min((uint32_t)T, m - t0);
     uint32_t rec[RPT][EW];
-    uint32_t grp[RPT], rank[RPT], lead[RPT], tot[RPT];
+    uint32_t grp[RPT], rank[RPT], lead[RPT];
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
       uint32_t e = w * 32 * RPT + r * 32 + lane;
@@ -942,21 +978,30 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
     }
     warp_ranks<RPT>(grp, rank, lead, sm.gcnt, (uint32_t)kMaxGroups);
     __syncthreads();
-#pragma unroll
-    for (int r = 0; r < RPT; ++r) {
-      tot[r] = 0;
-      if (grp[r] == kNoBucket) continue;
-      uint32_t all;
-      const uint32_t at = tile_rank(grp[r], rank[r], sm.gcnt, all);
-      const uint32_t dest = sm.cursor[grp[r]] + at;
-      if (dest < m) RecIO<EW>::store(oth + (size_t)dest * E, rec[r]);
-      else set_error(err, DEV_ERR_COUNT_MISMATCH);
-      tot[r] = at + 1 == all ? all : 0;
-    }
+    uint32_t gtot;
+    tile_rank(g_me, 0, sm.gcnt, gtot);  // this thread's group: records in the tile
+    const uint32_t goff = block_exclusive_scan<uint32_t>(gtot, sm.scan_tmp, nullptr);
+    sm.goff[g_me] = goff;
     __syncthreads();
 #pragma unroll
-    for (int r = 0; r < RPT; ++r)
-      if (tot[r]) sm.cursor[grp[r]] += tot[r];
+    for (int r = 0; r < RPT; ++r) {
+      if (grp[r] == kNoBucket) continue;
+      uint32_t all;
+      const uint32_t slot = sm.goff[grp[r]] + tile_rank(grp[r], rank[r], sm.gcnt, all);
+      RecIO<EW>::store(sm.stage + (size_t)slot * E, rec[r]);
+      sm.sgrp[slot] = (uint16_t)grp[r];
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < nvalid; i += kThreads) {
+      const uint32_t g = sm.sgrp[i];
+      const uint32_t dest = sm.cursor[g] + (i - sm.goff[g]);
+      uint32_t v[EW];
+      RecIO<EW>::load(sm.stage + (size_t)i * E, v);
+      if (dest < m) RecIO<EW>::store(oth + (size_t)dest * E, v);
+      else set_error(err, DEV_ERR_COUNT_MISMATCH);
+    }
+    __syncthreads();
+    sm.cursor[g_me] += gtot;
     clear_rows<RPT>(grp, lead, sm.gcnt);
     __syncthreads();
   }
