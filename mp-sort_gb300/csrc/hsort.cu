@@ -349,23 +349,19 @@ __device__ __forceinline__ uint32_t tile_rank(uint32_t b, uint32_t rank, const u
   const uint32_t w = warp_id();
   const uint4 x = *reinterpret_cast<const uint4*>(cnt + (size_t)b * kWarps);
   const uint32_t wd[4] = {x.x, x.y, x.z, x.w};
-  // byte j of the row (warp j's count) counts when j < w
-  uint32_t before = 0;
-  all = 0;
+  // byte j of the row (warp j's count) counts when j < w: byte dot products
+  // with 0x01 selectors sum them
+  uint32_t before = 0, tot = 0;
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
-    const uint32_t lo = wd[v] & 0x00ff00ffu, hi = (wd[v] >> 8) & 0x00ff00ffu;  // bytes 0,2 and 1,3
-    const uint32_t pair = lo + hi;                                           // (b0+b1) | (b2+b3) << 16
-    all += (pair & 0xffffu) + (pair >> 16);
     const int j0 = v * 4;
-    uint32_t keep = 0;  // bytes of this word below warp w
-    if (j0 + 4 <= (int)w) keep = 0xffffffffu;
-    else if (j0 < (int)w) keep = 0xffffffffu >> (8 * (4 - ((int)w - j0)));
-    const uint32_t m = wd[v] & keep;
-    const uint32_t mlo = m & 0x00ff00ffu, mhi = (m >> 8) & 0x00ff00ffu;
-    const uint32_t mp = mlo + mhi;
-    before += (mp & 0xffffu) + (mp >> 16);
+    uint32_t keep = 0;
+    if (j0 + 4 <= (int)w) keep = 0x01010101u;
+    else if (j0 < (int)w) keep = 0x01010101u >> (8 * (4 - ((int)w - j0)));
+    tot = __dp4a(wd[v], 0x01010101u, tot);
+    before = __dp4a(wd[v], keep, before);
   }
+  all = tot;
   return before + rank;
 }
 
