@@ -320,17 +320,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_count(HsortParams p, const u
 constexpr uint32_t kNoBucket = 0xffffffffu;
 static_assert(kWarps == 16, "a table row is one 16-byte vector");
 
-// `nbuckets` bounds the ids; padding items match each other under the label
-// nbuckets, so labels need bitlen(nbuckets) bits.
+// Ids are below `nbuckets`, so labels need bitlen(nbuckets - 1) bits.
+// Padding items sit above every real item of their row (the valid items of
+// a tile are a prefix), so they may share a label with real items: they are
+// masked out of every count.
 template <int RPT>
 __device__ __forceinline__ void warp_ranks(const uint32_t (&bkt)[RPT], uint32_t (&rank)[RPT], uint32_t (&lead)[RPT],
                                            uint8_t* cnt, uint32_t nbuckets) {
   static_assert(RPT <= 7, "per-warp counts must fit a byte");
   const uint32_t w = warp_id(), lane = lane_id();
-  const int bits = 32 - __clz(nbuckets);
+  const int bits = nbuckets > 1 ? 32 - __clz(nbuckets - 1) : 0;
 #pragma unroll
   for (int r = 0; r < RPT; ++r) {
-    const uint32_t peers = match_bits_rt(bkt[r] == kNoBucket ? nbuckets : bkt[r], bits);
+    const uint32_t valid = __ballot_sync(GB_FULL_MASK, bkt[r] != kNoBucket);
+    const uint32_t peers = match_bits_rt(bkt[r] & (nbuckets - 1), bits) & valid;
     const uint32_t leader = __ffs(peers) - 1;
     uint32_t old = 0;
     if (lane == leader && bkt[r] != kNoBucket) {
@@ -602,6 +605,50 @@ __global__ void k_build_tasks(const uint32_t* __restrict__ offsets, int grid,
   if (lo == hi || cnt == 1) push_copy(L, start, cnt, lo, hi, 0u, err);
   else if (cnt <= (uint32_t)kLocalMax) push(L.local, L.nlocal, L.cap_local, SortTask{start, cnt, lo, hi, 0u, TASK_SORT}, err);
   else push(L.split_out, L.nsplit_out, L.cap_split, SortTask{start, cnt, lo, hi, 0u, TASK_SORT}, err);
+}
+
+// Largest split task first: the level-1 buckets differ in size by tens of
+// percent and each is one CTA's work, so handing out the large ones first
+// shortens the round's tail (longest-processing-time order).  One block
+// sorts (~count, index) keys by a bitonic network and permutes the list in
+// place; lists above kOrderMax tasks are left as they are.
+constexpr int kOrderMax = 4096;
+__global__ void __launch_bounds__(1024) k_order_tasks(SortTask* list, const uint32_t* n_ptr) {
+  __shared__ unsigned long long key[kOrderMax];
+  const uint32_t n = *n_ptr;
+  if (n < 2 || n > (uint32_t)kOrderMax) return;
+  uint32_t np = 1;
+  while (np < n) np <<= 1;
+  for (uint32_t i = threadIdx.x; i < np; i += blockDim.x)
+    key[i] = i < n ? ((unsigned long long)(~list[i].count) << 32) | i : ~0ull;
+  __syncthreads();
+  for (uint32_t k = 2; k <= np; k <<= 1)
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) {
+        const uint32_t l = i ^ j;
+        if (l > i) {
+          const unsigned long long a = key[i], b = key[l];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            key[i] = b;
+            key[l] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  SortTask mine[kOrderMax / 1024];
+#pragma unroll
+  for (int q = 0; q < kOrderMax / 1024; ++q) {
+    const uint32_t i = threadIdx.x + q * 1024;
+    if (i < n) mine[q] = list[(uint32_t)key[i]];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < kOrderMax / 1024; ++q) {
+    const uint32_t i = threadIdx.x + q * 1024;
+    if (i < n) list[i] = mine[q];
+  }
 }
 
 // Block copy with four independent vector loads in flight per thread.
@@ -1227,7 +1274,8 @@ cudaError_t build_tasks(const uint32_t* offsets, int grid, const uint64_t* split
                         const TaskListsHost& lists, uint32_t* err, uint32_t* stats, cudaStream_t stream) {
   k_build_tasks<<<(nbuckets + 255) / 256, 256, 0, stream>>>(offsets, grid, splitters, nbuckets, n, lists_of(lists),
                                                             err, stats);
-  note_launches(1);
+  k_order_tasks<<<1, 1024, 0, stream>>>(lists.split_out, lists.nsplit_out);
+  note_launches(2);
   return cudaGetLastError();
 }
 
