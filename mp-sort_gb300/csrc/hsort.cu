@@ -742,7 +742,9 @@ __device__ __forceinline__ void block_minmax(uint64_t& mn, uint64_t& mx, uint64_
 // kInsertMax go back unchanged and are queued for another pass.  With
 // by_idx the bins are the input indices themselves (a bin of equal keys is
 // put back in input order; indices are distinct and below kLocalMax).
-template <int NT>
+// PACKED: the keys are ((key - min) << kLocalBits) | input index, distinct
+// and ordered as (key, index); the index arrays are not used.
+template <int NT, bool PACKED>
 __device__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint32_t s, uint64_t mn, uint64_t mx,
                                bool by_idx) {
   constexpr int kBins = 1 << kLocalBits;
@@ -757,7 +759,7 @@ __device__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint32_t s, uint6
   for (int r = 0; r < PER; ++r) {
     const uint32_t e = r * NT + threadIdx.x;
     if (e < s) {
-      bin[r] = by_idx ? (uint32_t)sm.idxA[a + e] : (uint32_t)((sm.keyA[a + e] - mn) >> shift);
+      bin[r] = !PACKED && by_idx ? (uint32_t)sm.idxA[a + e] : (uint32_t)((sm.keyA[a + e] - mn) >> shift);
       slot[r] = atomicAdd(&sm.cnt[bin[r]], 1u);
     }
   }
@@ -785,14 +787,14 @@ __device__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint32_t s, uint6
     if (e < s) {
       const uint32_t pos = sm.start[bin[r]] + slot[r];
       sm.keyB[a + pos] = sm.keyA[a + e];
-      sm.idxB[a + pos] = sm.idxA[a + e];
+      if (!PACKED) sm.idxB[a + pos] = sm.idxA[a + e];
     }
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < s; i += NT) {
     const uint64_t kv = sm.keyB[a + i];
-    const uint16_t iv = sm.idxB[a + i];
-    const uint32_t d = by_idx ? (uint32_t)iv : (uint32_t)((kv - mn) >> shift);
+    const uint16_t iv = PACKED ? 0 : sm.idxB[a + i];
+    const uint32_t d = !PACKED && by_idx ? (uint32_t)iv : (uint32_t)((kv - mn) >> shift);
     const uint32_t b0 = sm.start[d], b1 = sm.start[d + 1];
     const uint32_t sz = b1 - b0;
     uint32_t at = i;
@@ -800,7 +802,8 @@ __device__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint32_t s, uint6
       uint32_t r = 0;
       for (uint32_t j = b0; j < b1; ++j) {
         const uint64_t kj = sm.keyB[a + j];
-        r += (kj < kv) || (kj == kv && sm.idxB[a + j] < iv);
+        if (PACKED) r += kj < kv;
+        else r += (kj < kv) || (kj == kv && sm.idxB[a + j] < iv);
       }
       at = b0 + r;
     } else if (i == b0) {
@@ -809,46 +812,14 @@ __device__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint32_t s, uint6
       sm.bigsz[q] = (uint16_t)sz;
     }
     sm.keyA[a + at] = kv;
-    sm.idxA[a + at] = iv;
+    if (!PACKED) sm.idxA[a + at] = iv;
   }
   __syncthreads();
 }
 
-// Stable sort of `m` <= kLocalMax records of src by key into dst (distinct).
-template <int EW, int NT>
-__device__ void local_sort(LocalSmemT<NT>& sm, const uint8_t* src, uint8_t* dst, uint32_t m,
-                           const gbsort_key_word& kw, uint32_t* stats) {
-  constexpr int kLocalRpt = kLocalMax / NT;
-  constexpr uint32_t E = EW * 4;
-  const uint32_t w = warp_id(), lane = lane_id();
-  uint64_t mn = ~0ull, mx = 0;
-  {
-    uint64_t k[kLocalRpt];
-#pragma unroll
-    for (int r = 0; r < kLocalRpt; ++r) {
-      uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
-      k[r] = e < m ? key_at(src, e, E, kw) : 0;
-    }
-#pragma unroll
-    for (int r = 0; r < kLocalRpt; ++r) {
-      uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
-      if (e < m) {
-        sm.keyA[e] = k[r];
-        sm.idxA[e] = (uint16_t)e;
-        mn = k[r] < mn ? k[r] : mn;
-        mx = k[r] > mx ? k[r] : mx;
-      }
-    }
-  }
-  if (threadIdx.x == 0) sm.nbig = 0;
-  block_minmax<NT>(mn, mx, sm.red);
-  if (mn == mx) {  // one key: the input order is the stable order
-    block_copy_ilp<EW>(src, dst, m, NT);
-    __syncthreads();
-    return;
-  }
-  local_msd_pass<NT>(sm, 0, m, mn, mx, false);
-  // further passes over bins too large for insertion sort
+// Further passes over the bins too large to place by counting.
+template <int NT, bool PACKED>
+__device__ void local_big_bins(LocalSmemT<NT>& sm, uint32_t* stats) {
   for (;;) {
     uint32_t nb = sm.nbig;
     __syncthreads();
@@ -864,8 +835,57 @@ __device__ void local_sort(LocalSmemT<NT>& sm, const uint8_t* src, uint8_t* dst,
     }
     block_minmax<NT>(bmn, bmx, sm.red);
     if (threadIdx.x == 0) atomicAdd(stats + STAT_BIGBIN, 1u);
-    // equal keys: back into input order (their bin filled in any order)
-    local_msd_pass<NT>(sm, a, s, bmn, bmx, bmn == bmx);
+    // equal keys: back into input order (their bin filled in any order);
+    // packed keys are never equal
+    local_msd_pass<NT, PACKED>(sm, a, s, bmn, bmx, !PACKED && bmn == bmx);
+  }
+}
+
+// Stable sort of `m` <= kLocalMax records of src by key into dst (distinct).
+template <int EW, int NT>
+__device__ void local_sort(LocalSmemT<NT>& sm, const uint8_t* src, uint8_t* dst, uint32_t m,
+                           const gbsort_key_word& kw, uint32_t* stats) {
+  constexpr int kLocalRpt = kLocalMax / NT;
+  constexpr uint32_t E = EW * 4;
+  const uint32_t w = warp_id(), lane = lane_id();
+  uint64_t mn = ~0ull, mx = 0;
+  uint64_t k[kLocalRpt];
+#pragma unroll
+  for (int r = 0; r < kLocalRpt; ++r) {
+    uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
+    k[r] = e < m ? key_at(src, e, E, kw) : 0;
+    if (e < m) {
+      mn = k[r] < mn ? k[r] : mn;
+      mx = k[r] > mx ? k[r] : mx;
+    }
+  }
+  if (threadIdx.x == 0) sm.nbig = 0;
+  block_minmax<NT>(mn, mx, sm.red);
+  if (mn == mx) {  // one key: the input order is the stable order
+    block_copy_ilp<EW>(src, dst, m, NT);
+    __syncthreads();
+    return;
+  }
+  // a key range of at most 64 - kLocalBits bits leaves room for the input
+  // index below the key: one distinct 64-bit word per record
+  const bool packed = bitlen64(mx - mn) <= 64 - kLocalBits;
+#pragma unroll
+  for (int r = 0; r < kLocalRpt; ++r) {
+    uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
+    if (e < m) {
+      sm.keyA[e] = packed ? ((k[r] - mn) << kLocalBits) | e : k[r];
+      sm.idxA[e] = (uint16_t)e;
+    }
+  }
+  __syncthreads();
+  if (packed) {
+    local_msd_pass<NT, true>(sm, 0, m, 0, ((mx - mn) << kLocalBits) | (kLocalMax - 1), false);
+    local_big_bins<NT, true>(sm, stats);
+    for (uint32_t i = threadIdx.x; i < m; i += NT) sm.idxA[i] = (uint16_t)(sm.keyA[i] & (kLocalMax - 1));
+    __syncthreads();
+  } else {
+    local_msd_pass<NT, false>(sm, 0, m, mn, mx, false);
+    local_big_bins<NT, false>(sm, stats);
   }
   // gather the records into dst in sorted order, four loads in flight
   {
