@@ -745,7 +745,7 @@ __device__ __forceinline__ void block_minmax(uint64_t& mn, uint64_t& mx, uint64_
 // PACKED: the keys are ((key - min) << kLocalBits) | input index, distinct
 // and ordered as (key, index); the index arrays are not used.
 template <int NT, bool PACKED>
-__device__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint32_t s, uint64_t mn, uint64_t mx,
+__device__ __noinline__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint32_t s, uint64_t mn, uint64_t mx,
                                bool by_idx) {
   constexpr int kBins = 1 << kLocalBits;
   constexpr int PER = kLocalMax / NT;
