@@ -118,8 +118,23 @@ enum CounterSlot : int {
   CNT_WORDS = 64
 };
 
+constexpr int kMaxPieces = 16;  // host -> device pieces of a pipelined host sort
+constexpr int kMaxWaves = 16;   // level-2 waves (and device -> host pieces)
+
 struct HostCounters {  // pinned: the device counters of the last run are copied here
   uint32_t c[CNT_WORDS];
+  uint32_t starts[kMaxWaves + 1];  // first output record of each wave
+};
+
+// A host sort whose copies overlap the device work: the input goes up in
+// pieces aligned to the count kernel's chunks (each piece counted as it
+// lands), and level 2 runs in waves of level-1 buckets, each wave's output
+// range going down while the next wave sorts.
+struct HostPipe {
+  const uint8_t* h_in;
+  uint8_t* h_out;
+  int pieces;
+  int waves;
 };
 
 struct Context {
@@ -133,6 +148,8 @@ struct Context {
   DevBuf radix;            // host radix bytes (callback path)
   HostCounters* hc = nullptr;
   cudaEvent_t ev[8] = {};  // stage boundaries of the histogram sort
+  cudaStream_t cstream = nullptr;                // copies of a pipelined host sort
+  cudaEvent_t pev[kMaxPieces] = {}, wev[kMaxWaves] = {}, sev = nullptr, dev_done = nullptr;
   std::mutex mu;
   // shape of the last enqueued histogram sort (for hsort_collect)
   uint32_t run_nbuckets = 0, run_sample = 0, run_lsd_passes = 0;
@@ -145,8 +162,13 @@ Context* g_ctx[64] = {};
 int ctx_init(Context& c, int dev) {
   c.device = dev;
   GB_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  GB_CUDA(cudaStreamCreateWithFlags(&c.cstream, cudaStreamNonBlocking));
   GB_CUDA(cudaMallocHost(&c.hc, sizeof(HostCounters)));
   for (cudaEvent_t& e : c.ev) GB_CUDA(cudaEventCreate(&e));
+  for (cudaEvent_t& e : c.pev) GB_CUDA(cudaEventCreate(&e));
+  for (cudaEvent_t& e : c.wev) GB_CUDA(cudaEventCreate(&e));
+  GB_CUDA(cudaEventCreate(&c.sev));
+  GB_CUDA(cudaEventCreate(&c.dev_done));
   return GBSORT_OK;
 }
 
@@ -154,10 +176,19 @@ void ctx_destroy(Context& c) {
   if (c.stream) cudaStreamSynchronize(c.stream);
   DevBuf* bufs[] = {&c.A, &c.B, &c.hin, &c.hout, &c.keysA, &c.keysB, &c.idxA, &c.idxB, &c.small, &c.radix};
   for (DevBuf* b : bufs) b->release();
+  if (c.cstream) cudaStreamSynchronize(c.cstream);
   for (cudaEvent_t& e : c.ev)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t& e : c.pev)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t& e : c.wev)
+    if (e) cudaEventDestroy(e);
+  if (c.sev) cudaEventDestroy(c.sev);
+  if (c.dev_done) cudaEventDestroy(c.dev_done);
   if (c.hc) cudaFreeHost(c.hc);
   if (c.stream) cudaStreamDestroy(c.stream);
+  if (c.cstream) cudaStreamDestroy(c.cstream);
+  c.cstream = nullptr;
   c.hc = nullptr;
   c.stream = nullptr;
 }
@@ -452,7 +483,7 @@ int run_level2(const HsortParams& p, const Level2& l2, uint32_t* stats, uint32_t
 // anywhere (so it can be captured into a CUDA graph); the device counters
 // end up in c.hc once the stream reaches the end.  hsort_collect reads them.
 int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize, const gbsort_key_desc* key,
-                  bool learned, bool timing, const Knobs& knobs, cudaStream_t st) {
+                  bool learned, bool timing, const Knobs& knobs, cudaStream_t st, const HostPipe* hp = nullptr) {
   GB_CUDA(c.A.ensure((size_t)n * elsize));
   GB_CUDA(c.B.ensure((size_t)n * elsize));
   const int nb = choose_buckets(n, knobs);
@@ -493,11 +524,23 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
 
   ModelDev model{};
   int lookup = LOOKUP_PLAIN;
+  // pipelined: the input goes up in pieces of whole count chunks
+  const int pieces = hp ? std::min(hp->pieces, std::min(kMaxPieces, grid)) : 1;
+  if (hp)
+    for (int i = 0; i < pieces; ++i) {
+      const uint32_t r0 = hsort_chunk_begin(n, i * grid / pieces), r1 = hsort_chunk_begin(n, (i + 1) * grid / pieces);
+      GB_CUDA(cudaMemcpyAsync((uint8_t*)d_in + (size_t)r0 * elsize, hp->h_in + (size_t)r0 * elsize,
+                              (size_t)(r1 - r0) * elsize, cudaMemcpyHostToDevice, c.cstream));
+      GB_CUDA(cudaEventRecord(c.pev[i], c.cstream));
+    }
   if (timing) GB_CUDA(cudaEventRecord(c.ev[0], st));
   if (nb > 1) {
     uint64_t* sA = bump.take<uint64_t>(s);
     uint64_t* sB = bump.take<uint64_t>(s);
-    GB_CUDA(sample_keys(p.in, n, elsize, p.key, s, sA, st));
+    // pipelined: the sample is read from the pinned host array itself by the
+    // sampling kernel (over the host link, without waiting for the copy
+    // engine, which is busy with the pieces)
+    GB_CUDA(sample_keys(hp ? hp->h_in : p.in, n, elsize, p.key, s, sA, st));
     int rc = lsd_sort_keys(bump, sA, sB, nullptr, nullptr, s, 1, false, nullptr, err, st);
     if (rc) return rc;
     if (!learned) {
@@ -538,32 +581,89 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
     }
   }
   if (timing) GB_CUDA(cudaEventRecord(c.ev[1], st));
-  GB_CUDA(l1_count(p, lookup, S, nb, lookup == LOOKUP_LEARNED ? &model : nullptr, counts, stats, st));
+  const ModelDev* mp = lookup == LOOKUP_LEARNED ? &model : nullptr;
+  if (hp) {  // each piece is counted as soon as it has landed
+    for (int i = 0; i < pieces; ++i) {
+      GB_CUDA(cudaStreamWaitEvent(st, c.pev[i], 0));
+      GB_CUDA(l1_count(p, lookup, S, nb, mp, counts, stats, st, i * grid / pieces, (i + 1) * grid / pieces));
+    }
+  } else {
+    GB_CUDA(l1_count(p, lookup, S, nb, mp, counts, stats, st));
+  }
   if (timing) GB_CUDA(cudaEventRecord(c.ev[2], st));
   GB_CUDA(exclusive_scan_u32(counts, counts, (size_t)nb * grid, scan_tmp, st));
-  if (timing) GB_CUDA(cudaEventRecord(c.ev[3], st));
-  GB_CUDA(l1_scatter(p, lookup, S, nb, lookup == LOOKUP_LEARNED ? &model : nullptr, counts, stats, st));
-  if (timing) GB_CUDA(cudaEventRecord(c.ev[4], st));
-  {
-    TaskListsHost L = l2.round(-1);  // appends to split[0]
-    GB_CUDA(build_tasks(counts, grid, S, nb, n, L, err, stats, st));
+  // pipelined: the first output record of every wave of level-1 buckets
+  const int waves = hp ? std::max(1, std::min(std::min(hp->waves, kMaxWaves), nb)) : 1;
+  if (hp) {
+    for (int j = 0; j < waves; ++j)
+      GB_CUDA(cudaMemcpyAsync(&c.hc->starts[j], counts + (size_t)(j * nb / waves) * grid, 4, cudaMemcpyDeviceToHost,
+                              st));
+    c.hc->starts[waves] = n;
+    GB_CUDA(cudaEventRecord(c.sev, st));
   }
+  if (timing) GB_CUDA(cudaEventRecord(c.ev[3], st));
+  GB_CUDA(l1_scatter(p, lookup, S, nb, mp, counts, stats, st));
+  if (timing) GB_CUDA(cudaEventRecord(c.ev[4], st));
   static const bool trace = getenv("GBSORT_TRACE") != nullptr;
-  for (int r = 0; r < kSplitRounds; ++r) {
-    TaskListsHost L = l2.round(r);
-    GB_CUDA(cudaMemsetAsync(L.nsplit_out, 0, sizeof(uint32_t), st));
-    GB_CUDA(run_split_round(p, L, l2.work, stats, err, st));
-    if (trace && timing) {  // debugging aid: split tasks per round (synchronises)
-      uint32_t h[3];
-      GB_CUDA(cudaMemcpyAsync(h, l2.nsplit, 12, cudaMemcpyDeviceToHost, st));
-      GB_CUDA(cudaStreamSynchronize(st));
-      fprintf(stderr, "gbsort trace: round %d in %u out %u local %u\n", r, h[r & 1], h[(r + 1) & 1], h[2]);
+  for (int j = 0; j < waves; ++j) {
+    if (hp) {  // the wave's lists start empty
+      GB_CUDA(cudaMemsetAsync(l2.nsplit, 0, sizeof(uint32_t), st));
+      GB_CUDA(cudaMemsetAsync(l2.nlocal, 0, sizeof(uint32_t), st));
+    }
+    {
+      TaskListsHost L = l2.round(-1);  // appends to split[0]
+      GB_CUDA(build_tasks(counts, grid, S, nb, n, L, err, stats, st, j * nb / waves, (j + 1) * nb / waves));
+    }
+    for (int r = 0; r < kSplitRounds; ++r) {
+      TaskListsHost L = l2.round(r);
+      GB_CUDA(cudaMemsetAsync(L.nsplit_out, 0, sizeof(uint32_t), st));
+      GB_CUDA(run_split_round(p, L, l2.work, stats, err, st));
+      if (trace && timing) {  // debugging aid: split tasks per round (synchronises)
+        uint32_t h[3];
+        GB_CUDA(cudaMemcpyAsync(h, l2.nsplit, 12, cudaMemcpyDeviceToHost, st));
+        GB_CUDA(cudaStreamSynchronize(st));
+        fprintf(stderr, "gbsort trace: round %d in %u out %u local %u\n", r, h[r & 1], h[(r + 1) & 1], h[2]);
+      }
+    }
+    if (timing) GB_CUDA(cudaEventRecord(c.ev[5], st));
+    GB_CUDA(run_local(p, l2.local, l2.nlocal, l2.cap_local, l2.work, stats, st));
+    if (hp) {
+      GB_CUDA(require_zero(l2.nsplit + (kSplitRounds & 1), err, st));
+      GB_CUDA(cudaEventRecord(c.wev[j], st));
     }
   }
-  if (timing) GB_CUDA(cudaEventRecord(c.ev[5], st));
-  GB_CUDA(run_local(p, l2.local, l2.nlocal, l2.cap_local, l2.work, stats, st));
   if (timing) GB_CUDA(cudaEventRecord(c.ev[6], st));
   GB_CUDA(cudaMemcpyAsync(c.hc->c, counters, CNT_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  if (hp) {  // each wave's output range goes down as soon as the wave is sorted
+    GB_CUDA(cudaEventSynchronize(c.sev));
+    for (int j = 0; j < waves; ++j) {
+      const uint32_t r0 = c.hc->starts[j], r1 = c.hc->starts[j + 1];
+      if (r1 < r0 || r1 > n) {
+        set_err("wave bounds out of order");
+        return GBSORT_ERR_INTERNAL;
+      }
+      GB_CUDA(cudaStreamWaitEvent(c.cstream, c.wev[j], 0));
+      if (r1 > r0)
+        GB_CUDA(cudaMemcpyAsync(hp->h_out + (size_t)r0 * elsize, (const uint8_t*)d_out + (size_t)r0 * elsize,
+                                (size_t)(r1 - r0) * elsize, cudaMemcpyDeviceToHost, c.cstream));
+    }
+    GB_CUDA(cudaEventRecord(c.dev_done, c.cstream));
+    static const bool ptrace = getenv("GBSORT_PIPE_TRACE") != nullptr;
+    if (ptrace) {  // debugging aid: the pipeline's timeline (synchronises)
+      GB_CUDA(cudaEventSynchronize(c.dev_done));
+      float t;
+      cudaEventElapsedTime(&t, c.pev[0], c.pev[pieces - 1]);
+      fprintf(stderr, "gbsort pipe: pieces up by %.2f ms (after the first)\n", t);
+      cudaEventElapsedTime(&t, c.pev[0], c.sev);
+      fprintf(stderr, "gbsort pipe: counts scanned at %.2f\n", t);
+      for (int j = 0; j < waves; ++j) {
+        cudaEventElapsedTime(&t, c.pev[0], c.wev[j]);
+        fprintf(stderr, "gbsort pipe: wave %d sorted at %.2f\n", j, t);
+      }
+      cudaEventElapsedTime(&t, c.pev[0], c.dev_done);
+      fprintf(stderr, "gbsort pipe: last piece down at %.2f\n", t);
+    }
+  }
   c.run_nbuckets = (uint32_t)nb;
   c.run_sample = s;
   c.run_learned = learned;
@@ -691,6 +791,18 @@ int gbsort_sort_device(const void* d_in, void* d_out, size_t nmemb, size_t elsiz
   return sort_device_locked(*c, d_in, d_out, nmemb, elsize, key, method, st);
 }
 
+namespace {
+constexpr size_t kPipelineMin = (size_t)1 << 22;  // records; smaller host sorts copy in one piece each way
+bool is_pinned(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+}  // namespace
+
 int gbsort_sort_host(const void* in, void* out, size_t nmemb, size_t elsize, const gbsort_key_desc* key,
                      int method) {
   if (nmemb == 0) return GBSORT_OK;
@@ -706,6 +818,30 @@ int gbsort_sort_host(const void* in, void* out, size_t nmemb, size_t elsize, con
   const size_t bytes = nmemb * elsize;
   GB_CUDA(c->hin.ensure(bytes));
   GB_CUDA(c->hout.ensure(bytes));
+  // large sorts of pinned host arrays overlap their copies with the device
+  // work (pieces up, waves down); pageable arrays would make every copy
+  // synchronous, so they take the plain path
+  if (nmemb >= kPipelineMin && nmemb < 0xffffffffull && is_pinned(in) && is_pinned(out)) {
+    const uint32_t n = (uint32_t)nmemb, E = (uint32_t)elsize;
+    const bool hs_ok = hsort_layout_ok(c->hin.p, c->hout.p, E, key);
+    Knobs knobs;
+    int m = method == GBSORT_AUTO ? resolve_auto(E, key, n, hs_ok, &knobs) : method;
+    if (hs_ok && (m == GBSORT_HISTOGRAM_PLAIN || m == GBSORT_HISTOGRAM_LEARNED)) {
+      HostPipe hp{(const uint8_t*)in, (uint8_t*)out, 8, 8};
+      const unsigned long long l0 = launch_count();
+      rc = hsort_enqueue(*c, c->hin.p, c->hout.p, n, E, key, m == GBSORT_HISTOGRAM_LEARNED, false, knobs, c->stream,
+                         &hp);
+      cudaError_t e1 = cudaStreamSynchronize(c->stream), e2 = cudaStreamSynchronize(c->cstream);
+      if (rc) return rc;
+      if (e1 != cudaSuccess || e2 != cudaSuccess) {
+        set_err("pipelined host sort: %s", cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+        return GBSORT_ERR_CUDA;
+      }
+      rc = hsort_collect(*c);
+      if (rc == GBSORT_OK) g_stats.launches = (uint32_t)(launch_count() - l0);
+      return rc;
+    }
+  }
   GB_CUDA(cudaMemcpyAsync(c->hin.p, in, bytes, cudaMemcpyHostToDevice, c->stream));
   rc = sort_device_locked(*c, c->hin.p, c->hout.p, nmemb, elsize, key, method, c->stream);
   if (rc) return rc;

@@ -269,14 +269,14 @@ template <int LK>
 __global__ void __launch_bounds__(kThreads, 2) k_l1_count(HsortParams p, const uint64_t* __restrict__ S,
                                                         int nbuckets, ModelDev model,
                                                         uint32_t* __restrict__ counts,
-                                                        uint32_t* __restrict__ stats) {
+                                                        uint32_t* __restrict__ stats, uint32_t c0, uint32_t nchunks) {
   model = resolve_model(model);
   extern __shared__ __align__(16) uint8_t smem[];
   LookupSmem L;
   uint32_t* hist = reinterpret_cast<uint32_t*>(load_lookup<LK>(smem, S, nbuckets, model, L));
   for (int i = threadIdx.x; i < nbuckets; i += kThreads) hist[i] = 0;
   __syncthreads();
-  const uint32_t c = blockIdx.x, g = gridDim.x;
+  const uint32_t c = c0 + blockIdx.x, g = nchunks;  // this CTA's chunk of the nchunks
   const uint32_t cb = chunk_begin(p.n, c, g), ce = chunk_end(p.n, c, g);
   constexpr int U = 8;
   // keys of the next batch are loaded while the current batch is counted
@@ -592,9 +592,9 @@ __device__ __forceinline__ void push_copy(const TaskLists& L, uint32_t start, ui
 
 __global__ void k_build_tasks(const uint32_t* __restrict__ offsets, int grid,
                               const uint64_t* __restrict__ S, int nbuckets, uint32_t n, TaskLists L,
-                              uint32_t* err, uint32_t* stats) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nbuckets) return;
+                              uint32_t* err, uint32_t* stats, int b0, int b1) {
+  int b = b0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= b1) return;
   uint32_t start = offsets[(size_t)b * grid];
   uint32_t end = b + 1 < nbuckets ? offsets[(size_t)(b + 1) * grid] : n;
   uint32_t cnt = end - start;
@@ -1231,23 +1231,29 @@ static cudaError_t set_smem(const void* fn, size_t bytes) {
 }
 
 cudaError_t l1_count(const HsortParams& p, int lookup_kind, const uint64_t* splitters, int nbuckets,
-                     const void* model, uint32_t* counts, uint32_t* stats, cudaStream_t stream) {
+                     const void* model, uint32_t* counts, uint32_t* stats, cudaStream_t stream, int c0, int c1) {
   const ModelDev m = model ? *(const ModelDev*)model : ModelDev{};
   const int g = hsort_grid(p.n);
+  if (c1 < 0) c1 = g;
+  if (c1 <= c0) return cudaSuccess;
   cudaError_t e;
   if (lookup_kind == LOOKUP_LEARNED) {
     size_t sm = lookup_smem_bytes<LOOKUP_LEARNED>(nbuckets, &m) + 4 * (size_t)nbuckets;
     if ((e = set_smem((const void*)k_l1_count<LOOKUP_LEARNED>, sm)) != cudaSuccess) return e;
-    k_l1_count<LOOKUP_LEARNED><<<g, kThreads, sm, stream>>>(p, splitters, nbuckets, m, counts, stats);
+    k_l1_count<LOOKUP_LEARNED><<<c1 - c0, kThreads, sm, stream>>>(p, splitters, nbuckets, m, counts, stats,
+                                                                  (uint32_t)c0, (uint32_t)g);
     note_launches(1);
   } else {
     size_t sm = lookup_smem_bytes<LOOKUP_PLAIN>(nbuckets, &m) + 4 * (size_t)nbuckets;
     if ((e = set_smem((const void*)k_l1_count<LOOKUP_PLAIN>, sm)) != cudaSuccess) return e;
-    k_l1_count<LOOKUP_PLAIN><<<g, kThreads, sm, stream>>>(p, splitters, nbuckets, m, counts, stats);
+    k_l1_count<LOOKUP_PLAIN><<<c1 - c0, kThreads, sm, stream>>>(p, splitters, nbuckets, m, counts, stats,
+                                                                (uint32_t)c0, (uint32_t)g);
     note_launches(1);
   }
   return cudaGetLastError();
 }
+
+uint32_t hsort_chunk_begin(uint32_t n, int c) { return c >= hsort_grid(n) ? n : chunk_begin(n, (uint32_t)c, (uint32_t)hsort_grid(n)); }
 
 cudaError_t l1_scatter(const HsortParams& p, int lookup_kind, const uint64_t* splitters, int nbuckets,
                        const void* model, const uint32_t* offsets, uint32_t* stats, cudaStream_t stream) {
@@ -1290,10 +1296,23 @@ static TaskLists lists_of(const TaskListsHost& h) {
   return L;
 }
 
+__global__ void k_require_zero(const uint32_t* count, uint32_t* err) {
+  if (threadIdx.x == 0 && *count != 0) set_error(err, DEV_ERR_LEVELS);
+}
+
+cudaError_t require_zero(const uint32_t* count, uint32_t* err, cudaStream_t stream) {
+  k_require_zero<<<1, 32, 0, stream>>>(count, err);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
 cudaError_t build_tasks(const uint32_t* offsets, int grid, const uint64_t* splitters, int nbuckets, uint32_t n,
-                        const TaskListsHost& lists, uint32_t* err, uint32_t* stats, cudaStream_t stream) {
-  k_build_tasks<<<(nbuckets + 255) / 256, 256, 0, stream>>>(offsets, grid, splitters, nbuckets, n, lists_of(lists),
-                                                            err, stats);
+                        const TaskListsHost& lists, uint32_t* err, uint32_t* stats, cudaStream_t stream, int b0,
+                        int b1) {
+  if (b1 < 0) b1 = nbuckets;
+  if (b1 <= b0) return cudaSuccess;
+  k_build_tasks<<<(b1 - b0 + 255) / 256, 256, 0, stream>>>(offsets, grid, splitters, nbuckets, n, lists_of(lists),
+                                                           err, stats, b0, b1);
   k_order_tasks<<<1, 1024, 0, stream>>>(lists.split_out, lists.nsplit_out);
   note_launches(2);
   return cudaGetLastError();

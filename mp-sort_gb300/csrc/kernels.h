@@ -102,8 +102,12 @@ cudaError_t finalize_splitters(uint64_t* splitters, int nsplit, cudaStream_t str
 // Level-1 bucket counts per chunk ([nbuckets][grid]) and the stable scatter.
 // `model` points to a host copy of the ModelDev (cdf.cuh) for the learned
 // lookup, else null.  `stats` is the device statistics array (Stat indices).
+// l1_count counts chunks [c0, c1) of the hsort_grid(n) chunks (c1 < 0: all).
 cudaError_t l1_count(const HsortParams& p, int lookup, const uint64_t* splitters, int nbuckets,
-                     const void* model, uint32_t* counts, uint32_t* stats, cudaStream_t stream);
+                     const void* model, uint32_t* counts, uint32_t* stats, cudaStream_t stream, int c0 = 0,
+                     int c1 = -1);
+// First record of count chunk c (n for c >= hsort_grid(n)).
+uint32_t hsort_chunk_begin(uint32_t n, int c);
 cudaError_t l1_scatter(const HsortParams& p, int lookup, const uint64_t* splitters, int nbuckets,
                        const void* model, const uint32_t* offsets, uint32_t* stats, cudaStream_t stream);
 // Level-2 task lists (device memory).  A split round consumes split_in and
@@ -118,9 +122,12 @@ struct TaskListsHost {
   uint32_t cap_split;
   uint32_t cap_local;
 };
+// Tasks of level-1 buckets [b0, b1) (b1 < 0: all), largest split first.
 cudaError_t build_tasks(const uint32_t* offsets, int grid, const uint64_t* splitters, int nbuckets,
                         uint32_t n, const TaskListsHost& lists, uint32_t* err, uint32_t* stats,
-                        cudaStream_t stream);
+                        cudaStream_t stream, int b0 = 0, int b1 = -1);
+// err gets DEV_ERR_LEVELS unless *count is zero.
+cudaError_t require_zero(const uint32_t* count, uint32_t* err, cudaStream_t stream);
 cudaError_t run_split_round(const HsortParams& p, const TaskListsHost& lists, uint32_t* work_counter,
                             uint32_t* stats, uint32_t* err, cudaStream_t stream);
 cudaError_t run_local(const HsortParams& p, const SortTask* tasks, const uint32_t* ntasks, uint32_t cap,

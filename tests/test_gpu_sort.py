@@ -545,3 +545,28 @@ def test_autotune_feeds_auto(mp, given):
     if best["method"] != "lsd":
         assert st["nbuckets"] <= best["max_buckets"]
     device.tuning_clear()
+
+
+# ------------------------------------------------- pipelined host sorts --
+@pytest.mark.parametrize("method", ["auto", "plain", "learned"])
+@pytest.mark.parametrize("dist", ["uniform", "zipf", "equal", "sorted"])
+def test_host_sort_pipelined_pinned(mp, method, dist):
+    """Pinned host arrays of 2^22 records or more take the pipelined host
+    sort (pieces up while counting, waves down while sorting); the result is
+    the same stable order, out of place and in place."""
+    import torch
+    rng = numpy.random.default_rng(51)
+    dt = numpy.dtype([('key', 'u8'), ('val', 'i8')])
+    n = 5_000_000
+    a = make(dt, 'key', n, dist, rng)
+    pin_in = torch.empty(n * dt.itemsize, dtype=torch.uint8, pin_memory=True)
+    pin_out = torch.empty_like(pin_in, pin_memory=True)
+    hin = pin_in.numpy().view(dt)
+    hout = pin_out.numpy().view(dt)
+    hin[:] = a
+    mp.sort(hin, 'key', out=hout, method=method)
+    exp = O.numpy_sorted(a, 'key')
+    assert hout.tobytes() == exp.tobytes()
+    assert hin.tobytes() == a.tobytes()
+    mp.sort(hin, 'key', method=method)  # in place
+    assert hin.tobytes() == exp.tobytes()
