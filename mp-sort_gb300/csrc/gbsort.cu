@@ -464,6 +464,7 @@ struct Level2 {
   }
 };
 
+constexpr uint64_t kAutoLsdMax = (uint64_t)1 << 23;  // method auto, untuned: LSD up to this many records
 constexpr int kSplitRounds = 16;  // every round narrows each re-split range; 64-bit keys need few
 constexpr int kCdfEpochs = 8;     // gradient steps of the CDF model
 
@@ -734,7 +735,9 @@ int resolve_auto(uint32_t elsize, const gbsort_key_desc* key, uint64_t n, bool h
       return t.method;
     }
   }
-  return hs_ok ? GBSORT_HISTOGRAM_LEARNED : GBSORT_LSD;
+  // untuned: below about 8M records the LSD path's few full passes beat the
+  // histogram sort's fixed costs (measured crossover 8M-16M, 16 B records)
+  return hs_ok && n > kAutoLsdMax ? GBSORT_HISTOGRAM_LEARNED : GBSORT_LSD;
 }
 
 int sort_device_locked(Context& c, const void* d_in, void* d_out, size_t nmemb, size_t elsize,

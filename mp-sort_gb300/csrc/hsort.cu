@@ -431,6 +431,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
   constexpr int RPT = ScatterTile<EW>::kRpt, T = ScatterTile<EW>::kSize;
   constexpr bool kPre = ScatterTile<EW>::kPrefetch;
   constexpr bool kCombine = EW == 4;
+  constexpr uint32_t E = EW * 4;
   constexpr uint32_t kNoSlot = 0xffffffffu;
   extern __shared__ __align__(16) uint8_t smem[];
   LookupSmem L;
@@ -441,12 +442,18 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
   if (kCombine) q += 4 * (size_t)((nbuckets + 3) & ~3);
   uint4* held = reinterpret_cast<uint4*>(q);  // the held record of each bucket
   if (kCombine) q += 16 * (size_t)nbuckets;
+  // other record sizes: the tile and its destinations, written out by
+  // consecutive threads taking consecutive words of a record (one memory
+  // request per record or two, not one per word)
+  uint8_t* stage = q;
+  if (!kCombine) q += (size_t)T * E;
+  uint32_t* wdest = reinterpret_cast<uint32_t*>(q);
+  if (!kCombine) q += 4 * (size_t)T;
   uint8_t* cnt = q;  // [nbuckets][kWarps]
   for (int i = threadIdx.x; i < nbuckets * kWarps / 16; i += kThreads)
     reinterpret_cast<uint4*>(cnt)[i] = make_uint4(0, 0, 0, 0);
 
   const uint32_t w = warp_id(), lane = lane_id();
-  const uint32_t E = EW * 4;
   // the count kernel's chunks, several per CTA
   for (uint32_t c = blockIdx.x; c < (uint32_t)nchunks; c += gridDim.x) {
   const uint32_t g = (uint32_t)nchunks;
@@ -502,6 +509,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
     for (int r = 0; r < RPT; ++r) {
       tot[r] = 0;
       hold[r] = kNoSlot;
+      if (!kCombine) wdest[w * 32 * RPT + r * 32 + lane] = kNoSlot;
       if (bkt[r] == kNoBucket) continue;
       uint32_t all;
       const uint32_t at = tile_rank(bkt[r], rank[r], cnt, all);
@@ -512,7 +520,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
         continue;
       }
       uint8_t* to = p.bufA + (size_t)dest * E;
-      if constexpr (kCombine) {
+      if constexpr (!kCombine) {
+        const uint32_t e = w * 32 * RPT + r * 32 + lane;
+        RecIO<EW>::store(stage + (size_t)e * E, rec[r]);
+        wdest[e] = dest;
+        continue;
+      } else {
         if ((dest & 1u) == 0 && at + 1 == all) {  // starts a sector whose partner comes later
           hold[r] = dest;
           continue;
@@ -525,6 +538,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
       RecIO<EW>::store(to, rec[r]);
     }
     __syncthreads();
+    if constexpr (!kCombine) {
+      using V = typename std::conditional<E % 16 == 0, uint4,
+                                          typename std::conditional<E % 8 == 0, uint2, uint32_t>::type>::type;
+      constexpr uint32_t VPR = E / sizeof(V);
+      for (uint32_t f = threadIdx.x; f < nvalid * VPR; f += kThreads) {
+        const uint32_t i = f / VPR, qw = f % VPR;
+        const uint32_t d = wdest[i];
+        if (d != kNoSlot)
+          reinterpret_cast<V*>(p.bufA + (size_t)d * E)[qw] = reinterpret_cast<const V*>(stage + (size_t)i * E)[qw];
+      }
+    }
     // 3. advance the cursors, hold the open sectors, clear the rows
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
@@ -552,7 +576,8 @@ template <int EW, int LK>
 size_t l1_scatter_smem(int nbuckets, const ModelDev* m) {
   const size_t words = 4 * (size_t)((nbuckets + 3) & ~3);
   const size_t combine = EW == 4 ? words + 16 * (size_t)nbuckets : 0;
-  return lookup_smem_bytes<LK>(nbuckets, m) + words + combine + (size_t)nbuckets * kWarps;
+  const size_t stage = EW == 4 ? 0 : (size_t)ScatterTile<EW>::kSize * (EW * 4 + 4);
+  return lookup_smem_bytes<LK>(nbuckets, m) + words + combine + stage + (size_t)nbuckets * kWarps;
 }
 
 // ------------------------------------------------------------- tasks -----
@@ -1055,13 +1080,18 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
       sm.sgrp[slot] = (uint16_t)grp[r];
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < nvalid; i += kThreads) {
-      const uint32_t g = sm.sgrp[i];
-      const uint32_t dest = sm.cursor[g] + (i - sm.goff[g]);
-      uint32_t v[EW];
-      RecIO<EW>::load(sm.stage + (size_t)i * E, v);
-      if (dest < m) RecIO<EW>::store(oth + (size_t)dest * E, v);
-      else set_error(err, DEV_ERR_COUNT_MISMATCH);
+    {  // consecutive threads take consecutive words of consecutive records
+      using V = typename std::conditional<E % 16 == 0, uint4,
+                                          typename std::conditional<E % 8 == 0, uint2, uint32_t>::type>::type;
+      constexpr uint32_t VPR = E / sizeof(V);
+      for (uint32_t f = threadIdx.x; f < nvalid * VPR; f += kThreads) {
+        const uint32_t i = f / VPR, qw = f % VPR;
+        const uint32_t g = sm.sgrp[i];
+        const uint32_t dest = sm.cursor[g] + (i - sm.goff[g]);
+        if (dest < m)
+          reinterpret_cast<V*>(oth + (size_t)dest * E)[qw] = reinterpret_cast<const V*>(sm.stage + (size_t)i * E)[qw];
+        else set_error(err, DEV_ERR_COUNT_MISMATCH);
+      }
     }
     __syncthreads();
     sm.cursor[g_me] += gtot;
