@@ -1172,7 +1172,14 @@ __global__ void __launch_bounds__(NT, kLocalCtasPerSm) k_local(HsortParams p, co
     SortTask nxt{};
     if (threadIdx.x == 0) {
       nid = atomicAdd(work, 1u);
-      if (nid < nt) nxt = tasks[nid];
+      if (nid < nt) {
+        nxt = tasks[nid];
+        // the next task's records head for L2 while this one sorts
+        const uint8_t* ns = (nxt.src ? p.bufB : p.bufA) + (size_t)nxt.start * E;
+        const uint8_t* ne = ns + (size_t)nxt.count * E;
+        for (const uint8_t* q = (const uint8_t*)((uintptr_t)ns & ~(uintptr_t)127); q < ne; q += 128)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(q));
+      }
     }
     const uint8_t* src = (task.src ? p.bufB : p.bufA) + (size_t)task.start * E;
     uint8_t* out = p.out + (size_t)task.start * E;
