@@ -115,10 +115,17 @@ enum CounterSlot : int {
   CNT_LOSS = 23,         // final training loss (float)
   CNT_L2 = 24,           // level-2 task counters: nsplit[2], nlocal, work
   CNT_FALLBACK = 28,     // the learned splitters were rejected
+  CNT_OVERFLOW = 29,     // a bucket outgrew its reserved region (pipelined host sort)
   CNT_WORDS = 64
 };
 
 constexpr int kMaxPieces = 16;  // host -> device pieces of a pipelined host sort
+// Reserved bucket regions of the pipelined host sort: the sample's estimate
+// of a bucket times 1.5 plus 256 records.  With 128 sampled keys per bucket
+// the estimate's relative spread is about 9 %, so a bucket outgrows its
+// region only past five standard deviations.
+constexpr float kRegionSlack = 1.5f;
+constexpr uint32_t kRegionPad = 256;
 constexpr int kMaxWaves = 16;   // level-2 waves (and device -> host pieces)
 
 struct HostCounters {  // pinned: the device counters of the last run are copied here
@@ -485,18 +492,27 @@ int run_level2(const HsortParams& p, const Level2& l2, uint32_t* stats, uint32_t
 // end up in c.hc once the stream reaches the end.  hsort_collect reads them.
 int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize, const gbsort_key_desc* key,
                   bool learned, bool timing, const Knobs& knobs, cudaStream_t st, const HostPipe* hp = nullptr) {
-  GB_CUDA(c.A.ensure((size_t)n * elsize));
-  GB_CUDA(c.B.ensure((size_t)n * elsize));
   const int nb = choose_buckets(n, knobs);
   const int grid = hsort_grid(n);
+  // pipelined: the input goes up in pieces, each cut into `grid` count
+  // chunks, and is scattered as it lands into bucket regions reserved from
+  // the sample (slack kRegionSlack); scratch A holds the regions
+  const int pieces = hp ? std::min(hp->pieces, kMaxPieces) : 1;
+  const int G = grid * pieces;  // count chunks
+  const uint64_t a_cap64 =
+      hp ? std::min<uint64_t>((uint64_t)(n * (double)kRegionSlack) + (uint64_t)nb * (kRegionPad + 1), 0xffffffffull)
+         : n;
+  const uint32_t a_cap = (uint32_t)std::max<uint64_t>(a_cap64, n);
+  GB_CUDA(c.A.ensure((size_t)a_cap * elsize));
+  GB_CUDA(c.B.ensure((size_t)n * elsize));
   const uint64_t spb = knobs.sample_per_bucket ? (uint64_t)knobs.sample_per_bucket : 128;
   const uint32_t s = nb > 1 ? (uint32_t)std::min<uint64_t>(n, std::max<uint64_t>(4096, (uint64_t)nb * spb)) : 0;
   const uint32_t cap_split = (uint32_t)nb + n / 4096 + 4096;
   const uint32_t cap_local = 4u * (uint32_t)nb + n / 512 + 65536;
   const int lbits = 11;
   const int nleaf = 1 << lbits;
-  size_t small_bytes = (size_t)s * 16 + (size_t)nb * 8 + (size_t)nb * grid * 8 + Level2::bytes(cap_split, cap_local) +
-                       lsd_scratch_bytes(std::max<uint32_t>(s, 1), 1) + (size_t)nleaf * 64 + (size_t)nb * 4 +
+  size_t small_bytes = (size_t)s * 16 + (size_t)nb * 8 + (size_t)nb * G * 8 + Level2::bytes(cap_split, cap_local) +
+                       lsd_scratch_bytes(std::max<uint32_t>(s, 1), 1) + (size_t)nleaf * 64 + (size_t)nb * 24 +
                        (4 << 20);
   GB_CUDA(c.small.ensure(small_bytes));
   Bump bump{c.small.as<uint8_t>()};
@@ -509,8 +525,8 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
   uint32_t* fallback = counters + CNT_FALLBACK;
   GB_CUDA(cudaMemsetAsync(counters, 0, CNT_WORDS * sizeof(uint32_t), st));
   uint64_t* S = bump.take<uint64_t>((size_t)std::max(nb, 2));
-  uint32_t* counts = bump.take<uint32_t>((size_t)nb * grid);
-  uint32_t* scan_tmp = bump.take<uint32_t>(scan_tmp_words((size_t)nb * grid));
+  uint32_t* counts = bump.take<uint32_t>((size_t)nb * G);
+  uint32_t* scan_tmp = bump.take<uint32_t>(scan_tmp_words((size_t)nb * G));
   Level2 l2;
   l2.carve(bump, counters + CNT_L2, cap_split, cap_local);
 
@@ -522,22 +538,24 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
   p.n = n;
   p.elsize = elsize;
   p.key = key->word[0];
+  p.a_cap = a_cap;
+  p.chunks = (uint32_t)G;
 
   ModelDev model{};
   int lookup = LOOKUP_PLAIN;
-  // pipelined: the input goes up in pieces of whole count chunks
-  const int pieces = hp ? std::min(hp->pieces, std::min(kMaxPieces, grid)) : 1;
   if (hp)
     for (int i = 0; i < pieces; ++i) {
-      const uint32_t r0 = hsort_chunk_begin(n, i * grid / pieces), r1 = hsort_chunk_begin(n, (i + 1) * grid / pieces);
+      const uint32_t r0 = hsort_chunk_begin(n, i * grid, G), r1 = hsort_chunk_begin(n, (i + 1) * grid, G);
       GB_CUDA(cudaMemcpyAsync((uint8_t*)d_in + (size_t)r0 * elsize, hp->h_in + (size_t)r0 * elsize,
                               (size_t)(r1 - r0) * elsize, cudaMemcpyHostToDevice, c.cstream));
       GB_CUDA(cudaEventRecord(c.pev[i], c.cstream));
     }
   if (timing) GB_CUDA(cudaEventRecord(c.ev[0], st));
+  uint64_t* bump_sample = nullptr;  // the sorted sample (for the reserved regions)
   if (nb > 1) {
     uint64_t* sA = bump.take<uint64_t>(s);
     uint64_t* sB = bump.take<uint64_t>(s);
+    bump_sample = sA;
     // pipelined: the sample is read from the pinned host array itself by the
     // sampling kernel (over the host link, without waiting for the copy
     // engine, which is busy with the pieces)
@@ -583,27 +601,53 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
   }
   if (timing) GB_CUDA(cudaEventRecord(c.ev[1], st));
   const ModelDev* mp = lookup == LOOKUP_LEARNED ? &model : nullptr;
-  if (hp) {  // each piece is counted as soon as it has landed
-    for (int i = 0; i < pieces; ++i) {
-      GB_CUDA(cudaStreamWaitEvent(st, c.pev[i], 0));
-      GB_CUDA(l1_count(p, lookup, S, nb, mp, counts, stats, st, i * grid / pieces, (i + 1) * grid / pieces));
-    }
-  } else {
-    GB_CUDA(l1_count(p, lookup, S, nb, mp, counts, stats, st));
-  }
-  if (timing) GB_CUDA(cudaEventRecord(c.ev[2], st));
-  GB_CUDA(exclusive_scan_u32(counts, counts, (size_t)nb * grid, scan_tmp, st));
-  // pipelined: the first output record of every wave of level-1 buckets
+  // pipelined: each piece is counted and scattered into the reserved bucket
+  // regions as soon as it has landed; if a bucket outgrows its region the
+  // scatters stop and level 1 is redone exactly from the complete input
+  bool regions = false;
+  uint32_t *region = nullptr, *total = nullptr, *out_start = nullptr;
   const int waves = hp ? std::max(1, std::min(std::min(hp->waves, kMaxWaves), nb)) : 1;
   if (hp) {
-    for (int j = 0; j < waves; ++j)
-      GB_CUDA(cudaMemcpyAsync(&c.hc->starts[j], counts + (size_t)(j * nb / waves) * grid, 4, cudaMemcpyDeviceToHost,
-                              st));
+    uint32_t* cap = bump.take<uint32_t>(nb);
+    region = bump.take<uint32_t>(nb);
+    total = bump.take<uint32_t>(nb);
+    out_start = bump.take<uint32_t>(nb);
+    uint32_t* overflow = counters + CNT_OVERFLOW;
+    GB_CUDA(bucket_caps(bump_sample, s, S, nb, n, kRegionSlack, kRegionPad, cap, st));
+    GB_CUDA(exclusive_scan_u32(cap, region, (size_t)nb, scan_tmp, st));
+    GB_CUDA(cudaMemsetAsync(total, 0, sizeof(uint32_t) * nb, st));
+    for (int i = 0; i < pieces; ++i) {
+      GB_CUDA(cudaStreamWaitEvent(st, c.pev[i], 0));
+      GB_CUDA(l1_count(p, lookup, S, nb, mp, counts, stats, st, i * grid, (i + 1) * grid));
+      GB_CUDA(region_offsets(counts, G, nb, region, cap, total, i * grid, (i + 1) * grid, overflow, st));
+      GB_CUDA(l1_scatter(p, lookup, S, nb, mp, counts, stats, st, i * grid, (i + 1) * grid, overflow));
+    }
+    GB_CUDA(cudaMemcpyAsync(&c.hc->c[CNT_OVERFLOW], overflow, 4, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaEventRecord(c.sev, st));
+    GB_CUDA(cudaEventSynchronize(c.sev));
+    regions = c.hc->c[CNT_OVERFLOW] == 0 && !getenv("GBSORT_NO_REGIONS");
+    if (regions) {
+      GB_CUDA(exclusive_scan_u32(total, out_start, (size_t)nb, scan_tmp, st));
+    } else {  // exact level 1 over the complete input
+      p.a_cap = n;
+      GB_CUDA(l1_count(p, lookup, S, nb, mp, counts, stats, st));
+      GB_CUDA(exclusive_scan_u32(counts, counts, (size_t)nb * G, scan_tmp, st));
+      GB_CUDA(l1_scatter(p, lookup, S, nb, mp, counts, stats, st));
+    }
+    // the first output record of every wave of level-1 buckets
+    for (int j = 0; j < waves; ++j) {
+      const uint32_t* at = regions ? out_start + (size_t)(j * nb / waves) : counts + (size_t)(j * nb / waves) * G;
+      GB_CUDA(cudaMemcpyAsync(&c.hc->starts[j], at, 4, cudaMemcpyDeviceToHost, st));
+    }
     c.hc->starts[waves] = n;
     GB_CUDA(cudaEventRecord(c.sev, st));
+  } else {
+    GB_CUDA(l1_count(p, lookup, S, nb, mp, counts, stats, st));
+    if (timing) GB_CUDA(cudaEventRecord(c.ev[2], st));
+    GB_CUDA(exclusive_scan_u32(counts, counts, (size_t)nb * G, scan_tmp, st));
+    if (timing) GB_CUDA(cudaEventRecord(c.ev[3], st));
+    GB_CUDA(l1_scatter(p, lookup, S, nb, mp, counts, stats, st));
   }
-  if (timing) GB_CUDA(cudaEventRecord(c.ev[3], st));
-  GB_CUDA(l1_scatter(p, lookup, S, nb, mp, counts, stats, st));
   if (timing) GB_CUDA(cudaEventRecord(c.ev[4], st));
   static const bool trace = getenv("GBSORT_TRACE") != nullptr;
   for (int j = 0; j < waves; ++j) {
@@ -613,7 +657,11 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
     }
     {
       TaskListsHost L = l2.round(-1);  // appends to split[0]
-      GB_CUDA(build_tasks(counts, grid, S, nb, n, L, err, stats, st, j * nb / waves, (j + 1) * nb / waves));
+      if (regions)
+        GB_CUDA(build_region_tasks(region, total, out_start, S, nb, L, err, stats, st, j * nb / waves,
+                                   (j + 1) * nb / waves));
+      else
+        GB_CUDA(build_tasks(counts, G, S, nb, n, L, err, stats, st, j * nb / waves, (j + 1) * nb / waves));
     }
     for (int r = 0; r < kSplitRounds; ++r) {
       TaskListsHost L = l2.round(r);
@@ -957,6 +1005,7 @@ int gbsort_sort_segments_device(const void* d_in, void* d_out, const uint64_t* s
   p.n = N;
   p.elsize = E;
   p.key = key->word[0];
+  p.a_cap = N;
   rc = run_level2(p, l2, stats, err, st);
   if (rc) return rc;
   GB_CUDA(cudaMemcpyAsync(c->hc->c, counters, CNT_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));

@@ -425,7 +425,10 @@ template <int EW, int LK>
 __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const uint64_t* __restrict__ S,
                                                              int nbuckets, ModelDev model,
                                                              const uint32_t* __restrict__ offsets,
-                                                             int nchunks, uint32_t* __restrict__ stats) {
+                                                             int nchunks, uint32_t* __restrict__ stats,
+                                                             uint32_t c0, uint32_t c1,
+                                                             const uint32_t* __restrict__ skip_if) {
+  if (skip_if && *skip_if) return;  // a reserved region overflowed: the exact path redoes level 1
   model = resolve_model(model);
   uint32_t* err = stats + STAT_SLOTS;  // the error word follows the statistics
   constexpr int RPT = ScatterTile<EW>::kRpt, T = ScatterTile<EW>::kSize;
@@ -455,7 +458,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
 
   const uint32_t w = warp_id(), lane = lane_id();
   // the count kernel's chunks, several per CTA
-  for (uint32_t c = blockIdx.x; c < (uint32_t)nchunks; c += gridDim.x) {
+  for (uint32_t c = c0 + blockIdx.x; c < c1; c += gridDim.x) {
   const uint32_t g = (uint32_t)nchunks;
   const uint32_t cb = chunk_begin(p.n, c, g), ce = chunk_end(p.n, c, g);
   __syncthreads();
@@ -515,7 +518,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
       const uint32_t at = tile_rank(bkt[r], rank[r], cnt, all);
       const uint32_t dest = cursor[bkt[r]] + at;
       tot[r] = at + 1 == all ? all : 0;  // the run's last record advances the cursor
-      if (dest >= p.n) {
+      if (dest >= p.a_cap) {
         set_error(err, DEV_ERR_COUNT_MISMATCH);
         continue;
       }
@@ -611,7 +614,7 @@ __device__ __forceinline__ void push(SortTask* list, uint32_t* n, uint32_t cap, 
 __device__ __forceinline__ void push_copy(const TaskLists& L, uint32_t start, uint32_t cnt, uint64_t lo, uint64_t hi,
                                           uint32_t src, uint32_t* err) {
   for (uint32_t s0 = 0; s0 < cnt; s0 += kCopyPiece)
-    push(L.local, L.nlocal, L.cap_local, SortTask{start + s0, min(kCopyPiece, cnt - s0), lo, hi, src, TASK_COPY},
+    push(L.local, L.nlocal, L.cap_local, make_task(start + s0, min(kCopyPiece, cnt - s0), lo, hi, src != 0, true),
          err);
 }
 
@@ -628,8 +631,8 @@ __global__ void k_build_tasks(const uint32_t* __restrict__ offsets, int grid,
   uint64_t lo = b == 0 ? 0ull : S[b - 1];
   uint64_t hi = b == nbuckets - 1 ? ~0ull : S[b] - 1;
   if (lo == hi || cnt == 1) push_copy(L, start, cnt, lo, hi, 0u, err);
-  else if (cnt <= (uint32_t)kLocalMax) push(L.local, L.nlocal, L.cap_local, SortTask{start, cnt, lo, hi, 0u, TASK_SORT}, err);
-  else push(L.split_out, L.nsplit_out, L.cap_split, SortTask{start, cnt, lo, hi, 0u, TASK_SORT}, err);
+  else if (cnt <= (uint32_t)kLocalMax) push(L.local, L.nlocal, L.cap_local, make_task(start, cnt, lo, hi, false, false), err);
+  else push(L.split_out, L.nsplit_out, L.cap_split, make_task(start, cnt, lo, hi, false, false), err);
 }
 
 // Largest split task first: the level-1 buckets differ in size by tens of
@@ -944,8 +947,9 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
                            uint32_t* stats, uint32_t* err) {
   constexpr uint32_t E = EW * 4;
   constexpr int RPT = Tile<EW>::kRpt, T = Tile<EW>::kSize;
-  const uint8_t* src = (task.src ? p.bufB : p.bufA) + (size_t)task.start * E;
-  uint8_t* oth = (task.src ? p.bufA : p.bufB) + (size_t)task.start * E;
+  const bool in_b = (task.flags & TASK_SRC_B) != 0;
+  const uint8_t* src = (in_b ? p.bufB : p.bufA) + (size_t)task.from * E;
+  uint8_t* oth = (in_b ? p.bufA : p.bufB) + (size_t)task.start * E;
   const uint32_t m = task.count;
   int bits = bitlen64(task.hi - task.lo);
   int shift = bits > kSplitBits ? bits - kSplitBits : 0;
@@ -1107,14 +1111,14 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
     const uint32_t s = g1 - g0;
     const uint64_t glo = blo + ((uint64_t)b0 << shift);
     const uint64_t ghi = b1 >= nbins ? bhi : blo + ((uint64_t)b1 << shift) - 1;
-    const uint32_t nsrc = task.src ^ 1u;
+    const uint32_t nsrc = in_b ? 0u : 1u;
     if (glo == ghi || s == 1) {
       push_copy(L, task.start + g0, s, glo, ghi, nsrc, err);
     } else if (s <= (uint32_t)kLocalMax) {
-      push(L.local, L.nlocal, L.cap_local, SortTask{task.start + g0, s, glo, ghi, nsrc, TASK_SORT}, err);
+      push(L.local, L.nlocal, L.cap_local, make_task(task.start + g0, s, glo, ghi, nsrc != 0, false), err);
     } else {
       atomicAdd(stats + STAT_PUSHED, 1u);
-      push(L.split_out, L.nsplit_out, L.cap_split, SortTask{task.start + g0, s, glo, ghi, nsrc, TASK_SORT}, err);
+      push(L.split_out, L.nsplit_out, L.cap_split, make_task(task.start + g0, s, glo, ghi, nsrc != 0, false), err);
     }
   }
   __syncthreads();
@@ -1138,8 +1142,26 @@ __global__ void __launch_bounds__(kThreads, 2) k_split(HsortParams p, TaskLists 
     const SortTask task = sm.next;
     __syncthreads();
     if (t >= nt) break;
-    if (task.kind == TASK_COPY || task.count <= (uint32_t)kLocalMax) {  // forwarded as is
+    // forwarded as is (a task still in a reserved bucket region is split, so
+    // that its records move out of the region in the first round)
+    if (task.from == task.start && ((task.flags & TASK_COPY) || task.count <= (uint32_t)kLocalMax)) {
       if (threadIdx.x == 0) push(L.local, L.nlocal, L.cap_local, task, err);
+      continue;
+    }
+    if (task.from != task.start && ((task.flags & TASK_COPY) || task.count <= (uint32_t)kLocalMax)) {
+      // a small bucket or a copy piece still in its reserved region: moved
+      // out now (later rounds write scratch A at final positions, which may
+      // cover a region); a copy piece is final, a small bucket becomes a
+      // local task in scratch B
+      constexpr uint32_t E = EW * 4;
+      const bool copy = (task.flags & TASK_COPY) != 0;
+      block_copy_ilp<EW>(p.bufA + (size_t)task.from * E, (copy ? p.out : p.bufB) + (size_t)task.start * E,
+                         task.count, kThreads);
+      if (!copy && threadIdx.x == 0) {
+        __threadfence();
+        push(L.local, L.nlocal, L.cap_local, make_task(task.start, task.count, task.lo, task.hi, true, false), err);
+      }
+      __syncthreads();
       continue;
     }
     if (threadIdx.x == 0) atomicAdd(stats + STAT_SPLIT, 1u);
@@ -1175,15 +1197,15 @@ __global__ void __launch_bounds__(NT, kLocalCtasPerSm) k_local(HsortParams p, co
       if (nid < nt) {
         nxt = tasks[nid];
         // the next task's records head for L2 while this one sorts
-        const uint8_t* ns = (nxt.src ? p.bufB : p.bufA) + (size_t)nxt.start * E;
+        const uint8_t* ns = ((nxt.flags & TASK_SRC_B) ? p.bufB : p.bufA) + (size_t)nxt.from * E;
         const uint8_t* ne = ns + (size_t)nxt.count * E;
         for (const uint8_t* q = (const uint8_t*)((uintptr_t)ns & ~(uintptr_t)127); q < ne; q += 128)
           asm volatile("prefetch.global.L2 [%0];" ::"l"(q));
       }
     }
-    const uint8_t* src = (task.src ? p.bufB : p.bufA) + (size_t)task.start * E;
+    const uint8_t* src = ((task.flags & TASK_SRC_B) ? p.bufB : p.bufA) + (size_t)task.from * E;
     uint8_t* out = p.out + (size_t)task.start * E;
-    if (task.kind == TASK_COPY || task.count == 1) {
+    if ((task.flags & TASK_COPY) || task.count == 1) {
       block_copy_ilp<EW>(src, out, task.count, NT);
       if (threadIdx.x == 0) atomicAdd(stats + STAT_COPY, 1u);
       __syncthreads();
@@ -1270,7 +1292,7 @@ static cudaError_t set_smem(const void* fn, size_t bytes) {
 cudaError_t l1_count(const HsortParams& p, int lookup_kind, const uint64_t* splitters, int nbuckets,
                      const void* model, uint32_t* counts, uint32_t* stats, cudaStream_t stream, int c0, int c1) {
   const ModelDev m = model ? *(const ModelDev*)model : ModelDev{};
-  const int g = hsort_grid(p.n);
+  const int g = p.chunks ? (int)p.chunks : hsort_grid(p.n);
   if (c1 < 0) c1 = g;
   if (c1 <= c0) return cudaSuccess;
   cudaError_t e;
@@ -1290,12 +1312,18 @@ cudaError_t l1_count(const HsortParams& p, int lookup_kind, const uint64_t* spli
   return cudaGetLastError();
 }
 
-uint32_t hsort_chunk_begin(uint32_t n, int c) { return c >= hsort_grid(n) ? n : chunk_begin(n, (uint32_t)c, (uint32_t)hsort_grid(n)); }
+uint32_t hsort_chunk_begin(uint32_t n, int c, int chunks) {
+  return c >= chunks ? n : chunk_begin(n, (uint32_t)c, (uint32_t)chunks);
+}
 
 cudaError_t l1_scatter(const HsortParams& p, int lookup_kind, const uint64_t* splitters, int nbuckets,
-                       const void* model, const uint32_t* offsets, uint32_t* stats, cudaStream_t stream) {
+                       const void* model, const uint32_t* offsets, uint32_t* stats, cudaStream_t stream, int c0,
+                       int c1, const uint32_t* skip_if) {
   const ModelDev m = model ? *(const ModelDev*)model : ModelDev{};
-  const int g = hsort_grid(p.n);
+  const int g = p.chunks ? (int)p.chunks : hsort_grid(p.n);
+  if (c1 < 0) c1 = g;
+  if (c1 <= c0) return cudaSuccess;
+  const int ctas = std::min(hsort_grid(p.n), c1 - c0);
   cudaError_t e = cudaSuccess;
   bool ok = dispatch_ew(p.elsize, [&](auto ewc) {
     constexpr int EW = decltype(ewc)::value;
@@ -1303,15 +1331,17 @@ cudaError_t l1_scatter(const HsortParams& p, int lookup_kind, const uint64_t* sp
       size_t sm = l1_scatter_smem<EW, LOOKUP_LEARNED>(nbuckets, &m);
       e = set_smem((const void*)k_l1_scatter<EW, LOOKUP_LEARNED>, sm);
       if (e == cudaSuccess)
-        k_l1_scatter<EW, LOOKUP_LEARNED><<<g, kThreads, sm, stream>>>(p, splitters, nbuckets, m,
-                                                                               offsets, g, stats);
+        k_l1_scatter<EW, LOOKUP_LEARNED><<<ctas, kThreads, sm, stream>>>(p, splitters, nbuckets, m, offsets, g,
+                                                                                  stats, (uint32_t)c0, (uint32_t)c1,
+                                                                                  skip_if);
       note_launches(1);
     } else {
       size_t sm = l1_scatter_smem<EW, LOOKUP_PLAIN>(nbuckets, &m);
       e = set_smem((const void*)k_l1_scatter<EW, LOOKUP_PLAIN>, sm);
       if (e == cudaSuccess)
-        k_l1_scatter<EW, LOOKUP_PLAIN><<<g, kThreads, sm, stream>>>(p, splitters, nbuckets, m,
-                                                                             offsets, g, stats);
+        k_l1_scatter<EW, LOOKUP_PLAIN><<<ctas, kThreads, sm, stream>>>(p, splitters, nbuckets, m, offsets, g,
+                                                                                stats, (uint32_t)c0, (uint32_t)c1,
+                                                                                skip_if);
       note_launches(1);
     }
   });
@@ -1335,6 +1365,92 @@ static TaskLists lists_of(const TaskListsHost& h) {
 
 __global__ void k_require_zero(const uint32_t* count, uint32_t* err) {
   if (threadIdx.x == 0 && *count != 0) set_error(err, DEV_ERR_LEVELS);
+}
+
+// cap[b] = ceil(sample share of bucket b * n * slack) + pad.
+__global__ void k_bucket_caps(const uint64_t* __restrict__ x, uint32_t s, const uint64_t* __restrict__ S,
+                              int nbuckets, uint32_t n, float slack, uint32_t pad, uint32_t* __restrict__ cap) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbuckets) return;
+  // sample keys in [S[b-1], S[b]): lower bounds of the two splitters
+  auto lower = [&](uint64_t k) {
+    uint32_t lo = 0, hi = s;
+    while (lo < hi) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (x[mid] < k) lo = mid + 1;
+      else hi = mid;
+    }
+    return lo;
+  };
+  const uint32_t i0 = b == 0 ? 0u : lower(S[b - 1]);
+  const uint32_t i1 = b == nbuckets - 1 ? s : lower(S[b]);
+  const double est = (double)(i1 - i0) * (double)n / (double)s;
+  cap[b] = (uint32_t)min(est * (double)slack + 1.0, (double)n) + pad;
+}
+
+__global__ void k_region_offsets(uint32_t* __restrict__ counts, int chunks, int nbuckets,
+                                 const uint32_t* __restrict__ region, const uint32_t* __restrict__ cap,
+                                 uint32_t* __restrict__ total, int c0, int c1, uint32_t* overflow) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbuckets) return;
+  uint32_t run = total[b];
+  uint32_t* row = counts + (size_t)b * chunks;
+  for (int c = c0; c < c1; ++c) {
+    const uint32_t x = row[c];
+    row[c] = region[b] + run;
+    run += x;
+  }
+  total[b] = run;
+  if (run > cap[b]) atomicOr(overflow, 1u);
+}
+
+__global__ void k_build_region_tasks(const uint32_t* __restrict__ region, const uint32_t* __restrict__ total,
+                                     const uint32_t* __restrict__ out_start, const uint64_t* __restrict__ S,
+                                     int nbuckets, TaskLists L, uint32_t* err, uint32_t* stats, int b0, int b1) {
+  const int b = b0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= b1) return;
+  const uint32_t cnt = total[b];
+  if (cnt == 0) return;
+  atomicMax(stats + STAT_MAX_BUCKET, cnt);
+  const uint64_t lo = b == 0 ? 0ull : S[b - 1];
+  const uint64_t hi = b == nbuckets - 1 ? ~0ull : S[b] - 1;
+  if (lo == hi || cnt == 1) {  // copy pieces, each moved by one CTA of the first split round
+    for (uint32_t s0 = 0; s0 < cnt; s0 += kCopyPiece) {
+      SortTask t = make_task(out_start[b] + s0, min(kCopyPiece, cnt - s0), lo, hi, false, true);
+      t.from = region[b] + s0;
+      push(L.split_out, L.nsplit_out, L.cap_split, t, err);
+    }
+  } else {
+    SortTask t = make_task(out_start[b], cnt, lo, hi, false, false);
+    t.from = region[b];
+    push(L.split_out, L.nsplit_out, L.cap_split, t, err);
+  }
+}
+
+cudaError_t bucket_caps(const uint64_t* sorted_sample, uint32_t s, const uint64_t* splitters, int nbuckets,
+                        uint32_t n, float slack, uint32_t pad, uint32_t* cap, cudaStream_t stream) {
+  k_bucket_caps<<<(nbuckets + 255) / 256, 256, 0, stream>>>(sorted_sample, s, splitters, nbuckets, n, slack, pad, cap);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t region_offsets(uint32_t* counts, int chunks, int nbuckets, const uint32_t* region, const uint32_t* cap,
+                           uint32_t* total, int c0, int c1, uint32_t* overflow, cudaStream_t stream) {
+  k_region_offsets<<<(nbuckets + 127) / 128, 128, 0, stream>>>(counts, chunks, nbuckets, region, cap, total, c0, c1,
+                                                               overflow);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t build_region_tasks(const uint32_t* region, const uint32_t* total, const uint32_t* out_start,
+                               const uint64_t* splitters, int nbuckets, const TaskListsHost& lists, uint32_t* err,
+                               uint32_t* stats, cudaStream_t stream, int b0, int b1) {
+  if (b1 <= b0) return cudaSuccess;
+  k_build_region_tasks<<<(b1 - b0 + 255) / 256, 256, 0, stream>>>(region, total, out_start, splitters, nbuckets,
+                                                                  lists_of(lists), err, stats, b0, b1);
+  k_order_tasks<<<1, 1024, 0, stream>>>(lists.split_out, lists.nsplit_out);
+  note_launches(2);
+  return cudaGetLastError();
 }
 
 cudaError_t require_zero(const uint32_t* count, uint32_t* err, cudaStream_t stream) {

@@ -70,13 +70,21 @@ enum StatSlot : int {
 enum Lookup : int { LOOKUP_PLAIN = 0, LOOKUP_LEARNED = 1 };
 
 struct SortTask {        // one bucket or sub-bucket of the level-2 task engine
-  uint32_t start;        // first record (same index in every buffer)
+  uint32_t start;        // first record in the destination buffers (the other scratch buffer, the output)
   uint32_t count;        // records
   uint64_t lo, hi;       // key range [lo, hi] of the records
-  uint32_t src;          // 0: scratch A, 1: scratch B
-  uint32_t kind;         // TASK_* below
+  uint32_t from;         // first record in the source buffer: start, except for the level-1
+                         // buckets of a scatter into reserved (gapped) bucket regions
+  uint32_t flags;        // TASK_* below
 };
-enum TaskKind : uint32_t { TASK_SORT = 0, TASK_COPY = 1 };
+enum TaskFlags : uint32_t {
+  TASK_SRC_B = 1,  // the records are in scratch B (else scratch A)
+  TASK_COPY = 2,   // one key: copied, not sorted
+};
+__host__ __device__ inline SortTask make_task(uint32_t start, uint32_t count, uint64_t lo, uint64_t hi, bool in_b,
+                                              bool copy) {
+  return SortTask{start, count, lo, hi, start, (in_b ? (uint32_t)TASK_SRC_B : 0u) | (copy ? (uint32_t)TASK_COPY : 0u)};
+}
 
 struct HsortParams {
   const uint8_t* in;
@@ -86,6 +94,8 @@ struct HsortParams {
   uint32_t n;
   uint32_t elsize;
   gbsort_key_word key;
+  uint32_t a_cap;      // records scratch A holds (n, or more for reserved bucket regions)
+  uint32_t chunks;     // count chunks of the input (0: hsort_grid(n))
 };
 
 bool hsort_supported(uint32_t elsize);
@@ -102,14 +112,27 @@ cudaError_t finalize_splitters(uint64_t* splitters, int nsplit, cudaStream_t str
 // Level-1 bucket counts per chunk ([nbuckets][grid]) and the stable scatter.
 // `model` points to a host copy of the ModelDev (cdf.cuh) for the learned
 // lookup, else null.  `stats` is the device statistics array (Stat indices).
-// l1_count counts chunks [c0, c1) of the hsort_grid(n) chunks (c1 < 0: all).
+// The input is cut into p.chunks count chunks (hsort_grid(n) when 0);
+// l1_count counts chunks [c0, c1) (c1 < 0: all) into counts[bucket][chunk].
 cudaError_t l1_count(const HsortParams& p, int lookup, const uint64_t* splitters, int nbuckets,
                      const void* model, uint32_t* counts, uint32_t* stats, cudaStream_t stream, int c0 = 0,
                      int c1 = -1);
-// First record of count chunk c (n for c >= hsort_grid(n)).
-uint32_t hsort_chunk_begin(uint32_t n, int c);
+// First record of chunk c of `chunks` (n for c >= chunks).
+uint32_t hsort_chunk_begin(uint32_t n, int c, int chunks);
+// Reserved bucket regions from the sorted sample: cap[b] = the bucket's
+// estimated size times slack (plus pad); the caller scans cap into starts.
+cudaError_t bucket_caps(const uint64_t* sorted_sample, uint32_t s, const uint64_t* splitters, int nbuckets,
+                        uint32_t n, float slack, uint32_t pad, uint32_t* cap, cudaStream_t stream);
+// Scatter offsets of chunks [c0, c1) into reserved regions: counts of those
+// chunks become region start + the bucket's running total (kept in total[]);
+// *overflow is set if a bucket outgrows its region.
+cudaError_t region_offsets(uint32_t* counts, int chunks, int nbuckets, const uint32_t* region, const uint32_t* cap,
+                           uint32_t* total, int c0, int c1, uint32_t* overflow, cudaStream_t stream);
+// Scatter of chunks [c0, c1) (c1 < 0: all) to offsets[bucket][chunk]; does
+// nothing if *skip_if is set (a region overflow).
 cudaError_t l1_scatter(const HsortParams& p, int lookup, const uint64_t* splitters, int nbuckets,
-                       const void* model, const uint32_t* offsets, uint32_t* stats, cudaStream_t stream);
+                       const void* model, const uint32_t* offsets, uint32_t* stats, cudaStream_t stream,
+                       int c0 = 0, int c1 = -1, const uint32_t* skip_if = nullptr);
 // Level-2 task lists (device memory).  A split round consumes split_in and
 // appends to split_out and local; build_tasks appends to split_out and local.
 struct TaskListsHost {
@@ -126,6 +149,12 @@ struct TaskListsHost {
 cudaError_t build_tasks(const uint32_t* offsets, int grid, const uint64_t* splitters, int nbuckets,
                         uint32_t n, const TaskListsHost& lists, uint32_t* err, uint32_t* stats,
                         cudaStream_t stream, int b0 = 0, int b1 = -1);
+// Tasks of buckets [b0, b1) that still lie in their reserved regions: the
+// bucket at region[b], `total[b]` records, going to out_start[b]; every one
+// goes to the split list (single-key buckets in copy pieces).
+cudaError_t build_region_tasks(const uint32_t* region, const uint32_t* total, const uint32_t* out_start,
+                               const uint64_t* splitters, int nbuckets, const TaskListsHost& lists, uint32_t* err,
+                               uint32_t* stats, cudaStream_t stream, int b0, int b1);
 // err gets DEV_ERR_LEVELS unless *count is zero.
 cudaError_t require_zero(const uint32_t* count, uint32_t* err, cudaStream_t stream);
 cudaError_t run_split_round(const HsortParams& p, const TaskListsHost& lists, uint32_t* work_counter,

@@ -164,6 +164,7 @@ extern "C" GBSORT_API int gbsort_sort_device_noalloc(const void* d_in, void* d_o
   p.n = n;
   p.elsize = E;
   p.key = key->word[0];
+  p.a_cap = n;
 
   if (nb > 1) {
     NA_CUDA(sample_keys(p.in, n, E, p.key, s_eff, sA, st));

@@ -63,12 +63,12 @@ __global__ void __launch_bounds__(kThreads) k_segment_ranges(const uint8_t* __re
         else
           for (uint32_t i = 0; i < pieces; ++i) {
             uint32_t s0 = i * kCopyPieceSeg;
-            tasks[at + i] = SortTask{(uint32_t)a + s0, min(kCopyPieceSeg, cnt - s0), mn, mx, 0u, TASK_COPY};
+            tasks[at + i] = make_task((uint32_t)a + s0, min(kCopyPieceSeg, cnt - s0), mn, mx, false, true);
           }
       } else {
         uint32_t at = atomicAdd(ntasks, 1u);
         if (at >= cap) set_error(err, DEV_ERR_TASK_OVERFLOW);
-        else tasks[at] = SortTask{(uint32_t)a, cnt, mn, mx, 0u, TASK_SORT};
+        else tasks[at] = make_task((uint32_t)a, cnt, mn, mx, false, false);
       }
     }
     __syncthreads();

@@ -548,13 +548,18 @@ def test_autotune_feeds_auto(mp, given):
 
 
 # ------------------------------------------------- pipelined host sorts --
+@pytest.mark.parametrize("regions", [True, False])
 @pytest.mark.parametrize("method", ["auto", "plain", "learned"])
 @pytest.mark.parametrize("dist", ["uniform", "zipf", "equal", "sorted"])
-def test_host_sort_pipelined_pinned(mp, method, dist):
+def test_host_sort_pipelined_pinned(mp, method, dist, regions, monkeypatch):
     """Pinned host arrays of 2^22 records or more take the pipelined host
-    sort (pieces up while counting, waves down while sorting); the result is
-    the same stable order, out of place and in place."""
+    sort (pieces scattered into reserved bucket regions as they land, waves
+    down while sorting; or, without regions, the exact level 1 the sort
+    falls back to when a region overflows); the result is the same stable
+    order, out of place and in place."""
     import torch
+    if not regions:
+        monkeypatch.setenv("GBSORT_NO_REGIONS", "1")
     rng = numpy.random.default_rng(51)
     dt = numpy.dtype([('key', 'u8'), ('val', 'i8')])
     n = 5_000_000
