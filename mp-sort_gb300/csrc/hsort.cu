@@ -710,8 +710,7 @@ struct LocalSmemT {
   uint64_t keyB[kLocalMax];  // keys in sorted order
   uint16_t idxA[kLocalMax];
   uint16_t idxB[kLocalMax];
-  uint32_t cnt[1 << kLocalBits];          // bin counts, then bin cursors
-  uint32_t start[(1 << kLocalBits) + 1];
+  uint32_t cnt[(1 << kLocalBits) + 1];    // bin counts, then (scanned in place) bin starts and the end
   uint16_t big[kLocalMax / (kInsertMax + 1) + 2];  // start of pending bins
   uint16_t bigsz[kLocalMax / (kInsertMax + 1) + 2];
   uint32_t nbig;
@@ -803,17 +802,17 @@ __device__ __noinline__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint
     uint32_t pre = block_exclusive_scan<uint32_t, NT>(sum, sm.scan_tmp, nullptr);
 #pragma unroll
     for (int i = 0; i < BPT; ++i) {
-      sm.start[threadIdx.x * BPT + i] = pre;
+      sm.cnt[threadIdx.x * BPT + i] = pre;
       pre += loc[i];
     }
-    if (threadIdx.x == NT - 1) sm.start[kBins] = pre;
+    if (threadIdx.x == NT - 1) sm.cnt[kBins] = pre;
   }
   __syncthreads();
 #pragma unroll
   for (int r = 0; r < PER; ++r) {
     const uint32_t e = r * NT + threadIdx.x;
     if (e < s) {
-      const uint32_t pos = sm.start[bin[r]] + slot[r];
+      const uint32_t pos = sm.cnt[bin[r]] + slot[r];
       sm.keyB[a + pos] = sm.keyA[a + e];
       if (!PACKED) sm.idxB[a + pos] = sm.idxA[a + e];
     }
@@ -823,7 +822,7 @@ __device__ __noinline__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint
     const uint64_t kv = sm.keyB[a + i];
     const uint16_t iv = PACKED ? 0 : sm.idxB[a + i];
     const uint32_t d = !PACKED && by_idx ? (uint32_t)iv : (uint32_t)((kv - mn) >> shift);
-    const uint32_t b0 = sm.start[d], b1 = sm.start[d + 1];
+    const uint32_t b0 = sm.cnt[d], b1 = sm.cnt[d + 1];
     const uint32_t sz = b1 - b0;
     uint32_t at = i;
     if (sz <= (uint32_t)kInsertMax) {
