@@ -1079,6 +1079,10 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
       if (grp[r] == kNoBucket) continue;
       uint32_t all;
       const uint32_t slot = sm.goff[grp[r]] + tile_rank(grp[r], rank[r], sm.gcnt, all);
+      if (slot >= nvalid) {  // impossible with consistent ranks; never write past the tile
+        set_error(err, DEV_ERR_COUNT_MISMATCH);
+        continue;
+      }
       RecIO<EW>::store(sm.stage + (size_t)slot * E, rec[r]);
       sm.sgrp[slot] = (uint16_t)grp[r];
     }
