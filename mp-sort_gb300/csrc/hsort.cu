@@ -901,15 +901,13 @@ __device__ void local_sort(LocalSmemT<NT>& sm, const uint8_t* src, uint8_t* dst,
     uint32_t e = w * 32 * kLocalRpt + r * 32 + lane;
     if (e < m) {
       sm.keyA[e] = packed ? ((k[r] - mn) << kLocalBits) | e : k[r];
-      sm.idxA[e] = (uint16_t)e;
+      if (!packed) sm.idxA[e] = (uint16_t)e;
     }
   }
   __syncthreads();
-  if (packed) {
+  if (packed) {  // the input index of each sorted record is the low bits of its key word
     local_msd_pass<NT, true>(sm, 0, m, 0, ((mx - mn) << kLocalBits) | (kLocalMax - 1), false);
     local_big_bins<NT, true>(sm, stats);
-    for (uint32_t i = threadIdx.x; i < m; i += NT) sm.idxA[i] = (uint16_t)(sm.keyA[i] & (kLocalMax - 1));
-    __syncthreads();
   } else {
     local_msd_pass<NT, false>(sm, 0, m, mn, mx, false);
     local_big_bins<NT, false>(sm, stats);
@@ -926,7 +924,11 @@ __device__ void local_sort(LocalSmemT<NT>& sm, const uint8_t* src, uint8_t* dst,
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         uint32_t f = f0 + u * NT;
-        if (f < nv) v[u] = reinterpret_cast<const V*>(src + (size_t)sm.idxA[f / VPR] * E)[f % VPR];
+        if (f < nv) {
+          const uint32_t i = f / VPR;
+          const uint32_t from = packed ? (uint32_t)(sm.keyA[i] & (kLocalMax - 1)) : sm.idxA[i];
+          v[u] = reinterpret_cast<const V*>(src + (size_t)from * E)[f % VPR];
+        }
       }
 #pragma unroll
       for (int u = 0; u < U; ++u) {
