@@ -207,6 +207,25 @@ def run_ours(args):
         torch.cuda.synchronize()
         plain_rps = n / (p0.elapsed_time(p1) / max(1, args.steps // 2) / 1e3)
 
+    # orientation: the library sort of the same records with torch (a stable
+    # key sort, CUB's radix sort underneath, then the record gather by index)
+    torch_rps = None
+    if not args.no_compare and world == 1:
+        def torch_step():
+            k = rec[:, 0] ^ (-2**63)  # uint64 order as int64
+            _, idx = torch.sort(k, stable=True)
+            torch.index_select(rec, 0, idx, out=out)
+        torch_step()
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(max(1, args.steps // 2)):
+            torch_step()
+        t1.record(stream)
+        torch.cuda.synchronize()
+        torch_rps = n / (t0.elapsed_time(t1) / max(1, args.steps // 2) / 1e3)
+
     st = stats_steps[-1]
     stage_ms = {k: round(sum(s["stage_ms"][k] for s in stats_steps) / len(stats_steps), 4)
                 for k in st["stage_ms"]}
@@ -263,6 +282,8 @@ def run_ours(args):
         "gpu_launches": launches * args.steps if launches else None,
         "learned_vs_plain": {"learned_records_per_s": value / world if args.method == "learned" else None,
                              "plain_records_per_s": plain_rps},
+        "orientation": {"torch_sort_records_per_s": torch_rps,
+                        "what": "torch.sort(keys, stable=True) + index_select of the records, same GPU"},
         "stage_ms": stage_ms,
         "sort_stats": {k: v for k, v in st.items() if k != "stage_ms"},
         "parity": {"sorted": ok_sorted, "permutation": ok_perm, "stable": ok_stable},
@@ -303,6 +324,23 @@ def cpu_baseline(args, seconds=None):
         t = ts[1]
     return {"value": n / t, "unit": UNIT, "cores": threads, "kind": kind,
             "sample": "%d records of the same 16 B layout, median of 3 sorts" % n}
+
+
+def cpu_sort_seconds(a, orderby, repeat=3):
+    """Median wall time of the CPU port of mpsort_omp (or the reference
+    build, where present) sorting array a on all host cores."""
+    import oracle as O
+    threads = os.cpu_count() or 1
+    if O.ref_lib() is not None:
+        O.set_ref_threads(threads)
+        return O.time_ref_sort(a, orderby, 'omp', repeat=repeat), "reference", threads
+    ts = []
+    for _ in range(repeat):
+        t0 = time.perf_counter()
+        O.oracle_mpsort(a, orderby, threads)
+        ts.append(time.perf_counter() - t0)
+    ts.sort()
+    return ts[len(ts) // 2], "port", threads
 
 
 def _u64(t):
@@ -350,6 +388,10 @@ def run_config(args):
         exp = ref if ref is not None else O.numpy_sorted(arr, 'key')
         res.update(value=res["learned_records_per_s"], n=n,
                    parity={"equals_reference" if ref is not None else "equals_stable_sort": got.tobytes() == exp.tobytes()})
+        if not args.no_cpu:
+            t, kind, cores = cpu_sort_seconds(arr, 'key')
+            res["cpu_baseline"] = {"value": n / t, "unit": UNIT, "cores": cores, "kind": kind,
+                                   "sample": "the whole workload, median of 3 sorts"}
     elif args.config == "3":
         buf, dt, offs = W.segments_3(torch)
         out = torch.empty_like(buf)
@@ -373,6 +415,18 @@ def run_config(args):
         seg_of_pos = torch.cumsum(seg_start.to(torch.int64), 0)
         ok_perm = bool((torch.bincount(pay, minlength=n) == 1).all().item()) and \
             bool((seg_of_pos[pay] == seg_of_pos).all().item())
+        if not args.no_cpu:
+            host = buf.cpu().numpy().view(dt)
+            k = int(numpy.searchsorted(offs, 2_000_000))
+            k = max(1, min(k, len(offs) - 1))
+            t = 0.0
+            for i in range(k):
+                a, b = int(offs[i]), int(offs[i + 1])
+                if b > a:
+                    t += cpu_sort_seconds(host[a:b].copy(), 'key', repeat=1)[0]
+            kind, cores = cpu_sort_seconds(host[:16].copy(), 'key', repeat=1)[1:]
+            res["cpu_baseline"] = {"value": int(offs[k]) / t, "unit": UNIT, "cores": cores, "kind": kind,
+                                   "sample": "the first %d arrays (%d records), one CPU sort per array" % (k, int(offs[k]))}
         res.update(value=n / (ms / 1e3), n=n, nseg=len(offs) - 1, ms_per_step=ms,
                    per_array_loop_records_per_s=n / (ms_loop / 1e3), per_array_loop_ms=ms_loop,
                    parity={"sorted": ok_sorted, "stable": ok_stable, "permutation": ok_perm},
@@ -396,6 +450,12 @@ def run_config(args):
         ok_stable = bool(((key[1:] != key[:-1]) | (ident[1:] > ident[:-1])).all().item())
         res.update(value=res["learned"]["records_per_s"], n=n,
                    parity={"sorted": ok_sorted, "permutation": ok_perm, "stable": ok_stable})
+        if not args.no_cpu:
+            m = min(n, 2_000_000)
+            sample = buf[:m * dt.itemsize].cpu().numpy().view(dt).copy()
+            t, kind, cores = cpu_sort_seconds(sample, 'key')
+            res["cpu_baseline"] = {"value": m / t, "unit": UNIT, "cores": cores, "kind": kind,
+                                   "sample": "the first %d records of the workload, median of 3 sorts" % m}
     elif args.config == "5":
         buf, dt, na, nb, common = W.snapshots_5(torch)
         out = torch.empty_like(buf)
@@ -417,6 +477,19 @@ def run_config(args):
         ok_sorted = bool((ida[1:] > ida[:-1]).all().item()) and bool((idb[1:] > idb[:-1]).all().item())
         res.update(value=(na + nb) / (ms / 1e3), n=na + nb, ms_per_step=ms, pairs=k, expected_pairs=common,
                    parity={"pairs": ok_pairs, "sorted_unique": ok_sorted})
+        if not args.no_cpu:
+            m = 1_000_000
+            host = buf.cpu().numpy().view(dt)
+            sa, sb = host[:m].copy(), host[na:na + m].copy()
+            ta, kind, cores = cpu_sort_seconds(sa, 'id', repeat=1)
+            tb = cpu_sort_seconds(sb, 'id', repeat=1)[0]
+            import oracle as O
+            ssa, ssb = O.numpy_sorted(sa, 'id'), O.numpy_sorted(sb, 'id')
+            t0 = time.perf_counter()
+            numpy.intersect1d(ssa['id'], ssb['id'], assume_unique=True, return_indices=True)
+            tj = time.perf_counter() - t0
+            res["cpu_baseline"] = {"value": 2 * m / (ta + tb + tj), "unit": UNIT, "cores": cores, "kind": kind,
+                                   "sample": "1e6 records of each snapshot: two CPU sorts + numpy.intersect1d"}
     line = {"metric": "sorted records/s, configuration " + args.config, "unit": UNIT, "n_gpus": 1,
             "higher_is_better": True, "data": "synthetic (workloads.py, seeded)"}
     line.update(res)
