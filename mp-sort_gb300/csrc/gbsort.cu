@@ -844,6 +844,13 @@ int gbsort_sort_device(const void* d_in, void* d_out, size_t nmemb, size_t elsiz
 
 namespace {
 constexpr size_t kPipelineMin = (size_t)1 << 22;  // records; smaller host sorts copy in one piece each way
+// An integer setting from the environment, within [lo, hi], else dflt.
+int env_int(const char* name, int dflt, int lo, int hi) {
+  const char* e = getenv(name);
+  if (!e) return dflt;
+  const int v = atoi(e);
+  return v >= lo && v <= hi ? v : dflt;
+}
 bool is_pinned(const void* p) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
@@ -878,7 +885,9 @@ int gbsort_sort_host(const void* in, void* out, size_t nmemb, size_t elsize, con
     Knobs knobs;
     int m = method == GBSORT_AUTO ? resolve_auto(E, key, n, hs_ok, &knobs) : method;
     if (hs_ok && (m == GBSORT_HISTOGRAM_PLAIN || m == GBSORT_HISTOGRAM_LEARNED)) {
-      HostPipe hp{(const uint8_t*)in, (uint8_t*)out, 8, 8};
+      static const int pieces = env_int("GBSORT_PIPE_PIECES", 16, 1, kMaxPieces);
+      static const int waves = env_int("GBSORT_PIPE_WAVES", 16, 1, kMaxWaves);
+      HostPipe hp{(const uint8_t*)in, (uint8_t*)out, pieces, waves};
       const unsigned long long l0 = launch_count();
       rc = hsort_enqueue(*c, c->hin.p, c->hout.p, n, E, key, m == GBSORT_HISTOGRAM_LEARNED, false, knobs, c->stream,
                          &hp);
