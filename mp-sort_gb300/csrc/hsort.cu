@@ -39,6 +39,13 @@ namespace {
 constexpr int kLocalMax = GB_LOCAL_MAX;          // records a local sort holds in shared memory
 constexpr int kLocalThreads = GB_LOCAL_THREADS;  // threads of a local-sort CTA
 constexpr int kLocalCtasPerSm = GB_LOCAL_CTAS;
+// Records above 16 bytes: one CTA fewer per SM, which leaves L1 room for the
+// gather's reads of the group (measured: 40-byte records 13.1 ms with three,
+// 18.4 ms with four CTAs per SM on 5e8 records).
+template <int EW>
+constexpr int local_ctas_per_sm() {
+  return EW > 4 && kLocalCtasPerSm > 1 ? kLocalCtasPerSm - 1 : kLocalCtasPerSm;
+}
 constexpr int kLocalBits = 11;         // bins of the local counting pass (about one record each)
 constexpr int kInsertMax = 24;         // bins up to this size use insertion sort
 constexpr int kSplitBits = 12;         // bins of a bucket split
@@ -390,7 +397,11 @@ struct Tile {
 // Tile of the level-1 scatter: up to GB_SCATTER_RPT / EW records per thread.
 template <int EW>
 struct ScatterTile {
-  static constexpr int kRpt = (GB_SCATTER_RPT / EW) < 1 ? 1 : ((GB_SCATTER_RPT / EW) > 7 ? 7 : (GB_SCATTER_RPT / EW));
+  // records of 24-40 bytes: two per thread (a tile of 1024; the staged tile
+  // still leaves room for two CTAs per SM)
+  static constexpr int kRpt = (EW >= 6 && EW <= 10) ? 2
+                              : (GB_SCATTER_RPT / EW) < 1 ? 1
+                              : ((GB_SCATTER_RPT / EW) > 7 ? 7 : (GB_SCATTER_RPT / EW));
   static constexpr int kSize = kThreads * kRpt;
   static constexpr bool kPrefetch = GB_SCATTER_PREFETCH != 0;
 };
@@ -905,18 +916,25 @@ __device__ void local_sort(LocalSmemT<NT>& sm, const uint8_t* src, uint8_t* dst,
     }
   }
   __syncthreads();
-  if (packed) {  // the input index of each sorted record is the low bits of its key word
+  using V = typename std::conditional<EW % 4 == 0, uint4,
+                                      typename std::conditional<EW % 2 == 0, uint2, uint32_t>::type>::type;
+  constexpr int VPR = E / sizeof(V);
+  // the input index of each sorted record is the low bits of its key word;
+  // records of several vectors read it once into idxA
+  const bool idx_in_key = packed && VPR == 1;
+  if (packed) {
     local_msd_pass<NT, true>(sm, 0, m, 0, ((mx - mn) << kLocalBits) | (kLocalMax - 1), false);
     local_big_bins<NT, true>(sm, stats);
+    if (!idx_in_key) {
+      for (uint32_t i = threadIdx.x; i < m; i += NT) sm.idxA[i] = (uint16_t)(sm.keyA[i] & (kLocalMax - 1));
+      __syncthreads();
+    }
   } else {
     local_msd_pass<NT, false>(sm, 0, m, mn, mx, false);
     local_big_bins<NT, false>(sm, stats);
   }
   // gather the records into dst in sorted order, four loads in flight
   {
-    using V = typename std::conditional<EW % 4 == 0, uint4,
-                                        typename std::conditional<EW % 2 == 0, uint2, uint32_t>::type>::type;
-    constexpr int VPR = E / sizeof(V);
     constexpr int U = sizeof(V) >= 16 ? 2 : 4;
     const uint32_t nv = m * VPR;
     for (uint32_t f0 = threadIdx.x; f0 < nv; f0 += NT * U) {
@@ -926,7 +944,7 @@ __device__ void local_sort(LocalSmemT<NT>& sm, const uint8_t* src, uint8_t* dst,
         uint32_t f = f0 + u * NT;
         if (f < nv) {
           const uint32_t i = f / VPR;
-          const uint32_t from = packed ? (uint32_t)(sm.keyA[i] & (kLocalMax - 1)) : sm.idxA[i];
+          const uint32_t from = idx_in_key ? (uint32_t)(sm.keyA[i] & (kLocalMax - 1)) : sm.idxA[i];
           v[u] = reinterpret_cast<const V*>(src + (size_t)from * E)[f % VPR];
         }
       }
@@ -1175,7 +1193,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split(HsortParams p, TaskLists 
 }
 
 template <int EW, int NT = kLocalThreads>
-__global__ void __launch_bounds__(NT, kLocalCtasPerSm) k_local(HsortParams p, const SortTask* __restrict__ tasks,
+__global__ void __launch_bounds__(NT, local_ctas_per_sm<EW>()) k_local(HsortParams p, const SortTask* __restrict__ tasks,
                                                         const uint32_t* __restrict__ ntasks, uint32_t cap,
                                                         uint32_t* __restrict__ work, uint32_t* __restrict__ stats) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
@@ -1197,14 +1215,23 @@ __global__ void __launch_bounds__(NT, kLocalCtasPerSm) k_local(HsortParams p, co
     __syncthreads();
     uint32_t nid = 0;
     SortTask nxt{};
-    if (threadIdx.x == 0) {
-      nid = atomicAdd(work, 1u);
-      if (nid < nt) {
-        nxt = tasks[nid];
-        // the next task's records head for L2 while this one sorts
-        const uint8_t* ns = ((nxt.flags & TASK_SRC_B) ? p.bufB : p.bufA) + (size_t)nxt.from * E;
-        const uint8_t* ne = ns + (size_t)nxt.count * E;
-        for (const uint8_t* q = (const uint8_t*)((uintptr_t)ns & ~(uintptr_t)127); q < ne; q += 128)
+    if (warp_id() == 0) {
+      const uint32_t lane = lane_id();
+      if (lane == 0) {
+        nid = atomicAdd(work, 1u);
+        if (nid < nt) nxt = tasks[nid];
+      }
+      // the next task's records head for L2 while this one sorts; the
+      // warp's lanes share the lines
+      const uint32_t id = __shfl_sync(GB_FULL_MASK, nid, 0);
+      if (id < nt) {
+        const uint32_t from = __shfl_sync(GB_FULL_MASK, nxt.from, 0);
+        const uint32_t cnt = __shfl_sync(GB_FULL_MASK, nxt.count, 0);
+        const uint32_t flags = __shfl_sync(GB_FULL_MASK, nxt.flags, 0);
+        const uint8_t* ns = ((flags & TASK_SRC_B) ? p.bufB : p.bufA) + (size_t)from * E;
+        const uint8_t* ne = ns + (size_t)cnt * E;
+        for (const uint8_t* q = (const uint8_t*)((uintptr_t)ns & ~(uintptr_t)127) + 128 * lane; q < ne;
+             q += 128 * 32)
           asm volatile("prefetch.global.L2 [%0];" ::"l"(q));
       }
     }
@@ -1477,7 +1504,8 @@ cudaError_t build_tasks(const uint32_t* offsets, int grid, const uint64_t* split
 }
 
 int split_grid() { return num_sms() * 2; }
-int local_grid() { return num_sms() * kLocalCtasPerSm; }
+template <int EW>
+int local_grid() { return num_sms() * local_ctas_per_sm<EW>(); }
 
 cudaError_t run_split_round(const HsortParams& p, const TaskListsHost& lists, uint32_t* work_counter,
                             uint32_t* stats, uint32_t* err, cudaStream_t stream) {
@@ -1505,7 +1533,7 @@ cudaError_t run_local(const HsortParams& p, const SortTask* tasks, const uint32_
     size_t sm = sizeof(LocalSmemT<kLocalThreads>);
     e = set_smem((const void*)k_local<EW>, sm);
     if (e == cudaSuccess)
-      k_local<EW><<<local_grid(), kLocalThreads, sm, stream>>>(p, tasks, ntasks, cap, work_counter, stats);
+      k_local<EW><<<local_grid<EW>(), kLocalThreads, sm, stream>>>(p, tasks, ntasks, cap, work_counter, stats);
     note_launches(1);
   });
   if (!ok) return cudaErrorInvalidValue;
