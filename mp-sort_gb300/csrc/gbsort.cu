@@ -261,8 +261,8 @@ int lsd_sort_keys(Bump& bump, uint64_t* keys, uint64_t* keys2, uint32_t* idx, ui
                   int nwords, bool skip_trivial, int* passes_out, uint32_t* err, cudaStream_t st) {
   uint32_t* hist = bump.take<uint32_t>((size_t)8 * 256 * nwords);
   uint32_t* starts = bump.take<uint32_t>((size_t)8 * 256 * nwords);
-  unsigned long long* status = bump.take<unsigned long long>((size_t)lsd_tiles(n) * 256);
-  uint32_t* ticket = bump.take<uint32_t>(1);
+  unsigned long long* status = bump.take<unsigned long long>((size_t)lsd_tiles(n) * 256 + 1);
+  uint32_t* ticket = reinterpret_cast<uint32_t*>(status + (size_t)lsd_tiles(n) * 256);  // cleared with the status
   GB_CUDA(lsd_digit_histograms(keys, n, nwords, hist, st));
   GB_CUDA(lsd_digit_starts(hist, nwords, starts, st));
   std::vector<int> pass_word, pass_shift;
@@ -349,7 +349,8 @@ int lsd_collect(Context& c) {
 
 int run_lsd(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize, const gbsort_key_desc* key,
             const uint8_t* d_radix, uint32_t rsize, cudaStream_t st) {
-  int rc = lsd_enqueue(c, d_in, d_out, n, elsize, key, d_radix, rsize, true, st);
+  // the constant-digit check costs a host round trip: worth it for large sorts only
+  int rc = lsd_enqueue(c, d_in, d_out, n, elsize, key, d_radix, rsize, n >= (1u << 22), st);
   if (rc) return rc;
   GB_CUDA(cudaStreamSynchronize(st));
   return lsd_collect(c);

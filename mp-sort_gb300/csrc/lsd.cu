@@ -293,8 +293,14 @@ cudaError_t lsd_onesweep(const uint64_t* keys_in, const uint32_t* idx_in, uint64
                          uint32_t n, int nwords, int word, int shift, const uint32_t* starts,
                          unsigned long long* status, uint32_t* ticket, uint32_t* err, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
-  cudaError_t e = cudaMemsetAsync(status, 0, sizeof(unsigned long long) * 256 * (size_t)lsd_tiles(n), stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(ticket, 0, sizeof(uint32_t), stream);
+  const size_t words = (size_t)256 * lsd_tiles(n);
+  cudaError_t e;
+  if ((void*)ticket == (void*)(status + words)) {  // the usual layout: one clear for both
+    e = cudaMemsetAsync(status, 0, sizeof(unsigned long long) * words + sizeof(uint32_t), stream);
+  } else {
+    e = cudaMemsetAsync(status, 0, sizeof(unsigned long long) * words, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ticket, 0, sizeof(uint32_t), stream);
+  }
   if (e != cudaSuccess) return e;
 #define GB_LSD_CASE(NWV)                                                                                       \
   case NWV:                                                                                                    \

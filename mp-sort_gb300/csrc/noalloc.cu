@@ -141,8 +141,8 @@ extern "C" GBSORT_API int gbsort_sort_device_noalloc(const void* d_in, void* d_o
   uint64_t* sB = cv.take<uint64_t>(s_eff);
   uint32_t* shist = cv.take<uint32_t>(8 * 256);
   uint32_t* sstarts = cv.take<uint32_t>(8 * 256);
-  unsigned long long* sstatus = cv.take<unsigned long long>((size_t)lsd_tiles(s_eff > 0 ? s_eff : 1) * 256);
-  uint32_t* sticket = cv.take<uint32_t>(1);
+  unsigned long long* sstatus = cv.take<unsigned long long>((size_t)lsd_tiles(s_eff > 0 ? s_eff : 1) * 256 + 1);
+  uint32_t* sticket = reinterpret_cast<uint32_t*>(sstatus + (size_t)lsd_tiles(s_eff > 0 ? s_eff : 1) * 256);
   if (!cv.ok()) {
     fprintf(stderr, "gbsort_sort_device_noalloc: scratch layout exceeds the static array\n");
     return GBSORT_ERR_BAD_ARG;
