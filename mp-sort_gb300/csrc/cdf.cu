@@ -325,11 +325,11 @@ __global__ void k_quantile_splitters(const uint64_t* __restrict__ x, uint32_t s,
   S[i] = x[c > 0 ? c - 1 : 0];
 }
 
-// Judge of a splitter set on the sorted sample: every key with a bucket's
+// Check of a splitter set on the sorted sample: every key with a bucket's
 // worth of sample copies must own a single-key bucket [k, k+1), and no
 // other bucket may hold more than `limit` sample keys.  flags[0] != 0 means
 // rejected; counts (nbuckets) must start at zero.
-__global__ void k_judge_count(const uint64_t* __restrict__ x, uint32_t s, const uint64_t* __restrict__ S, int nbuckets,
+__global__ void k_vet_count(const uint64_t* __restrict__ x, uint32_t s, const uint64_t* __restrict__ S, int nbuckets,
                               uint32_t* __restrict__ counts, uint32_t* __restrict__ flags) {
   const uint32_t need = (s + nbuckets - 1) / nbuckets;
   const uint32_t nsplit = (uint32_t)(nbuckets - 1);
@@ -343,7 +343,7 @@ __global__ void k_judge_count(const uint64_t* __restrict__ x, uint32_t s, const 
   }
 }
 
-__global__ void k_judge_max(const uint32_t* __restrict__ counts, int nbuckets, uint32_t limit, uint32_t* __restrict__ flags) {
+__global__ void k_vet_max(const uint32_t* __restrict__ counts, int nbuckets, uint32_t limit, uint32_t* __restrict__ flags) {
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbuckets; b += gridDim.x * blockDim.x)
     if (counts[b] > limit) atomicOr(flags, 2u);
 }
@@ -456,7 +456,7 @@ cudaError_t quantile_splitters(const uint64_t* x, uint32_t s, int nsplit, uint64
   return cudaGetLastError();
 }
 
-cudaError_t judge_splitters(const uint64_t* x, uint32_t s, const uint64_t* S, int nbuckets, uint32_t* counts,
+cudaError_t vet_splitters(const uint64_t* x, uint32_t s, const uint64_t* S, int nbuckets, uint32_t* counts,
                             uint32_t* flags, cudaStream_t st) {
   cudaError_t e;
   if ((e = cudaMemsetAsync(counts, 0, sizeof(uint32_t) * nbuckets, st)) != cudaSuccess) return e;
@@ -464,8 +464,8 @@ cudaError_t judge_splitters(const uint64_t* x, uint32_t s, const uint64_t* S, in
   // a bucket may hold up to 2.5x its share of the sample before the plain
   // splitters take over
   const uint32_t limit = (uint32_t)(2.5 * (double)s / (double)nbuckets) + 8;
-  k_judge_count<<<grid_for(s, 256), 256, 0, st>>>(x, s, S, nbuckets, counts, flags);
-  k_judge_max<<<grid_for(nbuckets, 256), 256, 0, st>>>(counts, nbuckets, limit, flags);
+  k_vet_count<<<grid_for(s, 256), 256, 0, st>>>(x, s, S, nbuckets, counts, flags);
+  k_vet_max<<<grid_for(nbuckets, 256), 256, 0, st>>>(counts, nbuckets, limit, flags);
   note_launches(2);
   return cudaGetLastError();
 }

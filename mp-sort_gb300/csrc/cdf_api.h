@@ -47,7 +47,7 @@ cudaError_t quantile_splitters(const uint64_t* x, uint32_t s, int nsplit, uint64
                                cudaStream_t st);
 // Rejects (flags[0] != 0) a splitter set that leaves a heavy sample key out
 // of a single-key bucket or puts more than 2.5x its share in any bucket.
-cudaError_t judge_splitters(const uint64_t* x, uint32_t s, const uint64_t* S, int nbuckets, uint32_t* counts,
+cudaError_t vet_splitters(const uint64_t* x, uint32_t s, const uint64_t* S, int nbuckets, uint32_t* counts,
                             uint32_t* flags, cudaStream_t st);
 
 }  // namespace gb

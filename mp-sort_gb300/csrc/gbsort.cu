@@ -582,13 +582,13 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
       GB_CUDA(cdf_train(sA, s, sh, kCdfEpochs, 0.5f, w, st));
       GB_CUDA(cdf_splitters(sA, s, sh, nb, w.knots, S, st));
       GB_CUDA(finalize_splitters(S, nb - 1, st));
-      // the plain splitters judge the model's: if the sample shows a heavy
+      // the plain splitters vet the model's: if the sample shows a heavy
       // key outside a single-key bucket or an overfull bucket, the sample's
       // own quantiles (what the bisection converges to) replace them, on the
       // device; the model still serves the lookup, with windows for the
       // final splitters
       uint32_t* jcounts = bump.take<uint32_t>(nb);
-      GB_CUDA(judge_splitters(sA, s, S, nb, jcounts, fallback, st));
+      GB_CUDA(vet_splitters(sA, s, S, nb, jcounts, fallback, st));
       GB_CUDA(quantile_splitters(sA, s, nb - 1, S, fallback, st));
       GB_CUDA(finalize_splitters(S, nb - 1, st, fallback));
       GB_CUDA(cdf_windows(sh, nb, w.knots, S, win, wlo, whi, widest, st));
