@@ -67,7 +67,9 @@ typedef struct gbsort_stats {
     uint32_t launches;           /* kernels this sort enqueued */
     uint32_t splitter_fallback;  /* 1: the model's splitters failed the sample check and the
                                     sample quantiles (the plain splitters) were used */
-    uint32_t reserved[2];
+    uint32_t heavy_keys;         /* keys owning a single-key bucket worth three splitters or more,
+                                    looked up by hash before the bucket search */
+    uint32_t reserved;
 } gbsort_stats;
 
 /* Sort nmemb records of elsize bytes from d_in into d_out (device memory;

@@ -305,6 +305,28 @@ __global__ void k_cdf_windows(CdfShape sh, int nbuckets, const float2* __restric
   }
 }
 
+// Knot pair of leaf l from the buckets of its first and last key: bucket + 1/2
+// over nbuckets, so that the floor of the prediction is that bucket at both
+// ends (nbuckets is a power of two: the quotients are exact).
+__global__ void k_refit_knots(CdfShape sh, int nbuckets, const uint64_t* __restrict__ S, float2* __restrict__ knots,
+                              const uint32_t* __restrict__ only_if) {
+  if (only_if && *only_if == 0) return;
+  sh = resolve_shape(sh);
+  const int nleaf = 1 << sh.lbits;
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nleaf) return;
+  uint64_t first = sh.kmin + ((uint64_t)l << sh.lshift), last;
+  if (l == nleaf - 1) last = ~0ull;
+  else last = sh.kmin + ((uint64_t)(l + 1) << sh.lshift) - 1;
+  if (sh.lshift >= 64) {  // a single leaf spans everything
+    first = sh.kmin;
+    last = ~0ull;
+  }
+  const float inv = 1.f / (float)nbuckets;
+  const uint32_t bx = true_bucket(S, nbuckets - 1, first), by = true_bucket(S, nbuckets - 1, last);
+  knots[l] = make_float2(((float)bx + 0.5f) * inv, ((float)by + 0.5f) * inv);
+}
+
 __global__ void k_pack_windows(const uint32_t* __restrict__ lo, const uint32_t* __restrict__ hi, int nleaf,
                                uint32_t* __restrict__ win, uint32_t* wide) {
   int l = blockIdx.x * blockDim.x + threadIdx.x;
@@ -445,6 +467,15 @@ cudaError_t cdf_windows(const CdfShape& sh, int nbuckets, const float2* knots, c
   k_cdf_windows<<<grid_for(nbuckets + nleaf, 128), 128, 0, st>>>(sh, nbuckets, knots, S, tmp_lo, tmp_hi);
   k_pack_windows<<<grid_for(nleaf, 256), 256, 0, st>>>(tmp_lo, tmp_hi, nleaf, win, widest);
   note_launches(2);
+  return cudaGetLastError();
+}
+
+cudaError_t refit_knots(const CdfShape& sh, int nbuckets, const uint64_t* S, float2* knots, const uint32_t* only_if,
+                        cudaStream_t st) {
+  const int nleaf = 1 << sh.lbits;
+  if (nbuckets < 2) return cudaSuccess;
+  k_refit_knots<<<grid_for(nleaf, 256), 256, 0, st>>>(sh, nbuckets, S, knots, only_if);
+  note_launches(1);
   return cudaGetLastError();
 }
 

@@ -45,6 +45,13 @@ cudaError_t cdf_windows(const CdfShape& sh, int nbuckets, const float2* knots, c
 // (only when *only_if != 0, if only_if is given).
 cudaError_t quantile_splitters(const uint64_t* x, uint32_t s, int nsplit, uint64_t* S, const uint32_t* only_if,
                                cudaStream_t st);
+// Knots of every leaf set from the splitters S instead of the training (only
+// when *only_if != 0): the model then predicts, at each leaf's first and last
+// key, the true bucket, and in between no more splitters away than the leaf
+// holds.  Used when the sample quantiles replaced the model's splitters,
+// which the trained knots do not predict.
+cudaError_t refit_knots(const CdfShape& sh, int nbuckets, const uint64_t* S, float2* knots, const uint32_t* only_if,
+                        cudaStream_t st);
 // Rejects (flags[0] != 0) a splitter set that leaves a heavy sample key out
 // of a single-key bucket or puts more than 2.5x its share in any bucket.
 cudaError_t vet_splitters(const uint64_t* x, uint32_t s, const uint64_t* S, int nbuckets, uint32_t* counts,

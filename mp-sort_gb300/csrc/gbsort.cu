@@ -116,6 +116,7 @@ enum CounterSlot : int {
   CNT_L2 = 24,           // level-2 task counters: nsplit[2], nlocal, work
   CNT_FALLBACK = 28,     // the learned splitters were rejected
   CNT_OVERFLOW = 29,     // a bucket outgrew its reserved region (pipelined host sort)
+  CNT_HEAVY = 30,        // keys in the heavy-key table
   CNT_WORDS = 64
 };
 
@@ -514,7 +515,7 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
   const int nleaf = 1 << lbits;
   size_t small_bytes = (size_t)s * 16 + (size_t)nb * 8 + (size_t)nb * G * 8 + Level2::bytes(cap_split, cap_local) +
                        lsd_scratch_bytes(std::max<uint32_t>(s, 1), 1) + (size_t)nleaf * 64 + (size_t)nb * 24 +
-                       (4 << 20);
+                       sizeof(HeavyTable) + (4 << 20);
   GB_CUDA(c.small.ensure(small_bytes));
   Bump bump{c.small.as<uint8_t>()};
   uint32_t* counters = bump.take<uint32_t>(CNT_WORDS);
@@ -585,12 +586,13 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
       // the plain splitters vet the model's: if the sample shows a heavy
       // key outside a single-key bucket or an overfull bucket, the sample's
       // own quantiles (what the bisection converges to) replace them, on the
-      // device; the model still serves the lookup, with windows for the
-      // final splitters
+      // device; the model still serves the lookup, its knots then set from
+      // the final splitters, with windows for them
       uint32_t* jcounts = bump.take<uint32_t>(nb);
       GB_CUDA(vet_splitters(sA, s, S, nb, jcounts, fallback, st));
       GB_CUDA(quantile_splitters(sA, s, nb - 1, S, fallback, st));
       GB_CUDA(finalize_splitters(S, nb - 1, st, fallback));
+      GB_CUDA(refit_knots(sh, nb, S, w.knots, fallback, st));
       GB_CUDA(cdf_windows(sh, nb, w.knots, S, win, wlo, whi, widest, st));
       model.lbits = lbits;
       model.nbuckets = nb;
@@ -599,6 +601,9 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
       model.shape = dshape;
       lookup = LOOKUP_LEARNED;
     }
+    HeavyTable* heavy = bump.take<HeavyTable>(1);
+    GB_CUDA(heavy_table(S, nb - 1, heavy, counters + CNT_HEAVY, st));
+    p.heavy = heavy;
   }
   if (timing) GB_CUDA(cudaEventRecord(c.ev[1], st));
   const ModelDev* mp = lookup == LOOKUP_LEARNED ? &model : nullptr;
@@ -751,6 +756,7 @@ int hsort_collect(Context& c) {
   memcpy(&loss, &h[CNT_LOSS], 4);
   g_stats.model_loss = c.run_learned ? loss : 0.f;
   g_stats.splitter_fallback = c.run_learned && h[CNT_FALLBACK] ? 1u : 0u;
+  g_stats.heavy_keys = h[CNT_HEAVY];
   if (c.run_timing)
     for (int i = 0; i < 6; ++i) {
       float ms = 0.f;

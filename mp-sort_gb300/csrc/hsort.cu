@@ -223,6 +223,62 @@ __global__ void __launch_bounds__(1024) k_finalize_splitters(uint64_t* S, int ns
   }
 }
 
+// ------------------------------------------------------- heavy keys ------
+__device__ __forceinline__ uint32_t heavy_hash(uint64_t key) {
+  return (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - kHeavyLog2));
+}
+
+__global__ void __launch_bounds__(1024) k_heavy_table(const uint64_t* __restrict__ S, int nsplit,
+                                                      HeavyTable* __restrict__ t, uint32_t* held) {
+  for (int i = threadIdx.x; i < kHeavySlots; i += blockDim.x) t->slot[i].bucket1 = 0;
+  if (threadIdx.x == 0) t->n = t->probes = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i + 2 < nsplit; i += blockDim.x) {
+    const uint64_t a = S[i], b = S[i + 1];
+    if (a + 1 != b || S[i + 2] != b) continue;  // bucket i + 1 is not [a, a + 1) worth two splitters
+    const uint32_t h = heavy_hash(a);
+    // copies of b from i + 1 on: at least two, below 2^13; bucket i + 1 < 2^14
+    const uint32_t m = upper_bound_in(S, (uint32_t)i + 1, (uint32_t)nsplit, b) - ((uint32_t)i + 1);
+    for (int j = 0; j < kHeavyProbes; ++j) {  // a key that finds no slot keeps the ordinary lookup
+      HeavySlot& sl = t->slot[(h + j) & (kHeavySlots - 1)];
+      if (atomicCAS(&sl.bucket1, 0u, (uint32_t)i + 2) == 0) {
+        sl.key = a;
+        sl.weight = (m << 14) | ((uint32_t)i + 1);
+        atomicAdd(&t->n, 1u);
+        atomicMax(&t->probes, (uint32_t)j + 1);
+        break;
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && held) *held = t->n;
+}
+
+// The weight word of `key` if the table holds it (its bucket in the low 14
+// bits), else 0.  probes: the table's longest probe sequence, 0 for an empty
+// or absent table.
+constexpr uint32_t kHeavyBucketMask = 0x3fffu;
+__device__ __forceinline__ uint32_t heavy_lookup(const HeavyTable* t, uint32_t probes, uint64_t key) {
+  const uint32_t h = heavy_hash(key);
+  for (uint32_t j = 0; j < probes; ++j) {
+    const uint4 s = __ldg(reinterpret_cast<const uint4*>(&t->slot[(h + j) & (kHeavySlots - 1)]));
+    if (s.z == 0) break;
+    if ((((uint64_t)s.y << 32) | s.x) == key) return s.w;
+  }
+  return 0;
+}
+// The bucket of `key` if the table holds it, else kNoHeavy.
+constexpr uint32_t kNoHeavy = 0xffffffffu;
+__device__ __forceinline__ uint32_t heavy_bucket(const HeavyTable* t, uint32_t probes, uint64_t key) {
+  const uint32_t h = heavy_hash(key);
+  for (uint32_t j = 0; j < probes; ++j) {
+    const uint4 s = __ldg(reinterpret_cast<const uint4*>(&t->slot[(h + j) & (kHeavySlots - 1)]));
+    if (s.z == 0) break;
+    if ((((uint64_t)s.y << 32) | s.x) == key) return s.z - 1;
+  }
+  return kNoHeavy;
+}
+
 // ---------------------------------------------------------- lookups ------
 struct LookupSmem {
   uint64_t* S;
@@ -272,19 +328,12 @@ size_t lookup_smem_bytes(int nbuckets, const ModelDev* m) {
 }
 
 // ----------------------------------------------------- level-1 count ------
-template <int LK>
-__global__ void __launch_bounds__(kThreads, 2) k_l1_count(HsortParams p, const uint64_t* __restrict__ S,
-                                                        int nbuckets, ModelDev model,
-                                                        uint32_t* __restrict__ counts,
-                                                        uint32_t* __restrict__ stats, uint32_t c0, uint32_t nchunks) {
-  model = resolve_model(model);
-  extern __shared__ __align__(16) uint8_t smem[];
-  LookupSmem L;
-  uint32_t* hist = reinterpret_cast<uint32_t*>(load_lookup<LK>(smem, S, nbuckets, model, L));
-  for (int i = threadIdx.x; i < nbuckets; i += kThreads) hist[i] = 0;
-  __syncthreads();
-  const uint32_t c = c0 + blockIdx.x, g = nchunks;  // this CTA's chunk of the nchunks
-  const uint32_t cb = chunk_begin(p.n, c, g), ce = chunk_end(p.n, c, g);
+// Counts of records [cb, ce) per bucket into hist.  HEAVY: probe the
+// heavy-key table (hprobes > 0) first.
+template <int LK, bool HEAVY>
+__device__ __forceinline__ void count_range(const HsortParams& p, const LookupSmem& L, const ModelDev& model,
+                                            int nbuckets, uint32_t* hist, uint32_t* stats, uint32_t cb, uint32_t ce,
+                                            uint32_t hprobes) {
   constexpr int U = 8;
   // keys of the next batch are loaded while the current batch is counted
   uint64_t k[U], kn[U];
@@ -303,10 +352,45 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_count(HsortParams p, const u
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       uint32_t i = base + u * kThreads + threadIdx.x;
-      bool v = i < ce;
-      if (v) atomicAdd(&hist[lookup<LK>(L, model, nbuckets, k[u], stats + STAT_WINDOW_MISS)], 1u);
+      const bool v = i < ce;
+      if constexpr (!HEAVY) {
+        if (v) atomicAdd(&hist[lookup<LK>(L, model, nbuckets, k[u], stats + STAT_WINDOW_MISS)], 1u);
+        continue;
+      }
+      uint32_t hw = v ? heavy_lookup(p.heavy, hprobes, k[u]) : 0;
+      if (v && !hw) atomicAdd(&hist[lookup<LK>(L, model, nbuckets, k[u], stats + STAT_WINDOW_MISS)], 1u);
+      // records of heavy keys: the warp's two heaviest keys are counted with
+      // one atomic each (many lanes adding to one counter serialise)
+      if (__any_sync(GB_FULL_MASK, hw != 0)) {
+#pragma unroll
+        for (int round = 0; round < 2; ++round) {
+          const uint32_t top = __reduce_max_sync(GB_FULL_MASK, hw);
+          const uint32_t same = __ballot_sync(GB_FULL_MASK, top != 0 && hw == top);
+          if (same && lane_id() == (uint32_t)(__ffs(same) - 1)) atomicAdd(&hist[top & kHeavyBucketMask], __popc(same));
+          if (hw == top) hw = 0;
+        }
+        if (hw) atomicAdd(&hist[hw & kHeavyBucketMask], 1u);
+      }
     }
   }
+}
+
+template <int LK>
+__global__ void __launch_bounds__(kThreads, 2) k_l1_count(HsortParams p, const uint64_t* __restrict__ S,
+                                                        int nbuckets, ModelDev model,
+                                                        uint32_t* __restrict__ counts,
+                                                        uint32_t* __restrict__ stats, uint32_t c0, uint32_t nchunks) {
+  model = resolve_model(model);
+  extern __shared__ __align__(16) uint8_t smem[];
+  LookupSmem L;
+  uint32_t* hist = reinterpret_cast<uint32_t*>(load_lookup<LK>(smem, S, nbuckets, model, L));
+  for (int i = threadIdx.x; i < nbuckets; i += kThreads) hist[i] = 0;
+  __syncthreads();
+  const uint32_t hprobes = p.heavy ? p.heavy->probes : 0;
+  const uint32_t c = c0 + blockIdx.x, g = nchunks;  // this CTA's chunk of the nchunks
+  const uint32_t cb = chunk_begin(p.n, c, g), ce = chunk_end(p.n, c, g);
+  if (hprobes) count_range<LK, true>(p, L, model, nbuckets, hist, stats, cb, ce, hprobes);
+  else count_range<LK, false>(p, L, model, nbuckets, hist, stats, cb, ce, 0);
   __syncthreads();
   for (int b = threadIdx.x; b < nbuckets; b += kThreads) counts[(size_t)b * g + c] = hist[b];
 }
@@ -466,6 +550,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
   uint8_t* cnt = q;  // [nbuckets][kWarps]
   for (int i = threadIdx.x; i < nbuckets * kWarps / 16; i += kThreads)
     reinterpret_cast<uint4*>(cnt)[i] = make_uint4(0, 0, 0, 0);
+  const uint32_t hprobes = p.heavy ? p.heavy->probes : 0;
 
   const uint32_t w = warp_id(), lane = lane_id();
   // the count kernel's chunks, several per CTA
@@ -510,7 +595,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
       bkt[r] = kNoBucket;
       if (e < nvalid) {
         uint64_t k = key_from_regs<EW>(rec[r], p.key);
-        bkt[r] = lookup<LK>(L, model, nbuckets, k, stats + STAT_WINDOW_MISS);
+        const uint32_t hb = hprobes ? heavy_bucket(p.heavy, hprobes, k) : kNoHeavy;
+        bkt[r] = hb != kNoHeavy ? hb : lookup<LK>(L, model, nbuckets, k, stats + STAT_WINDOW_MISS);
       }
     }
     // 1. ranks within the warp, in (r, lane) order
@@ -1303,6 +1389,13 @@ cudaError_t plain_splitters(const uint64_t* sorted_sample, uint32_t s, int nspli
   if (e != cudaSuccess) return e;
   k_plain_splitters<<<(nsplit + 127) / 128, 128, 0, stream>>>(sorted_sample, s, nsplit, splitters, iters,
                                                                clt, cle);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t heavy_table(const uint64_t* splitters, int nsplit, HeavyTable* table, uint32_t* held,
+                        cudaStream_t stream) {
+  k_heavy_table<<<1, 1024, 0, stream>>>(splitters, nsplit, table, held);
   note_launches(1);
   return cudaGetLastError();
 }

@@ -86,6 +86,27 @@ __host__ __device__ inline SortTask make_task(uint32_t start, uint32_t count, ui
   return SortTask{start, count, lo, hi, start, (in_b ? (uint32_t)TASK_SRC_B : 0u) | (copy ? (uint32_t)TASK_COPY : 0u)};
 }
 
+// Keys heavy enough to own a single-key level-1 bucket worth three
+// splitters or more: a run of equal splitters k becomes [k, k+1) followed by
+// copies of k + 1 (finalize_splitters), so bucket i + 1 holds exactly the key
+// S[i] when S[i] + 1 == S[i + 1] == S[i + 2].  The level-1 kernels probe
+// this open-addressing table before the bucket lookup: a learned window
+// spans a heavy key's whole run, and a binary search every heavy record.
+constexpr int kHeavyLog2 = 11;
+constexpr int kHeavySlots = 1 << kHeavyLog2;
+constexpr int kHeavyProbes = 8;  // longest probe sequence an insert may take
+struct HeavySlot {
+  uint64_t key;
+  uint32_t bucket1;  // bucket + 1; 0 marks an empty slot
+  uint32_t weight;   // (splitters the key spans) << 14 | bucket: larger is heavier
+};
+struct HeavyTable {
+  uint32_t n;       // keys held
+  uint32_t probes;  // longest probe sequence of an insert (0: table empty)
+  uint32_t pad[2];
+  HeavySlot slot[kHeavySlots];
+};
+
 struct HsortParams {
   const uint8_t* in;
   uint8_t* out;
@@ -96,6 +117,7 @@ struct HsortParams {
   gbsort_key_word key;
   uint32_t a_cap;      // records scratch A holds (n, or more for reserved bucket regions)
   uint32_t chunks;     // count chunks of the input (0: hsort_grid(n))
+  const HeavyTable* heavy;  // heavy keys of the level-1 splitters (null: none)
 };
 
 bool hsort_supported(uint32_t elsize);
@@ -108,6 +130,10 @@ cudaError_t sample_keys(const uint8_t* rec, uint32_t n, uint32_t elsize, gbsort_
 cudaError_t plain_splitters(const uint64_t* sorted_sample, uint32_t s, int nsplit,
                             uint64_t* splitters, uint32_t* iters, int64_t* clt, int64_t* cle,
                             cudaStream_t stream);
+// The heavy-key table of sorted splitters S (one CTA); *held receives the
+// number of keys it holds.
+cudaError_t heavy_table(const uint64_t* splitters, int nsplit, HeavyTable* table, uint32_t* held,
+                        cudaStream_t stream);
 cudaError_t finalize_splitters(uint64_t* splitters, int nsplit, cudaStream_t stream, const uint32_t* only_if = nullptr);
 // Level-1 bucket counts per chunk ([nbuckets][grid]) and the stable scatter.
 // `model` points to a host copy of the ModelDev (cdf.cuh) for the learned

@@ -474,6 +474,28 @@ def test_learned_heavy_keys_balanced(mp, nvals):
     assert st["max_bucket"] <= max(limit, int(counts.max()))
 
 
+@pytest.mark.parametrize("method", ["plain", "learned"])
+@pytest.mark.parametrize("nheavy", [100, 600])
+def test_heavy_key_table(mp, method, nheavy):
+    """Keys that own single-key buckets worth several splitters are looked
+    up by hash before the bucket search: hundreds of them (hash collisions
+    included) over a uniform background sort exactly as the stable sort, and
+    the statistics report the table in use."""
+    rng = numpy.random.default_rng(nheavy)
+    n = 4_000_000
+    dt = numpy.dtype([('key', 'u8'), ('val', 'i8')])
+    a = numpy.zeros(n, dt)
+    heavy = rng.integers(0, 2**64, nheavy, dtype=numpy.uint64, endpoint=False)
+    a['key'] = rng.integers(0, 2**64, n, dtype=numpy.uint64, endpoint=False)
+    pick = rng.random(n) < 0.9
+    a['key'][pick] = heavy[rng.integers(0, nheavy, int(pick.sum()))]
+    a['val'] = numpy.arange(n)
+    check(mp, a, 'key', method)
+    st = mp.last_stats()
+    assert st["heavy_keys"] >= (50 if nheavy == 100 else 1), st
+    assert st["window_misses"] == 0
+
+
 # ------------------------------------------------------------ graph plans --
 @pytest.mark.parametrize("method", ["auto"] + METHODS)
 def test_plan_graph_replay(mp, method):
