@@ -69,7 +69,7 @@ typedef struct gbsort_stats {
                                     sample quantiles (the plain splitters) were used */
     uint32_t heavy_keys;         /* keys owning a single-key bucket worth three splitters or more,
                                     looked up by hash before the bucket search */
-    uint32_t reserved;
+    uint32_t refined_splits;     /* bucket splits whose crowded bins were cut into finer bins */
 } gbsort_stats;
 
 /* Sort nmemb records of elsize bytes from d_in into d_out (device memory;

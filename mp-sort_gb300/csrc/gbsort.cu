@@ -757,6 +757,7 @@ int hsort_collect(Context& c) {
   g_stats.model_loss = c.run_learned ? loss : 0.f;
   g_stats.splitter_fallback = c.run_learned && h[CNT_FALLBACK] ? 1u : 0u;
   g_stats.heavy_keys = h[CNT_HEAVY];
+  g_stats.refined_splits = h[STAT_REFINED];
   if (c.run_timing)
     for (int i = 0; i < 6; ++i) {
       float ms = 0.f;

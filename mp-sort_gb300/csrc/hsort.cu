@@ -48,8 +48,13 @@ constexpr int local_ctas_per_sm() {
 }
 constexpr int kLocalBits = 11;         // bins of the local counting pass (about one record each)
 constexpr int kInsertMax = 24;         // bins up to this size use insertion sort
-constexpr int kSplitBits = 12;         // bins of a bucket split
+#ifndef GB_SPLIT_BITS
+#define GB_SPLIT_BITS 12
+#endif
+constexpr int kSplitBits = GB_SPLIT_BITS;  // bins of a bucket split
 constexpr int kSplitBins = 1 << kSplitBits;
+constexpr int kFineBins = 2 * kSplitBins;  // bins of a split after crowded bins are refined
+constexpr uint32_t kCrowded = 512;     // records of a split bin that get it refined (at least)
 constexpr int kMaxGroups = 512;        // sub-buckets per split
 constexpr uint32_t kCopyPiece = 1u << 16;
 
@@ -817,12 +822,13 @@ struct LocalSmemT {
   SortTask next;
 };
 constexpr int kSplitTileBytes = kThreads * 64;  // a scatter tile: kThreads * RPT records of <= 16 / RPT words
+static_assert(kFineBins * 4 <= kSplitTileBytes, "the fine histogram fits the staging tile");
 struct SplitSmem {
   __align__(16) uint8_t stage[kSplitTileBytes];  // the tile in group order
   uint16_t sgrp[kThreads * 4];                   // group of each staged record
   uint32_t goff[kMaxGroups];                     // first staged slot of each group
-  uint32_t hist[kSplitBins];
-  uint16_t gmap[kSplitBins];
+  uint32_t hist[kSplitBins];  // bin counts; for refined bins then (first fine bin << 4 | sub-bin bits)
+  uint16_t gmap[kFineBins];
   uint32_t cursor[kMaxGroups];
   __align__(16) uint8_t gcnt[kMaxGroups * kWarps];  // warp-row ranking table, zero between tiles
   uint64_t red[2 * kWarps];
@@ -1044,6 +1050,46 @@ __device__ void local_sort(LocalSmemT<NT>& sm, const uint8_t* src, uint8_t* dst,
   __syncthreads();
 }
 
+// Fine bins of a split with refined (crowded) bins: cm[b] = first fine bin
+// of bin b << 4 | r, bin b being cut into 2^r sub-bins of its key range.
+__device__ __forceinline__ uint32_t fine_bin(const uint32_t* cm, uint64_t key, uint64_t blo, int shift,
+                                             uint32_t nbins) {
+  const uint64_t x = key > blo ? key - blo : 0;
+  const uint32_t b = (uint32_t)min(x >> shift, (uint64_t)(nbins - 1));
+  const uint32_t c = cm[b], r = c & 15u;
+  const uint32_t sub = r ? (uint32_t)(x >> (shift - (int)r)) & ((1u << r) - 1u) : 0u;
+  return (c >> 4) + sub;
+}
+// Least key of fine bin f (f below the number of fine bins).
+__device__ __forceinline__ uint64_t fine_bin_lo(const uint32_t* cm, uint32_t f, uint64_t blo, int shift,
+                                                uint32_t nbins) {
+  uint32_t lo = 0, hi = nbins;  // the last bin whose first fine bin is <= f
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if ((cm[mid] >> 4) <= f) lo = mid;
+    else hi = mid;
+  }
+  const uint32_t r = cm[lo] & 15u, sub = f - (cm[lo] >> 4);
+  return blo + ((uint64_t)lo << shift) + ((uint64_t)sub << (shift - (int)r));
+}
+// In-place exclusive scan of PER * kThreads bin counts (PER per thread).
+template <int PER>
+__device__ __forceinline__ void scan_bins(uint32_t* a, uint32_t* scan_tmp) {
+  uint32_t loc[PER], s = 0;
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    loc[i] = a[threadIdx.x * PER + i];
+    s += loc[i];
+  }
+  uint32_t pre = block_exclusive_scan<uint32_t>(s, scan_tmp, nullptr);
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    a[threadIdx.x * PER + i] = pre;
+    pre += loc[i];
+  }
+  __syncthreads();
+}
+
 // Split of one large bucket: 4096 bins of its key range, grouped into at most
 // 256 runs of consecutive bins, a stable scatter src -> other by group, and
 // one task per group (local sort, copy, or another split).
@@ -1100,50 +1146,104 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
     shift = bits > kSplitBits ? bits - kSplitBits : 0;
     nbins = (uint32_t)((bhi - blo) >> shift) + 1;
   }
-  // exclusive scan of the bins, then the group of every bin
-  {
+  // Crowded bins (clustered keys): a bin of more than kCrowded records and
+  // four times the mean is cut into 2^r sub-bins of its key range (r up to
+  // kSplitBits, at most kFineBins bins in all) and the bucket is
+  // histogrammed once more over these fine bins, so that it splits in one
+  // round rather than sending every crowded bin round the split again.  Fine
+  // bins keep key order: those of bin b follow those of bin b - 1.
+  const uint32_t crowd = max(kCrowded, 4 * (m / nbins));
+  bool crowded = false;
+  for (uint32_t b = threadIdx.x; b < nbins; b += kThreads) crowded |= sm.hist[b] > crowd;
+  const bool refined = __syncthreads_or(crowded) && shift > 0;
+  uint32_t* counts = sm.hist;  // bins the groups are formed from
+  uint32_t nfine = nbins;
+  if (refined) {
+    // sub-bin bits: about 128 records per fine bin, fewer bits for all
+    // while the total exceeds kFineBins
+    auto rbits = [&](uint32_t c, int cut) -> uint32_t {
+      if (c <= crowd) return 0;
+      const int r = min(min(bitlen64(c - 1) - 7, kSplitBits), shift) - cut;
+      return r > 0 ? (uint32_t)r : 0u;
+    };
     constexpr int PER = kSplitBins / kThreads;
-    uint32_t loc[PER], s = 0;
+    int cut = 0;
+    uint32_t total = 0, pre = 0;
+    for (;;) {
+      uint32_t s = 0;
+#pragma unroll
+      for (int i = 0; i < PER; ++i) {
+        const uint32_t b = threadIdx.x * PER + i;
+        if (b < nbins) s += 1u << rbits(sm.hist[b], cut);
+      }
+      pre = block_exclusive_scan<uint32_t>(s, sm.scan_tmp, &total);
+      if (total <= (uint32_t)kFineBins) break;
+      ++cut;  // all-zero bits give nbins <= kSplitBins fine bins, so this ends
+    }
+    uint32_t cm[PER];
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
-      loc[i] = sm.hist[threadIdx.x * PER + i];
-      s += loc[i];
+      const uint32_t b = threadIdx.x * PER + i;
+      const uint32_t r = b < nbins ? rbits(sm.hist[b], cut) : 0;
+      cm[i] = (pre << 4) | r;
+      pre += b < nbins ? 1u << r : 0u;
     }
-    uint32_t pre = block_exclusive_scan<uint32_t>(s, sm.scan_tmp, nullptr);
+    __syncthreads();
 #pragma unroll
-    for (int i = 0; i < PER; ++i) {
-      sm.hist[threadIdx.x * PER + i] = pre;
-      pre += loc[i];
+    for (int i = 0; i < PER; ++i) sm.hist[threadIdx.x * PER + i] = cm[i];
+    // the fine histogram lives in the staging tile until the scatter
+    counts = reinterpret_cast<uint32_t*>(sm.stage);
+    for (int i = threadIdx.x; i < kFineBins; i += kThreads) counts[i] = 0;
+    __syncthreads();
+    constexpr int U = 8;
+    for (uint32_t i0 = 0; i0 < m; i0 += kThreads * U) {
+      uint64_t kk[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        uint32_t i = i0 + u * kThreads + threadIdx.x;
+        kk[u] = i < m ? key_at(src, i, E, p.key) : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        uint32_t i = i0 + u * kThreads + threadIdx.x;
+        if (i < m) atomicAdd(&counts[fine_bin(sm.hist, kk[u], blo, shift, nbins)], 1u);
+      }
     }
+    nfine = total;
+    if (threadIdx.x == 0) atomicAdd(stats + STAT_REFINED, 1u);
+    __syncthreads();
   }
-  __syncthreads();
+  // exclusive scan of the bins, then the group of every bin
+  const uint32_t nscan = refined ? (uint32_t)kFineBins : (uint32_t)kSplitBins;
+  if (refined) scan_bins<kFineBins / kThreads>(counts, sm.scan_tmp);
+  else scan_bins<kSplitBins / kThreads>(counts, sm.scan_tmp);
   // group of a bin = slot of its midpoint: a bin holding most of the records
   // never shares a group with the empty bins on either side, so every group
   // that is split again covers a strictly narrower key range
   // target <= m / 2 keeps the first and the last bin's midpoints at least a
   // target apart, so no group spans every bin: each re-split narrows
   const uint32_t target = min(max((uint32_t)(kLocalMax - kLocalMax / 8), (m + kMaxGroups - 1) / kMaxGroups), m / 2);
-  for (uint32_t b = threadIdx.x; b < (uint32_t)kSplitBins; b += kThreads) {
+  for (uint32_t b = threadIdx.x; b < nscan; b += kThreads) {
     uint32_t gb_ = kMaxGroups - 1;
-    if (b < nbins) {
-      uint64_t incl = b + 1 < (uint32_t)kSplitBins ? sm.hist[b + 1] : m;
-      unsigned long long mid2 = (unsigned long long)sm.hist[b] + incl;
+    if (b < nfine) {
+      uint64_t incl = b + 1 < nscan ? counts[b + 1] : m;
+      unsigned long long mid2 = (unsigned long long)counts[b] + incl;
       gb_ = (uint32_t)min(mid2 / (2ull * target), (unsigned long long)(kMaxGroups - 1));
     }
     sm.gmap[b] = (uint16_t)gb_;
   }
   __syncthreads();
-  for (uint32_t b = threadIdx.x; b < nbins; b += kThreads) {
+  for (uint32_t b = threadIdx.x; b < nfine; b += kThreads) {
     int gcur = sm.gmap[b];
     int gprev = b ? (int)sm.gmap[b - 1] : -1;
     for (int g = gprev + 1; g <= gcur; ++g) {
-      sm.gstart[g] = sm.hist[b];
+      sm.gstart[g] = counts[b];
       sm.gfirst[g] = b;
     }
-    if (b == nbins - 1) {
+    if (b == nfine - 1) {
       for (int g = gcur + 1; g <= kMaxGroups; ++g) {
         sm.gstart[g] = m;
-        sm.gfirst[g] = nbins;
+        sm.gfirst[g] = nfine;
       }
     }
   }
@@ -1168,8 +1268,13 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
       if (e < nvalid) {
         RecIO<EW>::load(src + (size_t)(t0 + e) * E, rec[r]);
         uint64_t key = key_from_regs<EW>(rec[r], p.key);
-        uint64_t x = key > blo ? key - blo : 0;
-        uint32_t bin = (uint32_t)min(x >> shift, (uint64_t)(nbins - 1));
+        uint32_t bin;
+        if (refined) {
+          bin = fine_bin(sm.hist, key, blo, shift, nbins);
+        } else {
+          uint64_t x = key > blo ? key - blo : 0;
+          bin = (uint32_t)min(x >> shift, (uint64_t)(nbins - 1));
+        }
         grp[r] = sm.gmap[bin];
       }
     }
@@ -1218,8 +1323,9 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
     if (g1 == g0) continue;
     const uint32_t b0 = sm.gfirst[g], b1 = sm.gfirst[g + 1];
     const uint32_t s = g1 - g0;
-    const uint64_t glo = blo + ((uint64_t)b0 << shift);
-    const uint64_t ghi = b1 >= nbins ? bhi : blo + ((uint64_t)b1 << shift) - 1;
+    const uint64_t glo = refined ? fine_bin_lo(sm.hist, b0, blo, shift, nbins) : blo + ((uint64_t)b0 << shift);
+    const uint64_t ghi = b1 >= sm.gfirst[kMaxGroups] ? bhi  // (the number of bins there)
+                         : (refined ? fine_bin_lo(sm.hist, b1, blo, shift, nbins) : blo + ((uint64_t)b1 << shift)) - 1;
     const uint32_t nsrc = in_b ? 0u : 1u;
     if (glo == ghi || s == 1) {
       push_copy(L, task.start + g0, s, glo, ghi, nsrc, err);

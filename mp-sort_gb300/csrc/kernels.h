@@ -64,6 +64,7 @@ enum StatSlot : int {
   STAT_BIGBIN = 4,       // extra local MSD passes on clustered bins
   STAT_WINDOW_MISS = 5,  // learned lookups whose window missed (full search ran)
   STAT_MAX_BUCKET = 6,   // largest level-1 bucket
+  STAT_REFINED = 7,      // splits whose crowded bins were cut finer
   STAT_SLOTS = 8
 };
 

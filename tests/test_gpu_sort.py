@@ -475,6 +475,22 @@ def test_learned_heavy_keys_balanced(mp, nvals):
 
 
 @pytest.mark.parametrize("method", ["plain", "learned"])
+def test_split_refines_crowded_bins(mp, method):
+    """Particles in Gaussian clusters with Morton keys (40-byte records):
+    level-1 buckets hold dense cores beside sparse background, so split bins
+    crowd; those bins are cut finer within the same split and the records
+    still come out in the stable order."""
+    import torch
+    import workloads as W
+    n = 8_000_000
+    buf, dt = W.particles_4(torch, n)
+    a = buf.cpu().numpy().view(dt)
+    check(mp, a, 'key', method)
+    st = mp.last_stats()
+    assert st["splits"] > 0 and st["refined_splits"] > 0, st
+
+
+@pytest.mark.parametrize("method", ["plain", "learned"])
 @pytest.mark.parametrize("nheavy", [100, 600])
 def test_heavy_key_table(mp, method, nheavy):
     """Keys that own single-key buckets worth several splitters are looked
