@@ -34,17 +34,19 @@ namespace {
 #define GB_LOCAL_THREADS 256
 #endif
 #ifndef GB_LOCAL_CTAS
-#define GB_LOCAL_CTAS 4
+#define GB_LOCAL_CTAS 3
 #endif
 constexpr int kLocalMax = GB_LOCAL_MAX;          // records a local sort holds in shared memory
 constexpr int kLocalThreads = GB_LOCAL_THREADS;  // threads of a local-sort CTA
 constexpr int kLocalCtasPerSm = GB_LOCAL_CTAS;
-// Records above 16 bytes: one CTA fewer per SM, which leaves L1 room for the
-// gather's reads of the group (measured: 40-byte records 13.1 ms with three,
-// 18.4 ms with four CTAs per SM on 5e8 records).
+// Three CTAs per SM give 80 registers a thread: the local sort's pass calls
+// then need almost no stack (at four CTAs, 64 registers, the saves around
+// every call doubled the kernel's L2 stores; 1e9 x 16 B: 14.1 against 15.2
+// ms), and records above 16 bytes keep L1 room for the gather's reads of the
+// group (5e8 x 40 B: 13.1 ms with three, 18.4 ms with four).
 template <int EW>
 constexpr int local_ctas_per_sm() {
-  return EW > 4 && kLocalCtasPerSm > 1 ? kLocalCtasPerSm - 1 : kLocalCtasPerSm;
+  return kLocalCtasPerSm;
 }
 constexpr int kLocalBits = 11;         // bins of the local counting pass (about one record each)
 constexpr int kInsertMax = 24;         // bins up to this size use insertion sort
@@ -820,6 +822,8 @@ struct LocalSmemT {
   uint32_t scan_tmp[kNW];
   uint32_t task_id;
   SortTask next;
+  uint32_t pend_id;  // the task claimed for after the next one, and its descriptor
+  SortTask pend;
 };
 constexpr int kSplitTileBytes = kThreads * 64;  // a scatter tile: kThreads * RPT records of <= 16 / RPT words
 static_assert(kFineBins * 4 <= kSplitTileBytes, "the fine histogram fits the staging tile");
@@ -1405,13 +1409,17 @@ __global__ void __launch_bounds__(NT, local_ctas_per_sm<EW>()) k_local(HsortPara
     if (t >= nt) break;
     const SortTask task = sm.next;
     __syncthreads();
-    uint32_t nid = 0;
-    SortTask nxt{};
     if (warp_id() == 0) {
+      // the claim and its descriptor wait in shared memory: registers live
+      // across the sort would be saved to the stack around every pass call
       const uint32_t lane = lane_id();
+      uint32_t nid = 0;
+      SortTask nxt{};
       if (lane == 0) {
         nid = atomicAdd(work, 1u);
         if (nid < nt) nxt = tasks[nid];
+        sm.pend_id = nid;
+        sm.pend = nxt;
       }
       // the next task's records head for L2 while this one sorts; the
       // warp's lanes share the lines
@@ -1438,8 +1446,8 @@ __global__ void __launch_bounds__(NT, local_ctas_per_sm<EW>()) k_local(HsortPara
       if (threadIdx.x == 0) atomicAdd(stats + STAT_LOCAL, 1u);
     }
     if (threadIdx.x == 0) {
-      sm.task_id = nid;
-      sm.next = nxt;
+      sm.task_id = sm.pend_id;
+      sm.next = sm.pend;
     }
     __syncthreads();
   }
