@@ -70,6 +70,9 @@ typedef struct gbsort_stats {
     uint32_t heavy_keys;         /* keys owning a single-key bucket worth three splitters or more,
                                     looked up by hash before the bucket search */
     uint32_t refined_splits;     /* bucket splits whose crowded bins were cut into finer bins */
+    uint32_t pipelined;          /* 1: a host sort sent its input up in pieces, sorting as they landed */
+    uint32_t region_overflow;    /* pipelined: 0, or 1 + the first level-1 bucket that outgrew the
+                                    region reserved for it from the sample (level 1 was then redone) */
 } gbsort_stats;
 
 /* Sort nmemb records of elsize bytes from d_in into d_out (device memory;

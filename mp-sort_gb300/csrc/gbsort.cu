@@ -115,17 +115,23 @@ enum CounterSlot : int {
   CNT_LOSS = 23,         // final training loss (float)
   CNT_L2 = 24,           // level-2 task counters: nsplit[2], nlocal, work
   CNT_FALLBACK = 28,     // the learned splitters were rejected
-  CNT_OVERFLOW = 29,     // a bucket outgrew its reserved region (pipelined host sort)
   CNT_HEAVY = 30,        // keys in the heavy-key table
+  CNT_OVERFLOW = 31,     // a bucket outgrew its reserved region (pipelined host sort): bucket + 1,
+                         // then its capacity and count (3 words)
   CNT_WORDS = 64
 };
 
 constexpr int kMaxPieces = 16;  // host -> device pieces of a pipelined host sort
-// Reserved bucket regions of the pipelined host sort: the sample's estimate
-// of a bucket times 1.5 plus 256 records.  With 128 sampled keys per bucket
-// the estimate's relative spread is about 9 %, so a bucket outgrows its
-// region only past five standard deviations.
-constexpr float kRegionSlack = 1.5f;
+// Reserved bucket regions of the pipelined host sort.  A bucket holding c
+// of the s sampled keys gets (c + 5 sqrt(c + 1) + 10) * n / s records plus
+// 256: its count is c * n / s give or take sqrt(c + 1) * n / s, so the
+// region covers five standard deviations plus ten sampled keys' worth --
+// which matters for buckets the sample barely saw (after a heavy key's run
+// of equal splitters, the next bucket may hold no sampled key at all).  By
+// Cauchy-Schwarz, sum_b sqrt(c_b + 1) <= sqrt(nb (s + nb)), which bounds the
+// total reserved.
+constexpr double kRegionSigmas = 5.0;
+constexpr double kRegionSpare = 10.0;
 constexpr uint32_t kRegionPad = 256;
 constexpr int kMaxWaves = 16;   // level-2 waves (and device -> host pieces)
 
@@ -161,7 +167,7 @@ struct Context {
   std::mutex mu;
   // shape of the last enqueued histogram sort (for hsort_collect)
   uint32_t run_nbuckets = 0, run_sample = 0, run_lsd_passes = 0;
-  bool run_learned = false, run_timing = false;
+  bool run_learned = false, run_timing = false, run_pipelined = false;
 };
 
 std::mutex g_ctx_mu;
@@ -496,19 +502,25 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
                   bool learned, bool timing, const Knobs& knobs, cudaStream_t st, const HostPipe* hp = nullptr) {
   const int nb = choose_buckets(n, knobs);
   const int grid = hsort_grid(n);
+  const uint64_t spb = knobs.sample_per_bucket ? (uint64_t)knobs.sample_per_bucket : 128;
+  const uint32_t s = nb > 1 ? (uint32_t)std::min<uint64_t>(n, std::max<uint64_t>(4096, (uint64_t)nb * spb)) : 0;
   // pipelined: the input goes up in pieces, each cut into `grid` count
   // chunks, and is scattered as it lands into bucket regions reserved from
-  // the sample (slack kRegionSlack); scratch A holds the regions
+  // the sample (kRegion*); scratch A holds the regions
   const int pieces = hp ? std::min(hp->pieces, kMaxPieces) : 1;
   const int G = grid * pieces;  // count chunks
-  const uint64_t a_cap64 =
-      hp ? std::min<uint64_t>((uint64_t)(n * (double)kRegionSlack) + (uint64_t)nb * (kRegionPad + 1), 0xffffffffull)
-         : n;
+  uint64_t a_cap64 = n;
+  bool region_fit = false;  // the reserved regions fit 32-bit record offsets
+  if (hp && s > 0) {
+    const double per = (double)n / (double)s, snb = (double)s + nb;
+    const double reserved = ((double)s + kRegionSigmas * std::sqrt((double)nb * snb) + kRegionSpare * nb) * per +
+                            (double)nb * (kRegionPad + 2);
+    region_fit = reserved < 4294967295.0;
+    if (region_fit) a_cap64 = (uint64_t)reserved;
+  }
   const uint32_t a_cap = (uint32_t)std::max<uint64_t>(a_cap64, n);
   GB_CUDA(c.A.ensure((size_t)a_cap * elsize));
   GB_CUDA(c.B.ensure((size_t)n * elsize));
-  const uint64_t spb = knobs.sample_per_bucket ? (uint64_t)knobs.sample_per_bucket : 128;
-  const uint32_t s = nb > 1 ? (uint32_t)std::min<uint64_t>(n, std::max<uint64_t>(4096, (uint64_t)nb * spb)) : 0;
   const uint32_t cap_split = (uint32_t)nb + n / 4096 + 4096;
   const uint32_t cap_local = 4u * (uint32_t)nb + n / 512 + 65536;
   const int lbits = 11;
@@ -619,19 +631,24 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
     total = bump.take<uint32_t>(nb);
     out_start = bump.take<uint32_t>(nb);
     uint32_t* overflow = counters + CNT_OVERFLOW;
-    GB_CUDA(bucket_caps(bump_sample, s, S, nb, n, kRegionSlack, kRegionPad, cap, st));
-    GB_CUDA(exclusive_scan_u32(cap, region, (size_t)nb, scan_tmp, st));
-    GB_CUDA(cudaMemsetAsync(total, 0, sizeof(uint32_t) * nb, st));
-    for (int i = 0; i < pieces; ++i) {
-      GB_CUDA(cudaStreamWaitEvent(st, c.pev[i], 0));
-      GB_CUDA(l1_count(p, lookup, S, nb, mp, counts, stats, st, i * grid, (i + 1) * grid));
-      GB_CUDA(region_offsets(counts, G, nb, region, cap, total, i * grid, (i + 1) * grid, overflow, st));
-      GB_CUDA(l1_scatter(p, lookup, S, nb, mp, counts, stats, st, i * grid, (i + 1) * grid, overflow));
+    c.hc->c[CNT_OVERFLOW] = 0;
+    if (region_fit) {
+      GB_CUDA(bucket_caps(bump_sample, s, S, nb, n, kRegionSigmas, kRegionSpare, kRegionPad, cap, st));
+      GB_CUDA(exclusive_scan_u32(cap, region, (size_t)nb, scan_tmp, st));
+      GB_CUDA(cudaMemsetAsync(total, 0, sizeof(uint32_t) * nb, st));
+      for (int i = 0; i < pieces; ++i) {
+        GB_CUDA(cudaStreamWaitEvent(st, c.pev[i], 0));
+        GB_CUDA(l1_count(p, lookup, S, nb, mp, counts, stats, st, i * grid, (i + 1) * grid));
+        GB_CUDA(region_offsets(counts, G, nb, region, cap, total, i * grid, (i + 1) * grid, overflow, st));
+        GB_CUDA(l1_scatter(p, lookup, S, nb, mp, counts, stats, st, i * grid, (i + 1) * grid, overflow));
+      }
+      GB_CUDA(cudaMemcpyAsync(&c.hc->c[CNT_OVERFLOW], overflow, 12, cudaMemcpyDeviceToHost, st));
+    } else {  // regions would not fit 32-bit offsets: level 1 waits for the whole input
+      for (int i = 0; i < pieces; ++i) GB_CUDA(cudaStreamWaitEvent(st, c.pev[i], 0));
     }
-    GB_CUDA(cudaMemcpyAsync(&c.hc->c[CNT_OVERFLOW], overflow, 4, cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaEventRecord(c.sev, st));
     GB_CUDA(cudaEventSynchronize(c.sev));
-    regions = c.hc->c[CNT_OVERFLOW] == 0 && !getenv("GBSORT_NO_REGIONS");
+    regions = region_fit && c.hc->c[CNT_OVERFLOW] == 0 && !getenv("GBSORT_NO_REGIONS");
     if (regions) {
       GB_CUDA(exclusive_scan_u32(total, out_start, (size_t)nb, scan_tmp, st));
     } else {  // exact level 1 over the complete input
@@ -711,6 +728,9 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
       fprintf(stderr, "gbsort pipe: pieces up by %.2f ms (after the first)\n", t);
       cudaEventElapsedTime(&t, c.pev[0], c.sev);
       fprintf(stderr, "gbsort pipe: counts scanned at %.2f\n", t);
+      if (c.hc->c[CNT_OVERFLOW])
+        fprintf(stderr, "gbsort pipe: bucket %u outgrew its region (%u records reserved, %u counted)\n",
+                c.hc->c[CNT_OVERFLOW] - 1, c.hc->c[CNT_OVERFLOW + 1], c.hc->c[CNT_OVERFLOW + 2]);
       for (int j = 0; j < waves; ++j) {
         cudaEventElapsedTime(&t, c.pev[0], c.wev[j]);
         fprintf(stderr, "gbsort pipe: wave %d sorted at %.2f\n", j, t);
@@ -723,6 +743,7 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
   c.run_sample = s;
   c.run_learned = learned;
   c.run_timing = timing;
+  c.run_pipelined = hp != nullptr;
   return GBSORT_OK;
 }
 
@@ -758,6 +779,8 @@ int hsort_collect(Context& c) {
   g_stats.splitter_fallback = c.run_learned && h[CNT_FALLBACK] ? 1u : 0u;
   g_stats.heavy_keys = h[CNT_HEAVY];
   g_stats.refined_splits = h[STAT_REFINED];
+  g_stats.pipelined = c.run_pipelined ? 1u : 0u;
+  g_stats.region_overflow = c.run_pipelined ? h[CNT_OVERFLOW] : 0u;
   if (c.run_timing)
     for (int i = 0; i < 6; ++i) {
       float ms = 0.f;

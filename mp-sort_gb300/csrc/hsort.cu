@@ -1608,7 +1608,8 @@ __global__ void k_require_zero(const uint32_t* count, uint32_t* err) {
 
 // cap[b] = ceil(sample share of bucket b * n * slack) + pad.
 __global__ void k_bucket_caps(const uint64_t* __restrict__ x, uint32_t s, const uint64_t* __restrict__ S,
-                              int nbuckets, uint32_t n, float slack, uint32_t pad, uint32_t* __restrict__ cap) {
+                              int nbuckets, uint32_t n, double sigmas, double spare, uint32_t pad,
+                              uint32_t* __restrict__ cap) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nbuckets) return;
   // sample keys in [S[b-1], S[b]): lower bounds of the two splitters
@@ -1623,8 +1624,9 @@ __global__ void k_bucket_caps(const uint64_t* __restrict__ x, uint32_t s, const 
   };
   const uint32_t i0 = b == 0 ? 0u : lower(S[b - 1]);
   const uint32_t i1 = b == nbuckets - 1 ? s : lower(S[b]);
-  const double est = (double)(i1 - i0) * (double)n / (double)s;
-  cap[b] = (uint32_t)min(est * (double)slack + 1.0, (double)n) + pad;
+  const double c = (double)(i1 - i0);
+  const double want = (c + sigmas * sqrt(c + 1.0) + spare) * (double)n / (double)s;
+  cap[b] = (uint32_t)min(want + 1.0, (double)n) + pad;
 }
 
 __global__ void k_region_offsets(uint32_t* __restrict__ counts, int chunks, int nbuckets,
@@ -1640,7 +1642,12 @@ __global__ void k_region_offsets(uint32_t* __restrict__ counts, int chunks, int 
     run += x;
   }
   total[b] = run;
-  if (run > cap[b]) atomicOr(overflow, 1u);
+  // overflow[0] = first bucket that outgrew its region + 1; [1], [2] its
+  // capacity and count (for the pipeline trace)
+  if (run > cap[b] && atomicCAS(overflow, 0u, (uint32_t)b + 1) == 0) {
+    overflow[1] = cap[b];
+    overflow[2] = run;
+  }
 }
 
 __global__ void k_build_region_tasks(const uint32_t* __restrict__ region, const uint32_t* __restrict__ total,
@@ -1667,8 +1674,9 @@ __global__ void k_build_region_tasks(const uint32_t* __restrict__ region, const 
 }
 
 cudaError_t bucket_caps(const uint64_t* sorted_sample, uint32_t s, const uint64_t* splitters, int nbuckets,
-                        uint32_t n, float slack, uint32_t pad, uint32_t* cap, cudaStream_t stream) {
-  k_bucket_caps<<<(nbuckets + 255) / 256, 256, 0, stream>>>(sorted_sample, s, splitters, nbuckets, n, slack, pad, cap);
+                        uint32_t n, double sigmas, double spare, uint32_t pad, uint32_t* cap, cudaStream_t stream) {
+  k_bucket_caps<<<(nbuckets + 255) / 256, 256, 0, stream>>>(sorted_sample, s, splitters, nbuckets, n, sigmas, spare,
+                                                            pad, cap);
   note_launches(1);
   return cudaGetLastError();
 }

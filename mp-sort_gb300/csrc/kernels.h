@@ -146,13 +146,15 @@ cudaError_t l1_count(const HsortParams& p, int lookup, const uint64_t* splitters
                      int c1 = -1);
 // First record of chunk c of `chunks` (n for c >= chunks).
 uint32_t hsort_chunk_begin(uint32_t n, int c, int chunks);
-// Reserved bucket regions from the sorted sample: cap[b] = the bucket's
-// estimated size times slack (plus pad); the caller scans cap into starts.
+// Reserved bucket regions from the sorted sample: a bucket holding c of the
+// s sampled keys gets cap[b] = (c + sigmas sqrt(c + 1) + spare) * n / s
+// records (at most n) plus pad; the caller scans cap into starts.
 cudaError_t bucket_caps(const uint64_t* sorted_sample, uint32_t s, const uint64_t* splitters, int nbuckets,
-                        uint32_t n, float slack, uint32_t pad, uint32_t* cap, cudaStream_t stream);
+                        uint32_t n, double sigmas, double spare, uint32_t pad, uint32_t* cap, cudaStream_t stream);
 // Scatter offsets of chunks [c0, c1) into reserved regions: counts of those
 // chunks become region start + the bucket's running total (kept in total[]);
-// *overflow is set if a bucket outgrows its region.
+// if a bucket outgrows its region, overflow[0] becomes the first such bucket
+// + 1 and overflow[1], [2] its capacity and count.
 cudaError_t region_offsets(uint32_t* counts, int chunks, int nbuckets, const uint32_t* region, const uint32_t* cap,
                            uint32_t* total, int c0, int c1, uint32_t* overflow, cudaStream_t stream);
 // Scatter of chunks [c0, c1) (c1 < 0: all) to offsets[bucket][chunk]; does

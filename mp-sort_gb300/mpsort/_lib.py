@@ -39,7 +39,8 @@ class Stats(ctypes.Structure):
                 ("widest_window", ctypes.c_uint32), ("model_loss", ctypes.c_float),
                 ("stage_ms", ctypes.c_float * 6), ("launches", ctypes.c_uint32),
                 ("splitter_fallback", ctypes.c_uint32), ("heavy_keys", ctypes.c_uint32),
-                ("refined_splits", ctypes.c_uint32)]
+                ("refined_splits", ctypes.c_uint32), ("pipelined", ctypes.c_uint32),
+                ("region_overflow", ctypes.c_uint32)]
 
     STAGES = ("splitters", "count", "scan", "scatter", "split", "local")
 

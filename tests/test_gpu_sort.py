@@ -608,8 +608,12 @@ def test_host_sort_pipelined_pinned(mp, method, dist, regions, monkeypatch):
     hout = pin_out.numpy().view(dt)
     hin[:] = a
     mp.sort(hin, 'key', out=hout, method=method)
+    st = mp.last_stats()
     exp = O.numpy_sorted(a, 'key')
     assert hout.tobytes() == exp.tobytes()
     assert hin.tobytes() == a.tobytes()
+    if st["method"] != "lsd":
+        # regions reserved from the sample hold every bucket, skewed keys too
+        assert st["pipelined"] == 1 and (st["region_overflow"] == 0 or not regions), st
     mp.sort(hin, 'key', method=method)  # in place
     assert hin.tobytes() == exp.tobytes()
