@@ -56,7 +56,13 @@ constexpr int kInsertMax = 24;         // bins up to this size use insertion sor
 constexpr int kSplitBits = GB_SPLIT_BITS;  // bins of a bucket split
 constexpr int kSplitBins = 1 << kSplitBits;
 constexpr int kFineBins = 2 * kSplitBins;  // bins of a split after crowded bins are refined
-constexpr uint32_t kCrowded = 512;     // records of a split bin that get it refined (at least)
+#ifndef GB_SPLIT_CROWDED
+#define GB_SPLIT_CROWDED 512
+#endif
+constexpr uint32_t kCrowded = GB_SPLIT_CROWDED;  // records of a split bin that get it refined (at least)
+// Buckets below this many records are not refined: their second histogram
+// read costs more than the re-splits it saves (small segments sit in L2).
+constexpr uint32_t kRefineMin = 1u << 17;
 constexpr int kMaxGroups = 512;        // sub-buckets per split
 constexpr uint32_t kCopyPiece = 1u << 16;
 
@@ -1150,8 +1156,9 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
     shift = bits > kSplitBits ? bits - kSplitBits : 0;
     nbins = (uint32_t)((bhi - blo) >> shift) + 1;
   }
-  // Crowded bins (clustered keys): a bin of more than kCrowded records and
-  // four times the mean is cut into 2^r sub-bins of its key range (r up to
+  // Crowded bins (clustered keys): in a bucket of kRefineMin records or
+  // more, a bin of more than kCrowded records and four times the mean is
+  // cut into 2^r sub-bins of its key range (r up to
   // kSplitBits, at most kFineBins bins in all) and the bucket is
   // histogrammed once more over these fine bins, so that it splits in one
   // round rather than sending every crowded bin round the split again.  Fine
@@ -1159,7 +1166,7 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
   const uint32_t crowd = max(kCrowded, 4 * (m / nbins));
   bool crowded = false;
   for (uint32_t b = threadIdx.x; b < nbins; b += kThreads) crowded |= sm.hist[b] > crowd;
-  const bool refined = __syncthreads_or(crowded) && shift > 0;
+  const bool refined = __syncthreads_or(crowded) && shift > 0 && m >= kRefineMin;
   uint32_t* counts = sm.hist;  // bins the groups are formed from
   uint32_t nfine = nbins;
   if (refined) {

@@ -479,14 +479,21 @@ def test_split_refines_crowded_bins(mp, method):
     """Particles in Gaussian clusters with Morton keys (40-byte records):
     level-1 buckets hold dense cores beside sparse background, so split bins
     crowd; those bins are cut finer within the same split and the records
-    still come out in the stable order."""
+    still come out in the stable order.  32 level-1 buckets (a tuning
+    entry) make buckets of 250,000 records, large enough to be refined."""
     import torch
     import workloads as W
+    from mpsort import device
     n = 8_000_000
     buf, dt = W.particles_4(torch, n)
     a = buf.cpu().numpy().view(dt)
-    check(mp, a, 'key', method)
-    st = mp.last_stats()
+    device.tuning_set(n, dt, 'key', method, max_buckets=32)
+    try:
+        check(mp, a, 'key', "auto")
+        st = mp.last_stats()
+    finally:
+        device.tuning_clear()
+    assert st["method"] == method and st["nbuckets"] == 32, st
     assert st["splits"] > 0 and st["refined_splits"] > 0, st
 
 
