@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(1024) k_heavy_table(const uint64_t* __restrict
 // The weight word of `key` if the table holds it (its bucket in the low 14
 // bits), else 0.  probes: the table's longest probe sequence, 0 for an empty
 // or absent table.
-constexpr uint32_t kHeavyBucketMask = 0x3fffu;
+constexpr uint32_t kHeavyBucketMask = 0x3fffu;  // level-1 buckets are at most 8192 (k_finalize_splitters)
 __device__ __forceinline__ uint32_t heavy_lookup(const HeavyTable* t, uint32_t probes, uint64_t key) {
   const uint32_t h = heavy_hash(key);
   for (uint32_t j = 0; j < probes; ++j) {
@@ -1163,7 +1163,7 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
   // histogrammed once more over these fine bins, so that it splits in one
   // round rather than sending every crowded bin round the split again.  Fine
   // bins keep key order: those of bin b follow those of bin b - 1.
-  const uint32_t crowd = max(kCrowded, 4 * (m / nbins));
+  const uint32_t crowd = (uint32_t)max((unsigned long long)kCrowded, 4ull * (m / nbins));
   bool crowded = false;
   for (uint32_t b = threadIdx.x; b < nbins; b += kThreads) crowded |= sm.hist[b] > crowd;
   const bool refined = __syncthreads_or(crowded) && shift > 0 && m >= kRefineMin;
