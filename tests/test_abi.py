@@ -53,6 +53,29 @@ def test_key_descriptor_layout_matches_header(lib):
     assert ctypes.sizeof(L.Tuning) == 4 * 8
 
 
+def test_struct_fields_match_header_offsets(tmp_path):
+    """Every ctypes field of the Python binding sits at the offset the C
+    compiler gives the header's field of the same name."""
+    import mpsort._lib as L
+    pairs = [(L.Stats, "gbsort_stats"), (L.Tuning, "gbsort_tuning"), (L.KeyDesc, "gbsort_key_desc"),
+             (L.KeyWord, "gbsort_key_word")]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gbsort.h"', 'int main(void) {']
+    expect = []
+    for cls, cname in pairs:
+        lines.append('printf("%%zu\\n", sizeof(%s));' % cname)
+        expect.append(ctypes.sizeof(cls))
+        for f, _ in cls._fields_:
+            lines.append('printf("%%zu\\n", offsetof(%s, %s));' % (cname, f))
+            expect.append(getattr(cls, f).offset)
+    lines += ['return 0;', '}']
+    src, exe = tmp_path / "off.c", tmp_path / "off"
+    src.write_text("\n".join(lines) + "\n")
+    r = subprocess.run(["gcc", "-I", INCLUDE, str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    assert got == expect
+
+
 def test_key_desc_follows_binding_rules():
     import mpsort._lib as L
     dt = numpy.dtype([('a', 'u1'), ('k', 'i4'), ('v', ('u8', 2))], align=False)
