@@ -77,3 +77,29 @@ def test_layout_solver_brackets():
     recv = (GL_C[:T, 1:] - GL_C[:T, :-1]).sum(axis=0)
     assert (recv == numpy.diff(C)).all()
     assert (GL_C[:T] >= GL_CLT[:T]).all() and (GL_C[:T] <= GL_CLE[:T]).all()
+
+
+def test_cdf_oracle_gradient_matches_finite_differences():
+    """The NumPy model oracle (the checker of the device's forward and
+    backward kernels): its analytic gradient equals central differences of
+    its loss at every knot, for uniform, narrow and clustered keys."""
+    import cdf_oracle
+    rng = numpy.random.default_rng(17)
+    cases = ((5, rng.integers(0, 2**64, 3000, dtype=numpy.uint64, endpoint=False)),
+             (4, rng.integers(10**6, 10**6 + 700, 3000).astype(numpy.uint64)),
+             (6, (rng.normal(0, 1e9, 3000) + 2**62).astype(numpy.uint64)))
+    for lbits, keys in cases:
+        x = numpy.sort(keys)
+        y = numpy.sort(rng.random((1 << lbits) + 1))
+        y[0], y[-1] = 0.0, 1.0
+        kmin, kmax = int(x[0]), int(x[-1])
+        loss, pred, grad = cdf_oracle.forward_backward(x, kmin, kmax, lbits, y)
+        assert pred.shape == x.shape and grad.shape == y.shape
+        h = 1e-6
+        for j in range(len(y)):
+            yp, ym = y.copy(), y.copy()
+            yp[j] += h
+            ym[j] -= h
+            fd = (cdf_oracle.forward_backward(x, kmin, kmax, lbits, yp)[0] -
+                  cdf_oracle.forward_backward(x, kmin, kmax, lbits, ym)[0]) / (2 * h)
+            assert abs(fd - grad[j]) <= 1e-5 * max(abs(fd), 1e-3), (lbits, j, fd, grad[j])
