@@ -146,21 +146,39 @@ GBSORT_API int gbsort_debug_model(const uint64_t *sample, uint32_t s, int nbucke
 GBSORT_API int gbsort_debug_bisect(const uint64_t *sorted, uint32_t s, int nsplit, uint64_t *splitters,
                         int64_t *clt, int64_t *cle, uint32_t *rounds);
 
+/* Test of the bounded look-back wait of the LSD pass: one pass over n
+ * pseudo-random keys in which tile `withhold_tile` (of n / 4096) never
+ * publishes its counts, and every wait polls at most spin_limit times.
+ * Returns GBSORT_ERR_INTERNAL (message: the wait gave up) when a wait ran
+ * out, GBSORT_OK when none did (withhold_tile beyond the last tile).  The
+ * wait's limit in sorts is about a second.  No counterpart in the
+ * reference (its waits are MPI barriers). */
+GBSORT_API int gbsort_debug_lookback(uint32_t n, uint32_t withhold_tile, uint32_t spin_limit);
+
 /* Largest sort (nmemb * elsize bytes) gbsort_sort_device_noalloc accepts. */
 #define GBSORT_NOALLOC_MAX_BYTES (8u << 20)
 
 /* The histogram sort without any allocation, for callers that cannot call
- * cudaMalloc (a framework's caching allocator owns the memory budget, an
- * allocation would stall a latency-critical path, or running out of memory
- * half-way is not acceptable).  No counterpart in the reference, which
- * always allocates its temporaries.  Its scratch space is one fixed device
- * array inside libgbsort, held by every GPU that loads the library until
- * the process exits; sorts larger than GBSORT_NOALLOC_MAX_BYTES return
- * GBSORT_ERR_BAD_ARG.  Same layouts as the histogram sort (one-word key at a
- * 4-byte offset, 8-64 byte records); the result is the same stable order.
+ * cudaMalloc: code running inside a framework whose caching allocator owns
+ * the device memory budget, code on a latency-critical path where an
+ * allocation would synchronise the device, or code that must not run out
+ * of memory half-way.  No counterpart in the reference, which always
+ * allocates its temporaries.  Its scratch space is one fixed device array
+ * of 22 MiB inside libgbsort; sorts larger than GBSORT_NOALLOC_MAX_BYTES
+ * return GBSORT_ERR_BAD_ARG.  Same layouts as the histogram sort (one-word
+ * key at a 4-byte offset, 8-64 byte records); the result is the same stable
+ * order.
+ * Set-up: the CUDA driver creates the array on a GPU when it loads the
+ * library's device code there -- at context creation under eager module
+ * loading, else (lazy loading, CUDA's default) at the first call of this
+ * entry point on that GPU, which looks the array's address up with that GPU
+ * current.  That first call may therefore allocate device memory (the array,
+ * and the library's kernels if no other gbsort call has loaded them) and
+ * must not run while any thread captures a stream in global mode; every
+ * later call on that GPU allocates nothing.  The array then stays until the
+ * process exits.
  * All calls share the array and leave their data in it, so calls whose work
- * overlaps on the GPU race.  The first call on a device looks up the array's
- * address with that device current: make it before any stream capture.
+ * overlaps on the GPU (different streams or unordered host threads) race.
  * Waits for its work on `stream` to finish before returning. */
 GBSORT_API int gbsort_sort_device_noalloc(const void *d_in, void *d_out, size_t nmemb, size_t elsize,
                                           const gbsort_key_desc *key, void *stream);

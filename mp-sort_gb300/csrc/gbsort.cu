@@ -1148,6 +1148,43 @@ int gbsort_debug_bisect(const uint64_t* sorted, uint32_t s, int nsplit, uint64_t
   return GBSORT_OK;
 }
 
+int gbsort_debug_lookback(uint32_t n, uint32_t withhold_tile, uint32_t spin_limit) {
+  if (n == 0 || spin_limit == 0) return GBSORT_ERR_BAD_ARG;
+  Context* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  GB_CUDA(c->small.ensure((size_t)n * 16 + lsd_scratch_bytes(n, 1) + (1 << 16)));
+  Bump bump{c->small.as<uint8_t>()};
+  uint32_t* counters = bump.take<uint32_t>(CNT_WORDS);
+  uint64_t* kin = bump.take<uint64_t>(n);
+  uint64_t* kout = bump.take<uint64_t>(n);
+  uint32_t* hist = bump.take<uint32_t>(8 * 256);
+  uint32_t* starts = bump.take<uint32_t>(8 * 256);
+  unsigned long long* status = bump.take<unsigned long long>((size_t)lsd_tiles(n) * 256 + 1);
+  uint32_t* ticket = reinterpret_cast<uint32_t*>(status + (size_t)lsd_tiles(n) * 256);
+  uint32_t* err = counters + CNT_ERR;
+  cudaStream_t st = c->stream;
+  GB_CUDA(cudaMemsetAsync(counters, 0, CNT_WORDS * sizeof(uint32_t), st));
+  GB_CUDA(fill_hash(kin, (size_t)n * 8, 0x10cbac4ull, st));
+  GB_CUDA(lsd_digit_histograms(kin, n, 1, hist, st));
+  GB_CUDA(lsd_digit_starts(hist, 1, starts, st));
+  GB_CUDA(lsd_onesweep(kin, nullptr, kout, nullptr, n, 1, 0, 0, starts, status, ticket, err, st, spin_limit,
+                       withhold_tile));
+  uint32_t herr = 0;
+  GB_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  if (herr == DEV_ERR_TIMEOUT) {
+    set_err("a look-back wait gave up after %u polls (device code %u)", spin_limit, herr);
+    return GBSORT_ERR_INTERNAL;
+  }
+  if (herr) {
+    set_err("device check failed: code %u", herr);
+    return GBSORT_ERR_INTERNAL;
+  }
+  return GBSORT_OK;
+}
+
 namespace {
 // Trains the model on the sample for `epochs` steps and looks every key up
 // with the model (window search) and with the full search; see

@@ -44,9 +44,13 @@ uint32_t lsd_tiles(uint32_t n);
 // words (and idx, if not null) with offsets from starts (256 entries of this
 // digit) plus a decoupled look-back over the tiles; status and ticket are
 // scratch (zeroed here); err receives DEV_ERR_TIMEOUT if a wait gave up.
+// spin_limit: polls of one look-back wait before it gives up (0: about a
+// second's worth); withhold_tile: a tile that never publishes its counts
+// (tests of the bounded wait only; ~0u otherwise).
 cudaError_t lsd_onesweep(const uint64_t* keys_in, const uint32_t* idx_in, uint64_t* keys_out, uint32_t* idx_out,
                          uint32_t n, int nwords, int word, int shift, const uint32_t* starts,
-                         unsigned long long* status, uint32_t* ticket, uint32_t* err, cudaStream_t stream);
+                         unsigned long long* status, uint32_t* ticket, uint32_t* err, cudaStream_t stream,
+                         uint32_t spin_limit = 0, uint32_t withhold_tile = ~0u);
 // Pseudo-random contents for the first nbytes / 4 words of p (synthetic
 // inputs of the autotuner).
 cudaError_t fill_hash(void* p, size_t nbytes, uint64_t seed, cudaStream_t stream);

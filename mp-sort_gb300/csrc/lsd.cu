@@ -101,7 +101,8 @@ __global__ void __launch_bounds__(kThreads) k_lsd_onesweep(const uint64_t* __res
                                                             uint32_t* __restrict__ idx_out, uint32_t n, int word,
                                                             int shift, const uint32_t* __restrict__ starts,
                                                             unsigned long long* status, uint32_t* ticket,
-                                                            uint32_t* err) {
+                                                            uint32_t* err, uint32_t spin_limit,
+                                                            uint32_t withhold_tile) {
   using Rank = BlockRank<kLsdRpt, 8>;
   __shared__ uint16_t hist[Rank::kCounters];
   __shared__ uint32_t scan_tmp[kWarps];
@@ -151,16 +152,19 @@ __global__ void __launch_bounds__(kThreads) k_lsd_onesweep(const uint64_t* __res
     if (d == 255) cnt -= (uint32_t)kLsdTile - nvalid;
     unsigned long long* mine = status + (size_t)tile * 256 + d;
     unsigned long long excl = 0;
+    // withhold_tile (a test of the bounded wait) never publishes, so the
+    // next tile's wait runs out; it is ~0u in every sort
+    const bool publish = tile != withhold_tile;
     if (tile == 0) {
-      st_relaxed(mine, kStatPrefix | cnt);
+      if (publish) st_relaxed(mine, kStatPrefix | cnt);
     } else {
-      st_relaxed(mine, kStatAgg | cnt);
+      if (publish) st_relaxed(mine, kStatAgg | cnt);
       uint32_t j = tile - 1, spins = 0;
       for (;;) {
         const unsigned long long v = ld_relaxed(status + (size_t)j * 256 + d);
         const unsigned long long f = v & ~kStatValue;
         if (f == 0) {  // tile j has not published yet
-          if (++spins > kLookbackSpins) {
+          if (++spins > spin_limit) {
             set_error(err, DEV_ERR_TIMEOUT);
             break;
           }
@@ -171,7 +175,7 @@ __global__ void __launch_bounds__(kThreads) k_lsd_onesweep(const uint64_t* __res
         if (f == kStatPrefix || j == 0) break;
         --j;
       }
-      st_relaxed(mine, kStatPrefix | (excl + cnt));
+      if (publish) st_relaxed(mine, kStatPrefix | (excl + cnt));
     }
     base[d] = starts[d] + (uint32_t)excl - start[d];
   }
@@ -279,20 +283,23 @@ template <int NW, bool IDX>
 static cudaError_t launch_onesweep(const uint64_t* keys_in, const uint32_t* idx_in, uint64_t* keys_out,
                                    uint32_t* idx_out, uint32_t n, int word, int shift, const uint32_t* starts,
                                    unsigned long long* status, uint32_t* ticket, uint32_t* err,
-                                   cudaStream_t stream) {
+                                   uint32_t spin_limit, uint32_t withhold_tile, cudaStream_t stream) {
   const size_t smem = (size_t)NW * kLsdTile * 8 + (IDX ? (size_t)kLsdTile * 4 : 0);
   cudaError_t e = cudaFuncSetAttribute(k_lsd_onesweep<NW, IDX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
   k_lsd_onesweep<NW, IDX><<<lsd_tiles(n), kThreads, smem, stream>>>(keys_in, idx_in, keys_out, idx_out, n, word,
-                                                                     shift, starts, status, ticket, err);
+                                                                     shift, starts, status, ticket, err,
+                                                                     spin_limit, withhold_tile);
   return cudaGetLastError();
 }
 
 cudaError_t lsd_onesweep(const uint64_t* keys_in, const uint32_t* idx_in, uint64_t* keys_out, uint32_t* idx_out,
                          uint32_t n, int nwords, int word, int shift, const uint32_t* starts,
-                         unsigned long long* status, uint32_t* ticket, uint32_t* err, cudaStream_t stream) {
+                         unsigned long long* status, uint32_t* ticket, uint32_t* err, cudaStream_t stream,
+                         uint32_t spin_limit, uint32_t withhold_tile) {
   if (n == 0) return cudaSuccess;
+  if (spin_limit == 0) spin_limit = kLookbackSpins;
   const size_t words = (size_t)256 * lsd_tiles(n);
   cudaError_t e;
   if ((void*)ticket == (void*)(status + words)) {  // the usual layout: one clear for both
@@ -305,9 +312,9 @@ cudaError_t lsd_onesweep(const uint64_t* keys_in, const uint32_t* idx_in, uint64
 #define GB_LSD_CASE(NWV)                                                                                       \
   case NWV:                                                                                                    \
     e = idx_in ? launch_onesweep<NWV, true>(keys_in, idx_in, keys_out, idx_out, n, word, shift, starts, status,  \
-                                            ticket, err, stream)                                               \
+                                            ticket, err, spin_limit, withhold_tile, stream)                    \
                : launch_onesweep<NWV, false>(keys_in, idx_in, keys_out, idx_out, n, word, shift, starts,       \
-                                             status, ticket, err, stream);                                     \
+                                             status, ticket, err, spin_limit, withhold_tile, stream);          \
     break;
   switch (nwords) {
     GB_LSD_CASE(1)

@@ -8,7 +8,6 @@
 // half-way.  This entry point takes its scratch space (the two record
 // buffers and the small count / task / splitter arrays of the pipeline)
 // from one file-scope device array of fixed size instead of allocating it.
-// Every GPU that loads the library holds that array until the process exits.
 //
 // Limits and rules:
 //   * records * elsize <= GBSORT_NOALLOC_MAX_BYTES (8 MiB); larger sorts are
@@ -16,11 +15,16 @@
 //   * the plain (bisection) splitters are used; the result is the same
 //     stable order every other method produces;
 //   * all calls share the one array and each call leaves its contents
-//     behind: two calls whose work overlaps on the GPU (different streams,
-//     or different host threads without ordering) race on it;
-//   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture;
+//     behind (the counters are cleared at the start of every call): two
+//     calls whose work overlaps on the GPU (different streams, or different
+//     host threads without ordering) race on it;
+//   * set-up, once per device: the driver creates the array when it loads
+//     this file's device code on that device -- at context creation under
+//     eager module loading, else at the first cudaGetSymbolAddress below,
+//     made by the first call on that device with the device current.  That
+//     first call may allocate (the array, and the library's kernels if no
+//     other call loaded them) and must not run during a global-mode stream
+//     capture; later calls allocate nothing;
 //   * the call waits for the work on `stream` to finish (it reads the
 //     device-side consistency word back).
 #include <cuda_runtime.h>

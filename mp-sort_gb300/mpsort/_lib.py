@@ -87,6 +87,7 @@ SIGNATURES = {
     "gbsort_debug_buckets": (_I, [_P, _U32, _I, _P, _U32, _P, _P, _P, _P]),
     "gbsort_debug_model": (_I, [_P, _U32, _I, _I, _P, _U32, _P, _P, _P, _P, _P]),
     "gbsort_debug_bisect": (_I, [_P, _U32, _I, _P, _P, _P, _P]),
+    "gbsort_debug_lookback": (_I, [_U32, _U32, _U32]),
     "gbsort_plan_create": (_I, [_P, _SZ, _SZ, _P, _I]),
     "gbsort_plan_sort": (_I, [_P, _P, _P, _P]),
     "gbsort_plan_wait": (_I, [_P]),

@@ -3,7 +3,7 @@
 Run in a container where the MP-sort reference tree and its built library
 (``oracle/_ref/libref_omp.so``, from ``make -C oracle``) are available:
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py --reference <reference tree>
 
 Every expected output here is produced by the UNMODIFIED reference
 ``mpsort_omp`` and ``radix_sort`` (compiled from the reference sources),
@@ -61,7 +61,9 @@ def expect(arr, orderby):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="the MP-sort source tree")
+    ap.add_argument("--digests-only", action="store_true",
+                    help="rewrite digests.json only (golden.npz unchanged)")
     args = ap.parse_args()
     if O.ref_lib() is None:
         sys.exit("oracle/_ref/libref_omp.so is missing: run make -C oracle first")
@@ -160,8 +162,41 @@ def main():
     out["cb_issue7__out"] = omp
 
     path = os.path.join(HERE, "golden.npz")
-    numpy.savez_compressed(path, **out)
-    print("wrote", path, os.path.getsize(path), "bytes,", len(cases) + 2, "cases")
+    if not args.digests_only:
+        numpy.savez_compressed(path, **out)
+        print("wrote", path, os.path.getsize(path), "bytes,", len(cases) + 2, "cases")
+    write_digests()
+
+
+# Benchmark workloads too large to commit as vectors: the SHA-256 of the
+# unmodified reference's output (mpsort_omp, checked against radix_sort and
+# numpy's stable sort) on inputs that workloads.py regenerates bit for bit
+# from a seed, without a GPU.
+DIGEST_CASES = {
+    "cfg1_full": lambda W: (W.records_1(None), "key"),               # 1e6 x 12 B, PCG64 seed 0
+    "cfg2b_2e7": lambda W: (W.records_2_host(2 * 10**7, "2b"), "key"),  # sorted, 1 % swapped
+    "cfg2c_2e7": lambda W: (W.records_2_host(2 * 10**7, "2c"), "key"),  # Zipf(1.2) over 1e6 values
+}
+
+
+def write_digests():
+    import hashlib
+    import json
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    import workloads as W
+    dig = {}
+    for name, make in DIGEST_CASES.items():
+        arr, orderby = make(W)
+        ref = expect(arr, orderby)
+        dig[name] = {"n": len(arr), "dtype": str(arr.dtype.descr), "orderby": orderby,
+                     "sha256_in": hashlib.sha256(arr.tobytes()).hexdigest(),
+                     "sha256_out": hashlib.sha256(ref.tobytes()).hexdigest()}
+        print(name, dig[name]["sha256_out"])
+    path = os.path.join(HERE, "digests.json")
+    with open(path, "w") as f:
+        json.dump(dig, f, indent=1)
+        f.write("\n")
+    print("wrote", path)
 
 
 if __name__ == "__main__":

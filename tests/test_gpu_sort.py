@@ -624,3 +624,19 @@ def test_host_sort_pipelined_pinned(mp, method, dist, regions, monkeypatch):
         assert st["pipelined"] == 1 and (st["region_overflow"] == 0 or not regions), st
     mp.sort(hin, 'key', method=method)  # in place
     assert hin.tobytes() == exp.tobytes()
+
+
+# ----------------------------------------------- bounded look-back wait --
+def test_lookback_wait_runs_out_and_reports(mp):
+    """One LSD pass in which a tile never publishes its counts: the next
+    tile's look-back wait gives up after a few polls, the call returns
+    GBSORT_ERR_INTERNAL with the timeout message, and the device stays
+    usable (the same pass without the withheld tile, then a sort, succeed)."""
+    L = mp._lib.lib()
+    n = 8 * 4096
+    rc = L.gbsort_debug_lookback(n, 1, 64)
+    assert rc == mp._lib.ERR_INTERNAL
+    assert b"gave up" in L.gbsort_last_error()
+    assert L.gbsort_debug_lookback(n, 0xFFFFFFFF, 64) == 0
+    rng = numpy.random.default_rng(3)
+    check(mp, make([('key', 'u8'), ('val', 'i8')], 'key', 100_000, "uniform", rng), 'key', "lsd")

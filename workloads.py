@@ -72,6 +72,56 @@ def records_2(torch, n, dist, seed=1234):
     return rec.view(torch.uint8).view(-1), DT2
 
 
+def zipf_cdf_int(nv, bits=40):
+    """Cumulative integer weights of Zipf(s=1.2) over ranks 1..nv:
+    w_r = floor(2^bits * r^-1.2), computed exactly (the float estimate is
+    corrected by integer comparisons of w^5 r^6 against 2^(5 bits)), so the
+    table is the same on every machine -- no libm pow in the result."""
+    r = numpy.arange(1, nv + 1, dtype=numpy.float64)
+    w = numpy.floor(numpy.exp2(bits) * r ** -1.2).astype(numpy.int64)
+    top = 1 << (5 * bits)
+    out = numpy.empty(nv, dtype=numpy.int64)
+    for i in range(nv):
+        ri6 = (i + 1) ** 6
+        x = int(w[i])
+        while (x + 1) ** 5 * ri6 <= top:
+            x += 1
+        while x ** 5 * ri6 > top:
+            x -= 1
+        out[i] = x
+    return numpy.cumsum(out)
+
+
+def records_2_host(n, dist, seed=2):
+    """Configuration 2a / 2b / 2c keys as a numpy record array (PCG64
+    seeded, val = index): the host-side twin of keys_2, reproducible
+    without a GPU, so that the reference's CPU build can sort the very
+    same input."""
+    rng = numpy.random.Generator(numpy.random.PCG64(seed))
+    a = numpy.empty(n, DT2)
+    if dist in ("uniform", "2a"):
+        a['key'] = rng.integers(0, 2**64, n, dtype=numpy.uint64, endpoint=False)
+    elif dist in ("sorted1pct", "2b"):
+        k = numpy.arange(n, dtype=numpy.uint64)
+        m = n // 100
+        i = rng.integers(0, n, m)
+        j = rng.integers(0, n, m)
+        ki, kj = k[i].copy(), k[j].copy()
+        k[i] = kj
+        k[j] = ki
+        a['key'] = k
+    elif dist in ("zipf", "2c"):
+        nv = 10**6
+        cdf = zipf_cdf_int(nv)
+        vals = rng.integers(0, 2**64, nv, dtype=numpy.uint64, endpoint=False)
+        u = rng.integers(0, int(cdf[-1]), n, dtype=numpy.int64)
+        a['key'] = vals[numpy.searchsorted(cdf, u, side='right')]
+    else:
+        raise ValueError(dist)
+    a['val'] = numpy.arange(n)
+    return a
+
+
 def records_1(torch, n=10**6, seed=0):
     rng = numpy.random.Generator(numpy.random.PCG64(seed))
     a = numpy.empty(n, DT1)
@@ -165,3 +215,48 @@ def snapshots_5(torch, n=256 * 10**6, seed=5):
     recs[:, 2] = torch.rand(len(ids), device="cuda", generator=g).view(torch.int32)
     recs[:, 3] = torch.randint(0, 10**6, (len(ids),), device="cuda", generator=g, dtype=torch.int32)
     return recs.view(torch.uint8).view(-1), DT5, len(ia), len(ib), len(keep)
+
+
+def device_parity(torch, rec, out, n, key_col=0, ident_col=1, segment_start=None, signed=False):
+    """Size-independent parity of a sort of records whose `ident_col` word
+    holds the input index (integer tensors of shape (n, words) on the device,
+    input `rec` and output `out`):
+      key_payload  out[i].key == rec[out[i].ident].key for every i (each
+                   output record is the input record it names), and the
+                   record stayed in its segment;
+      permutation  every input index appears exactly once;
+      sorted       keys ascend (within each segment, if segment_start is a
+                   bool mask of segment first positions);
+      stable       equal keys keep ascending input index.
+    Together these pin the unique stable order record for record.  Keys are
+    compared as unsigned (signed=False: int64 words flipped into int64
+    order) or as signed integers."""
+    step = 1 << 27
+    ok_kp = ok_sorted = ok_stable = True
+    seen = torch.zeros(n, dtype=torch.int32, device=rec.device)
+    seg_id = None
+    if segment_start is not None:
+        seg_id = torch.cumsum(segment_start.to(torch.int32), 0, dtype=torch.int32)
+    for s in range(0, n, step):
+        e = min(n, s + step)
+        ident = out[s:e, ident_col].long()
+        if bool(((ident < 0) | (ident >= n)).any().item()):
+            return {"key_payload": False, "permutation": False, "sorted": False, "stable": False}
+        ok_kp &= bool(torch.equal(out[s:e, key_col], rec[ident, key_col]))
+        if seg_id is not None:
+            ok_kp &= bool(torch.equal(seg_id[ident], seg_id[s:e]))
+        seen.index_add_(0, ident, torch.ones_like(ident, dtype=torch.int32))
+        e1 = min(n, e + 1)
+        k = out[s:e1, key_col]
+        if not signed:
+            k = k ^ (-2**63)
+        up = k[1:] >= k[:-1]
+        tie_ok = (k[1:] != k[:-1]) | (out[s + 1:e1, ident_col] > out[s:e1 - 1, ident_col])
+        if segment_start is not None:
+            first = segment_start[s + 1:e1]
+            up |= first
+            tie_ok |= first
+        ok_sorted &= bool(up.all().item())
+        ok_stable &= bool(tie_ok.all().item())
+    ok_perm = bool((seen == 1).all().item())
+    return {"key_payload": ok_kp, "permutation": ok_perm, "sorted": ok_sorted, "stable": ok_stable}
