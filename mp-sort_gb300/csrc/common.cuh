@@ -107,6 +107,53 @@ __device__ __forceinline__ uint64_t key_from_regs(const uint32_t (&r)[E_WORDS], 
 
 __device__ __forceinline__ int bitlen64(uint64_t x) { return x ? 64 - __clzll(x) : 0; }
 
+// ---------------------------------------------------------------------------
+// Bulk asynchronous copies global -> shared memory (cp.async.bulk, the
+// untiled TMA form) completing on an mbarrier.  Addresses and sizes are
+// multiples of 16 bytes.  Waits are bounded: a wait that runs out returns
+// false and the caller records DEV_ERR_TIMEOUT.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+// Makes initialised mbarriers visible to the async proxy (before a barrier).
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// Orders this thread's earlier shared-memory accesses before later async
+// copies into the same memory.
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// One arrival that also expects `bytes` of transaction, then the copy.
+__device__ __forceinline__ void bulk_load(void* dst_smem, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst_smem)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{ .reg .pred p; mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for the completion of the mbarrier phase of the given parity, polling
+// at most `limit` times with a short back-off; false if it ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i) {
+    if (mbar_test(bar, parity)) return true;
+    __nanosleep(i < 64 ? 20 : 200);
+  }
+  return mbar_test(bar, parity);
+}
+constexpr uint32_t kBulkWaitPolls = 1u << 22;  // about a second of polling
+
 // Block-wide exclusive scan of one value per thread (NT threads).
 // `tmp` holds NT / 32 entries.  Returns the exclusive prefix; *total gets the sum.
 template <typename T, int NT = kThreads>

@@ -121,6 +121,9 @@ enum CounterSlot : int {
   CNT_WORDS = 64
 };
 
+// Bytes past the records of each scratch buffer: the staged local sorts copy
+// a task's byte range rounded out to 16 bytes.
+constexpr size_t kScratchSlack = 256;
 constexpr int kMaxPieces = 16;  // host -> device pieces of a pipelined host sort
 // Reserved bucket regions of the pipelined host sort.  A bucket holding c
 // of the s sampled keys gets (c + 5 sqrt(c + 1) + 10) * n / s records plus
@@ -519,8 +522,8 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
     if (region_fit) a_cap64 = (uint64_t)reserved;
   }
   const uint32_t a_cap = (uint32_t)std::max<uint64_t>(a_cap64, n);
-  GB_CUDA(c.A.ensure((size_t)a_cap * elsize));
-  GB_CUDA(c.B.ensure((size_t)n * elsize));
+  GB_CUDA(c.A.ensure((size_t)a_cap * elsize + kScratchSlack));
+  GB_CUDA(c.B.ensure((size_t)n * elsize + kScratchSlack));
   const uint32_t cap_split = (uint32_t)nb + n / 4096 + 4096;
   const uint32_t cap_local = 4u * (uint32_t)nb + n / 512 + 65536;
   const int lbits = 11;
@@ -1020,8 +1023,8 @@ int gbsort_sort_segments_device(const void* d_in, void* d_out, const uint64_t* s
     nbig += b - a;
   }
   if (nbig == n) return GBSORT_OK;
-  GB_CUDA(c->A.ensure((size_t)N * E));
-  GB_CUDA(c->B.ensure((size_t)N * E));
+  GB_CUDA(c->A.ensure((size_t)N * E + kScratchSlack));
+  GB_CUDA(c->B.ensure((size_t)N * E + kScratchSlack));
   const uint32_t cap_split = (uint32_t)nseg * 2 + N / 4096 + 4096;
   const uint32_t cap_local = 4u * (uint32_t)nseg + N / 512 + 65536;
   GB_CUDA(c->small.ensure(Level2::bytes(cap_split, cap_local) + (nseg + 1) * 8 + (1 << 20)));

@@ -36,9 +36,13 @@ namespace {
 #ifndef GB_LOCAL_CTAS
 #define GB_LOCAL_CTAS 3
 #endif
+#ifndef GB_STAGED_THREADS
+#define GB_STAGED_THREADS 512
+#endif
 constexpr int kLocalMax = GB_LOCAL_MAX;          // records a local sort holds in shared memory
 constexpr int kLocalThreads = GB_LOCAL_THREADS;  // threads of a local-sort CTA
 constexpr int kLocalCtasPerSm = GB_LOCAL_CTAS;
+constexpr int kStagedThreads = GB_STAGED_THREADS;  // threads of a staged local-sort CTA (two per SM)
 // Three CTAs per SM give 80 registers a thread: the local sort's pass calls
 // then need almost no stack (at four CTAs, 64 registers, the saves around
 // every call doubled the kernel's L2 stores; 1e9 x 16 B: 14.1 against 15.2
@@ -884,9 +888,8 @@ __device__ __forceinline__ void block_minmax(uint64_t& mn, uint64_t& mx, uint64_
 // put back in input order; indices are distinct and below kLocalMax).
 // PACKED: the keys are ((key - min) << kLocalBits) | input index, distinct
 // and ordered as (key, index); the index arrays are not used.
-template <int NT, bool PACKED>
-__device__ __noinline__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint32_t s, uint64_t mn, uint64_t mx,
-                               bool by_idx) {
+template <int NT, bool PACKED, typename SM>
+__device__ __noinline__ void local_msd_pass(SM& sm, uint32_t a, uint32_t s, uint64_t mn, uint64_t mx, bool by_idx) {
   constexpr int kBins = 1 << kLocalBits;
   constexpr int PER = kLocalMax / NT;
   static_assert(kLocalMax <= kBins, "input indices must fit the bins");
@@ -899,7 +902,8 @@ __device__ __noinline__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint
   for (int r = 0; r < PER; ++r) {
     const uint32_t e = r * NT + threadIdx.x;
     if (e < s) {
-      bin[r] = !PACKED && by_idx ? (uint32_t)sm.idxA[a + e] : (uint32_t)((sm.keyA[a + e] - mn) >> shift);
+      if constexpr (PACKED) bin[r] = (uint32_t)((sm.keyA[a + e] - mn) >> shift);
+      else bin[r] = by_idx ? (uint32_t)sm.idxA[a + e] : (uint32_t)((sm.keyA[a + e] - mn) >> shift);
       slot[r] = atomicAdd(&sm.cnt[bin[r]], 1u);
     }
   }
@@ -927,13 +931,14 @@ __device__ __noinline__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint
     if (e < s) {
       const uint32_t pos = sm.cnt[bin[r]] + slot[r];
       sm.keyB[a + pos] = sm.keyA[a + e];
-      if (!PACKED) sm.idxB[a + pos] = sm.idxA[a + e];
+      if constexpr (!PACKED) sm.idxB[a + pos] = sm.idxA[a + e];
     }
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < s; i += NT) {
     const uint64_t kv = sm.keyB[a + i];
-    const uint16_t iv = PACKED ? 0 : sm.idxB[a + i];
+    uint16_t iv = 0;
+    if constexpr (!PACKED) iv = sm.idxB[a + i];
     const uint32_t d = !PACKED && by_idx ? (uint32_t)iv : (uint32_t)((kv - mn) >> shift);
     const uint32_t b0 = sm.cnt[d], b1 = sm.cnt[d + 1];
     const uint32_t sz = b1 - b0;
@@ -942,7 +947,7 @@ __device__ __noinline__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint
       uint32_t r = 0;
       for (uint32_t j = b0; j < b1; ++j) {
         const uint64_t kj = sm.keyB[a + j];
-        if (PACKED) r += kj < kv;
+        if constexpr (PACKED) r += kj < kv;
         else r += (kj < kv) || (kj == kv && sm.idxB[a + j] < iv);
       }
       at = b0 + r;
@@ -952,14 +957,14 @@ __device__ __noinline__ void local_msd_pass(LocalSmemT<NT>& sm, uint32_t a, uint
       sm.bigsz[q] = (uint16_t)sz;
     }
     sm.keyA[a + at] = kv;
-    if (!PACKED) sm.idxA[a + at] = iv;
+    if constexpr (!PACKED) sm.idxA[a + at] = iv;
   }
   __syncthreads();
 }
 
 // Further passes over the bins too large to place by counting.
-template <int NT, bool PACKED>
-__device__ void local_big_bins(LocalSmemT<NT>& sm, uint32_t* stats) {
+template <int NT, bool PACKED, typename SM>
+__device__ void local_big_bins(SM& sm, uint32_t* stats) {
   for (;;) {
     uint32_t nb = sm.nbig;
     __syncthreads();
@@ -1058,6 +1063,256 @@ __device__ void local_sort(LocalSmemT<NT>& sm, const uint8_t* src, uint8_t* dst,
     }
   }
   __syncthreads();
+}
+
+// ------------------------------------------------ staged local sorts ----
+// Records of up to 16 bytes: a task's records come into shared memory with
+// one bulk asynchronous copy, issued while the previous task sorts (two
+// buffers), so no thread waits on DRAM; keys are read there, sorted as
+// packed words ((key - min) << 11 | input index, distinct and ordered as
+// (key, index)), and the records leave in sorted order by coalesced stores.
+// Without index arrays the shared memory of two CTAs per SM holds both
+// buffers: a task whose key range is wider than the 53 bits a packed word
+// keeps is packed by its top 53 bits and runs of equal prefixes are sorted
+// again by their full keys (local_refine_runs).
+template <int NT>
+struct LocalSmemP {
+  static constexpr int kNW = NT / 32;
+  static constexpr int kLongRuns = kLocalMax / (kInsertMax + 1) + 2;
+  uint64_t keyA[kLocalMax];  // packed keys (sorted order at the end)
+  uint64_t keyB[kLocalMax];
+  uint32_t cnt[(1 << kLocalBits) + 1];
+  uint16_t big[kLongRuns];  // pending bins of the MSD passes
+  uint16_t bigsz[kLongRuns];
+  uint16_t run[kLongRuns];  // long runs of equal prefixes (wide key ranges)
+  uint16_t runsz[kLongRuns];
+  uint32_t nbig, nrun;
+  uint64_t red[2 * kNW];
+  uint32_t scan_tmp[kNW];
+  uint32_t task_id[2], pend_staged;
+  SortTask task[2];  // the current task and the next one, alternating
+  uint64_t bar[2];   // completion of the two record buffers' copies
+};
+// One record buffer: kLocalMax records plus the 16-byte rounding of a start.
+template <int EW>
+__host__ __device__ constexpr uint32_t staged_buf_bytes() {
+  return (uint32_t)((kLocalMax * EW * 4 + 32 + 127) & ~127);
+}
+template <int EW, int NT>
+constexpr size_t staged_smem_bytes() {
+  return 2 * (size_t)staged_buf_bytes<EW>() + sizeof(LocalSmemP<NT>);
+}
+
+// Runs of equal packed prefixes (keys that differ only in the bits dropped
+// from a wide range) put back in (full key, index) order: short runs by one
+// thread's insertion sort, long ones re-packed relative to their own least
+// key (they differ only in the dropped bits, at most kLocalBits of them)
+// and sorted by the MSD pass.
+template <int EW, int NT>
+__device__ __noinline__ void local_refine_runs(LocalSmemP<NT>& sm, const uint8_t* rb, uint32_t m,
+                                               const gbsort_key_word& kw, uint32_t* stats) {
+  constexpr uint32_t E = EW * 4;
+  constexpr uint64_t kIdx = kLocalMax - 1;
+  bool any = false;
+  for (uint32_t i = threadIdx.x; i + 1 < m; i += NT) any |= (sm.keyA[i] >> kLocalBits) == (sm.keyA[i + 1] >> kLocalBits);
+  if (!__syncthreads_or(any)) return;
+  if (threadIdx.x == 0) sm.nrun = 0;
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < m; i += NT) {
+    // the prefix is the same for every member of a run, whatever order
+    // another thread's insertion sort has them in
+    const uint64_t pre = sm.keyA[i] >> kLocalBits;
+    if (i > 0 && (sm.keyA[i - 1] >> kLocalBits) == pre) continue;
+    uint32_t len = 1;
+    while (i + len < m && (sm.keyA[i + len] >> kLocalBits) == pre) ++len;
+    if (len == 1) continue;
+    if (len <= (uint32_t)kInsertMax) {
+      for (uint32_t a = i + 1; a < i + len; ++a) {
+        const uint64_t v = sm.keyA[a];
+        const uint32_t vi = (uint32_t)(v & kIdx);
+        const uint64_t vk = load_key_aligned4(rb + (size_t)vi * E, kw);
+        uint32_t b = a;
+        while (b > i) {
+          const uint64_t u = sm.keyA[b - 1];
+          const uint32_t ui = (uint32_t)(u & kIdx);
+          const uint64_t uk = load_key_aligned4(rb + (size_t)ui * E, kw);
+          if (uk < vk || (uk == vk && ui < vi)) break;
+          sm.keyA[b] = u;
+          --b;
+        }
+        sm.keyA[b] = v;
+      }
+    } else {
+      const uint32_t q = atomicAdd(&sm.nrun, 1u);
+      sm.run[q] = (uint16_t)i;
+      sm.runsz[q] = (uint16_t)len;
+    }
+  }
+  __syncthreads();
+  for (;;) {
+    const uint32_t nr = sm.nrun;
+    __syncthreads();
+    if (nr == 0) break;
+    const uint32_t a = sm.run[nr - 1], s = sm.runsz[nr - 1];
+    __syncthreads();
+    if (threadIdx.x == 0) sm.nrun = nr - 1;
+    uint64_t rmn = ~0ull, rmx = 0;
+    for (uint32_t e = threadIdx.x; e < s; e += NT) {
+      const uint64_t kk = load_key_aligned4(rb + (size_t)(sm.keyA[a + e] & kIdx) * E, kw);
+      rmn = kk < rmn ? kk : rmn;
+      rmx = kk > rmx ? kk : rmx;
+    }
+    block_minmax<NT>(rmn, rmx, sm.red);
+    for (uint32_t e = threadIdx.x; e < s; e += NT) {
+      const uint64_t v = sm.keyA[a + e];
+      const uint64_t kk = load_key_aligned4(rb + (size_t)(v & kIdx) * E, kw);
+      sm.keyA[a + e] = ((kk - rmn) << kLocalBits) | (v & kIdx);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(stats + STAT_BIGBIN, 1u);
+    local_msd_pass<NT, true>(sm, a, s, 0, ((rmx - rmn) << kLocalBits) | kIdx, false);
+    local_big_bins<NT, true>(sm, stats);
+  }
+}
+
+// In-place exclusive scan of the 2^kLocalBits bin counts of a staged local
+// sort (cnt[kBins] receives the total), one barrier inside; the caller
+// synchronises before reading the result.
+template <int NT>
+__device__ __forceinline__ void scan_local_bins(uint32_t* cnt, uint32_t* wtot) {
+  constexpr int kBins = 1 << kLocalBits;
+  constexpr int BPT = kBins / NT;
+  const uint32_t lane = lane_id(), w = warp_id();
+  uint32_t loc[BPT], sum = 0;
+#pragma unroll
+  for (int i = 0; i < BPT; ++i) {
+    loc[i] = cnt[threadIdx.x * BPT + i];
+    sum += loc[i];
+  }
+  uint32_t x = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(GB_FULL_MASK, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) wtot[w] = x;
+  __syncthreads();
+  uint32_t pre = x - sum;
+  for (uint32_t q = 0; q < w; ++q) pre += wtot[q];
+#pragma unroll
+  for (int i = 0; i < BPT; ++i) {
+    cnt[threadIdx.x * BPT + i] = pre;
+    pre += loc[i];
+  }
+  if (threadIdx.x == NT - 1) cnt[kBins] = pre;
+}
+
+// Stable sort of m <= kLocalMax records held in shared memory at rb into
+// dst (global memory).  The keys lie in [lo, hi], the task's range, which
+// fixes the packing without a reduction: a key's packed word is
+// ((key - lo) >> drop) << kLocalBits | its input index, and its bin the
+// word's top kLocalBits bits.  One pass places every word in its bin (a
+// slot by a shared-memory atomic), each word of a bin of up to kInsertMax
+// counts the smaller words of its bin -- distinct words, so this is the
+// stable (key, index) order -- and its record goes straight to that output
+// position; larger bins take further MSD passes, and a range wider than a
+// packed word (drop > 0) is finished by local_refine_runs before any record
+// leaves.  cnt is zero on entry and on return.
+template <int EW, int NT>
+__device__ void local_sort_staged(LocalSmemP<NT>& sm, const uint8_t* rb, uint8_t* dst, uint32_t m, uint64_t lo,
+                                  uint64_t hi, const gbsort_key_word& kw, uint32_t* stats, uint32_t* err) {
+  constexpr int PER = kLocalMax / NT;
+  constexpr int kBins = 1 << kLocalBits;
+  constexpr uint32_t E = EW * 4;
+  constexpr uint64_t kIdx = kLocalMax - 1;
+  using V = typename std::conditional<EW % 4 == 0, uint4,
+                                      typename std::conditional<EW % 2 == 0, uint2, uint32_t>::type>::type;
+  constexpr uint32_t VPR = E / sizeof(V);
+  auto put = [&](uint32_t at, uint32_t from) {  // record `from` of rb to output position `at`
+#pragma unroll
+    for (uint32_t q = 0; q < VPR; ++q)
+      reinterpret_cast<V*>(dst + (size_t)at * E)[q] = reinterpret_cast<const V*>(rb + (size_t)from * E)[q];
+  };
+  const uint64_t range = hi - lo;
+  const int rbits = bitlen64(range);
+  const int drop = rbits > 64 - kLocalBits ? rbits - (64 - kLocalBits) : 0;
+  const int pbits = bitlen64(((range >> drop) << kLocalBits) | kIdx);
+  const int shift = pbits > kLocalBits ? pbits - kLocalBits : 0;
+  uint64_t pk[PER];
+  uint32_t bin[PER], slot[PER];
+  bool bad = false;
+#pragma unroll
+  for (int r = 0; r < PER; ++r) {
+    const uint32_t e = r * NT + threadIdx.x;
+    if (e < m) {
+      const uint64_t k = load_key_aligned4(rb + (size_t)e * E, kw);
+      bad |= k < lo || k > hi;
+      const uint64_t off = k < lo ? 0 : (k > hi ? range : k - lo);
+      pk[r] = ((off >> drop) << kLocalBits) | e;
+      bin[r] = (uint32_t)(pk[r] >> shift);
+      slot[r] = atomicAdd(&sm.cnt[bin[r]], 1u);
+    }
+  }
+  if (bad) set_error(err, DEV_ERR_COUNT_MISMATCH);  // a key outside its task's range (never expected)
+  if (threadIdx.x == 0) sm.nbig = 0;
+  __syncthreads();
+  scan_local_bins<NT>(sm.cnt, sm.scan_tmp);
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < PER; ++r) {
+    const uint32_t e = r * NT + threadIdx.x;
+    if (e < m) sm.keyB[sm.cnt[bin[r]] + slot[r]] = pk[r];
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < m; i += NT) {
+    const uint64_t v = sm.keyB[i];
+    const uint32_t d = (uint32_t)(v >> shift);
+    const uint32_t b0 = sm.cnt[d], b1 = sm.cnt[d + 1];
+    if (b1 - b0 > (uint32_t)kInsertMax) {  // a crowded bin: further passes below
+      if (i == b0) {
+        const uint32_t q = atomicAdd(&sm.nbig, 1u);
+        sm.big[q] = (uint16_t)b0;
+        sm.bigsz[q] = (uint16_t)(b1 - b0);
+      }
+      sm.keyA[i] = v;
+      continue;
+    }
+    uint32_t at = i;
+    if (b1 - b0 > 1) {
+      uint32_t r = 0;
+      for (uint32_t j = b0; j < b1; ++j) r += sm.keyB[j] < v;
+      at = b0 + r;
+    }
+    if (drop) sm.keyA[at] = v;
+    else put(at, (uint32_t)(v & kIdx));
+  }
+  __syncthreads();
+  const uint32_t nb = sm.nbig;
+  if (nb) {  // crowded bins (clustered keys): MSD passes over their packed words in keyA
+    if (!drop)
+      for (uint32_t q = threadIdx.x; q < nb; q += NT) {
+        sm.run[q] = sm.big[q];
+        sm.runsz[q] = sm.bigsz[q];
+      }
+    __syncthreads();
+    local_big_bins<NT, true>(sm, stats);
+    if (!drop) {  // their records, now in order
+      for (uint32_t q = 0; q < nb; ++q) {
+        const uint32_t a = sm.run[q], s = sm.runsz[q];
+        for (uint32_t i = threadIdx.x; i < s; i += NT) put(a + i, (uint32_t)(sm.keyA[a + i] & kIdx));
+      }
+    }
+  }
+  if (drop) {  // a range wider than a packed word: equal prefixes sorted by full keys, then every record
+    local_refine_runs<EW, NT>(sm, rb, m, kw, stats);
+    for (uint32_t f = threadIdx.x; f < m * VPR; f += NT) {
+      const uint32_t i = f / VPR;
+      const uint32_t from = (uint32_t)(sm.keyA[i] & kIdx);
+      reinterpret_cast<V*>(dst)[f] = reinterpret_cast<const V*>(rb + (size_t)from * E)[f % VPR];
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i <= kBins; i += NT) sm.cnt[i] = 0;  // zero for the next task
 }
 
 // Fine bins of a split with refined (crowded) bins: cm[b] = first fine bin
@@ -1460,6 +1715,91 @@ __global__ void __launch_bounds__(NT, local_ctas_per_sm<EW>()) k_local(HsortPara
   }
 }
 
+// Local sorts of records up to 16 bytes, two CTAs per SM.  Thread 0 claims
+// the next task while the current one sorts and, if it is a sort task,
+// starts the bulk copy of its records into the other buffer; copy tasks and
+// single records go straight from global memory to the output.  Task
+// descriptors alternate between two shared slots, so one barrier per task
+// separates a claim from its use.  A copy whose wait runs out (about a
+// second) records DEV_ERR_TIMEOUT; the CTA then waits once more (bounded)
+// for the copies it has in flight and stops.
+template <int EW, int NT>
+__global__ void __launch_bounds__(NT, 2) k_local_staged(HsortParams p, const SortTask* __restrict__ tasks,
+                                                         const uint32_t* __restrict__ ntasks, uint32_t cap,
+                                                         uint32_t* __restrict__ work, uint32_t* __restrict__ stats) {
+  constexpr uint32_t E = EW * 4;
+  constexpr uint32_t kBuf = staged_buf_bytes<EW>();
+  extern __shared__ __align__(128) uint8_t smem_raw[];
+  uint8_t* rbuf = smem_raw;  // [2][kBuf]
+  LocalSmemP<NT>& sm = *reinterpret_cast<LocalSmemP<NT>*>(smem_raw + 2 * kBuf);
+  uint32_t* err = stats + STAT_SLOTS;
+  const uint32_t nt = min(*ntasks, cap);
+  auto staged = [](const SortTask& t) { return !(t.flags & TASK_COPY) && t.count > 1 && t.count <= (uint32_t)kLocalMax; };
+  auto source = [&](const SortTask& t) { return ((t.flags & TASK_SRC_B) ? p.bufB : p.bufA) + (size_t)t.from * E; };
+  // the task's byte range rounded out to 16 bytes (the slack lies inside
+  // the scratch allocations) into buffer `slot`
+  auto issue = [&](const SortTask& t, int slot) {
+    const uintptr_t a = (uintptr_t)source(t);
+    const uintptr_t a0 = a & ~(uintptr_t)15;
+    const uint32_t bytes = (uint32_t)(((a - a0) + (uintptr_t)t.count * E + 15) & ~(uintptr_t)15);
+    bulk_load(rbuf + (size_t)slot * kBuf, (const void*)a0, bytes, &sm.bar[slot]);
+  };
+  for (int i = threadIdx.x; i <= (1 << kLocalBits); i += NT) sm.cnt[i] = 0;
+  if (threadIdx.x == 0) {
+    mbar_init(&sm.bar[0], 1);
+    mbar_init(&sm.bar[1], 1);
+    mbar_init_fence();
+    const uint32_t id = atomicAdd(work, 1u);
+    sm.task_id[0] = id;
+    if (id < nt) {
+      sm.task[0] = tasks[id];
+      if (staged(sm.task[0])) issue(sm.task[0], 0);
+    }
+  }
+  __syncthreads();
+  uint32_t parity = 0;  // bit s: parity of the next completion of buffer s
+  for (int it = 0;; ++it) {
+    const int slot = it & 1;  // buffer and descriptor slot of this task; the next one takes the other
+    const uint32_t t = sm.task_id[slot];
+    if (t >= nt) break;
+    const SortTask task = sm.task[slot];
+    if (threadIdx.x == 0) {
+      const uint32_t nid = atomicAdd(work, 1u);
+      uint32_t st = 0;
+      if (nid < nt) {
+        const SortTask nxt = tasks[nid];
+        sm.task[slot ^ 1] = nxt;
+        if (staged(nxt)) {
+          fence_proxy_async_smem();
+          issue(nxt, slot ^ 1);
+          st = 1;
+        }
+      }
+      sm.task_id[slot ^ 1] = nid;
+      sm.pend_staged = st;
+    }
+    uint8_t* out = p.out + (size_t)task.start * E;
+    if (!staged(task)) {
+      block_copy_ilp<EW>(source(task), out, task.count, NT);
+      if (threadIdx.x == 0) atomicAdd(stats + STAT_COPY, 1u);
+    } else {
+      bool ok = mbar_wait_bounded(&sm.bar[slot], (parity >> slot) & 1u, kBulkWaitPolls);
+      ok = __syncthreads_and(ok);
+      if (!ok) {  // stop: wait once more for this CTA's copies, then leave
+        if (threadIdx.x == 0) set_error(err, DEV_ERR_TIMEOUT);
+        mbar_wait_bounded(&sm.bar[slot], (parity >> slot) & 1u, kBulkWaitPolls);
+        if (sm.pend_staged) mbar_wait_bounded(&sm.bar[slot ^ 1], (parity >> (slot ^ 1)) & 1u, kBulkWaitPolls);
+        return;
+      }
+      parity ^= 1u << slot;
+      const uint8_t* rb = rbuf + (size_t)slot * kBuf + ((uintptr_t)source(task) & 15);
+      local_sort_staged<EW, NT>(sm, rb, out, task.count, task.lo, task.hi, p.key, stats, err);
+      if (threadIdx.x == 0) atomicAdd(stats + STAT_LOCAL, 1u);
+    }
+    __syncthreads();
+  }
+}
+
 // ------------------------------------------------------------ dispatch --
 template <typename F>
 bool dispatch_ew(uint32_t elsize, F&& f) {
@@ -1752,10 +2092,18 @@ cudaError_t run_local(const HsortParams& p, const SortTask* tasks, const uint32_
   if (e != cudaSuccess) return e;
   bool ok = dispatch_ew(p.elsize, [&](auto ewc) {
     constexpr int EW = decltype(ewc)::value;
-    size_t sm = sizeof(LocalSmemT<kLocalThreads>);
-    e = set_smem((const void*)k_local<EW>, sm);
-    if (e == cudaSuccess)
-      k_local<EW><<<local_grid<EW>(), kLocalThreads, sm, stream>>>(p, tasks, ntasks, cap, work_counter, stats);
+    if constexpr (EW <= 4) {  // records up to 16 bytes: staged in shared memory by bulk copies
+      const size_t sm = staged_smem_bytes<EW, kStagedThreads>();
+      e = set_smem((const void*)k_local_staged<EW, kStagedThreads>, sm);
+      if (e == cudaSuccess)
+        k_local_staged<EW, kStagedThreads><<<num_sms() * 2, kStagedThreads, sm, stream>>>(p, tasks, ntasks, cap,
+                                                                                           work_counter, stats);
+    } else {
+      const size_t sm = sizeof(LocalSmemT<kLocalThreads>);
+      e = set_smem((const void*)k_local<EW>, sm);
+      if (e == cudaSuccess)
+        k_local<EW><<<local_grid<EW>(), kLocalThreads, sm, stream>>>(p, tasks, ntasks, cap, work_counter, stats);
+    }
     note_launches(1);
   });
   if (!ok) return cudaErrorInvalidValue;
