@@ -4,8 +4,10 @@
  * Plain pointers and sizes only.  Every entry point returns a gbsort_status;
  * none of them aborts the process.  Device entry points take device
  * pointers and a cudaStream_t passed as `void *` (NULL = the library's own
- * stream of the current device) and return once the work is enqueued on
- * that stream, except where stated.  Host entry points copy to the current
+ * stream of the current device, a blocking stream: it orders after work
+ * issued earlier on the legacy default stream, as the legacy stream itself
+ * would) and return once the work is enqueued on that stream, except where
+ * stated.  Host entry points copy to the current
  * CUDA device, sort there, copy back and return when the result is in host
  * memory.
  *
@@ -75,11 +77,42 @@ typedef struct gbsort_stats {
                                     region reserved for it from the sample (level 1 was then redone) */
 } gbsort_stats;
 
+/* OR into `method`: hash the records (gbsort_multiset_hash_device) before
+ * and after the sort and return GBSORT_ERR_INTERNAL if the output is not a
+ * permutation of the input -- the reference's self-check
+ * (mpsort-mpi.c:148-159, 324-330).  The call then waits for the sort. */
+#define GBSORT_VERIFY 0x100
+
 /* Sort nmemb records of elsize bytes from d_in into d_out (device memory;
  * d_out may equal d_in).  `key` describes the radix; `method` a
- * gbsort_method.  Requires nmemb < 2^32. */
+ * gbsort_method, optionally with GBSORT_VERIFY.  nmemb is a full size_t
+ * (radixsort.c:35): below 2^32 records every layout is taken; from 2^32 on
+ * the records are first cut into at most 15 key ranges of under 2^32 each
+ * by one stable partition pass (64-bit offsets, scratch of nmemb * elsize
+ * bytes, host synchronisation between the stages), which needs a one-word
+ * key at a 4-byte offset and 8-64 byte records (else
+ * GBSORT_ERR_UNSUPPORTED) and at most about 2.2e10 records (else
+ * GBSORT_ERR_BAD_ARG). */
 GBSORT_API int gbsort_sort_device(const void *d_in, void *d_out, size_t nmemb, size_t elsize,
                        const gbsort_key_desc *key, int method, void *stream);
+
+/* out[i] = source[index[i]] for nindex records of elsize bytes (device
+ * memory; int64 indices): mpsort.take / mpsort.permute of one process
+ * (reference mpsort/__init__.py:116-204, which needs two or three sorts
+ * across MPI ranks to do the same).  Indices outside [0, nsource) are not
+ * read: the call returns GBSORT_ERR_BAD_ARG (message: the first such
+ * position).  Waits for the gather. */
+GBSORT_API int gbsort_take_device(const void *d_source, size_t nsource, size_t elsize, const int64_t *d_index,
+                                  size_t nindex, void *d_out, void *stream);
+
+/* Order-independent 64-bit hash of the multiset of nmemb records of elsize
+ * bytes (device memory): the sum, modulo 2^64, of a 64-bit mix of every
+ * record's bytes, written to *d_hash (device memory) on `stream`.  Equal
+ * multisets give equal hashes whatever their order; a changed, lost or
+ * duplicated record changes the hash except with probability about 2^-64.
+ * Replaces the reference's byte-sum checksum (mpsort-mpi.c:148-159). */
+GBSORT_API int gbsort_multiset_hash_device(const void *d_records, size_t nmemb, size_t elsize,
+                                           uint64_t *d_hash, void *stream);
 
 /* Same, for host memory: in and out may be equal.  Blocks until done. */
 GBSORT_API int gbsort_sort_host(const void *in, void *out, size_t nmemb, size_t elsize,

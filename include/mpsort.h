@@ -25,6 +25,7 @@
 #define GBSORT_MPSORT_H
 
 #include <stddef.h>
+#include <stdint.h>
 
 #include "gbsort_key.h"
 
@@ -59,6 +60,32 @@ GBSORT_API int mpsort_last_status(void);
 GBSORT_API void mpsort_mpi_set_options(int options);
 GBSORT_API int mpsort_mpi_has_options(int options);
 GBSORT_API void mpsort_mpi_unset_options(int options);
+
+/* One-process forms of the reference's MPI entry points (reference
+ * mpsort.h:26-47, mpsort-mpi.c:129-331), for callers that link against the
+ * MPI interface but run one rank per GPU.  The communicator is taken as an
+ * opaque integer and not read (the MPI_Comm handle of either common MPI
+ * ABI passes in one register; a multi-rank sort is outside this library).
+ * As in the reference with one rank, base ends sorted and out receives the
+ * sorted records (outnmemb must equal nmemb, else nothing is sorted and the
+ * status is GBSORT_ERR_BAD_ARG).  With mpsort_radix_desc the sort is
+ * self-checked by a multiset hash of the records before and after, as the
+ * reference checks its checksum.  Status: mpsort_last_status(). */
+GBSORT_API void mpsort_mpi_newarray_impl(void *base, size_t nmemb, void *out, size_t outnmemb, size_t elsize,
+                                         void (*radix)(const void *ptr, void *radix, void *arg),
+                                         size_t rsize, void *arg, intptr_t comm, int line, const char *file);
+GBSORT_API void mpsort_mpi_impl(void *base, size_t nmemb, size_t elsize,
+                                void (*radix)(const void *ptr, void *radix, void *arg),
+                                size_t rsize, void *arg, intptr_t comm, int line, const char *file);
+/* Prints the stage times of the last sort on this thread (reference
+ * mpsort.h:49). */
+GBSORT_API void mpsort_mpi_report_last_run(void);
+
+#define mpsort_mpi(base, nmemb, elsize, radix, rsize, arg, comm) \
+    mpsort_mpi_impl(base, nmemb, elsize, radix, rsize, arg, (intptr_t)(comm), __LINE__, __FILE__)
+#define mpsort_mpi_newarray(base, nmemb, out, outnmemb, elsize, radix, rsize, arg, comm) \
+    mpsort_mpi_newarray_impl(base, nmemb, out, outnmemb, elsize, radix, rsize, arg, (intptr_t)(comm), \
+                             __LINE__, __FILE__)
 
 #ifdef __cplusplus
 }

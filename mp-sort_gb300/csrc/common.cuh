@@ -154,6 +154,14 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 }
 constexpr uint32_t kBulkWaitPolls = 1u << 22;  // about a second of polling
 
+// Bulk prefetch into L2 of the 16-byte aligned part of [p, p + bytes).
+__device__ __forceinline__ void prefetch_l2_range(const void* p, uint32_t bytes) {
+  const uintptr_t a = ((uintptr_t)p + 15) & ~(uintptr_t)15;
+  const uintptr_t b = ((uintptr_t)p + bytes) & ~(uintptr_t)15;
+  if (b > a)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((uint32_t)(b - a)) : "memory");
+}
+
 // Block-wide exclusive scan of one value per thread (NT threads).
 // `tmp` holds NT / 32 entries.  Returns the exclusive prefix; *total gets the sum.
 template <typename T, int NT = kThreads>

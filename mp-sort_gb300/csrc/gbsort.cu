@@ -163,6 +163,8 @@ struct Context {
   DevBuf idxA, idxB;       // generic path permutation
   DevBuf small;            // splitters, counts, tasks, model, counters
   DevBuf radix;            // host radix bytes (callback path)
+  DevBuf part;             // first partition of sorts of 2^32 records or more
+  DevBuf vh;               // multiset hashes of a self-checked sort
   HostCounters* hc = nullptr;
   cudaEvent_t ev[8] = {};  // stage boundaries of the histogram sort
   cudaStream_t cstream = nullptr;                // copies of a pipelined host sort
@@ -176,10 +178,15 @@ struct Context {
 std::mutex g_ctx_mu;
 Context* g_ctx[64] = {};
 
-int ctx_init(Context& c, int dev) {
+// blocking: the library's own streams of a device (the `NULL` stream of the
+// device entry points) order after work on the legacy default stream, so a
+// caller's earlier kernels there (filling the input, say) finish first; a
+// graph plan's capture streams do not.
+int ctx_init(Context& c, int dev, bool blocking) {
   c.device = dev;
-  GB_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
-  GB_CUDA(cudaStreamCreateWithFlags(&c.cstream, cudaStreamNonBlocking));
+  const unsigned flags = blocking ? cudaStreamDefault : cudaStreamNonBlocking;
+  GB_CUDA(cudaStreamCreateWithFlags(&c.stream, flags));
+  GB_CUDA(cudaStreamCreateWithFlags(&c.cstream, flags));
   GB_CUDA(cudaMallocHost(&c.hc, sizeof(HostCounters)));
   for (cudaEvent_t& e : c.ev) GB_CUDA(cudaEventCreate(&e));
   for (cudaEvent_t& e : c.pev) GB_CUDA(cudaEventCreate(&e));
@@ -191,7 +198,7 @@ int ctx_init(Context& c, int dev) {
 
 void ctx_destroy(Context& c) {
   if (c.stream) cudaStreamSynchronize(c.stream);
-  DevBuf* bufs[] = {&c.A, &c.B, &c.hin, &c.hout, &c.keysA, &c.keysB, &c.idxA, &c.idxB, &c.small, &c.radix};
+  DevBuf* bufs[] = {&c.A, &c.B, &c.hin, &c.hout, &c.keysA, &c.keysB, &c.idxA, &c.idxB, &c.small, &c.radix, &c.part, &c.vh};
   for (DevBuf* b : bufs) b->release();
   if (c.cstream) cudaStreamSynchronize(c.cstream);
   for (cudaEvent_t& e : c.ev)
@@ -228,7 +235,7 @@ int get_ctx(Context** out) {
   std::lock_guard<std::mutex> lk(g_ctx_mu);
   if (!g_ctx[dev]) {
     Context* c = new Context();
-    int rc = ctx_init(*c, dev);
+    int rc = ctx_init(*c, dev, true);
     if (rc) {
       delete c;
       return rc;
@@ -822,10 +829,132 @@ int resolve_auto(uint32_t elsize, const gbsort_key_desc* key, uint64_t n, bool h
   return hs_ok && n > kAutoLsdMax ? GBSORT_HISTOGRAM_LEARNED : GBSORT_LSD;
 }
 
+// Sorts of 2^32 records or more (64-bit counts): the splitters of P - 1
+// sample quantiles cut the records into P key ranges of under 2^32 records
+// each (P <= 15, about 1.5e9 records per range), one stable partition pass
+// moves every range into its place in a scratch copy, and each range is
+// then sorted into the output by the 32-bit pipeline.  A range of one key
+// (a key owning 2^32 records or more) is copied, not sorted.  Synchronises
+// with the host between the stages.
+int run_partitioned(Context& c, const void* d_in, void* d_out, uint64_t n, uint32_t E, const gbsort_key_desc* key,
+                    int method, cudaStream_t st) {
+  constexpr uint64_t kPartTarget = 1500000000ull;
+  constexpr uint64_t kPartMax = 0xfffffffeull;
+  const int P = (int)std::min<uint64_t>(15, (n + kPartTarget - 1) / kPartTarget);
+  if ((uint64_t)P * kPartTarget * 2 < n) {
+    set_err("%llu records exceed the partitioned sort's range (about 2.2e10)", (unsigned long long)n);
+    return GBSORT_ERR_BAD_ARG;
+  }
+  const int nsplit = P - 1;
+  const uint32_t s = 1u << 20;
+  const int g = part_grid();
+  GB_CUDA(c.part.ensure((size_t)n * E + kScratchSlack));
+  GB_CUDA(c.small.ensure((size_t)s * 16 + lsd_scratch_bytes(s, 1) + (size_t)g * 16 * 12 + (1 << 16)));
+  Bump bump{c.small.as<uint8_t>()};
+  uint32_t* counters = bump.take<uint32_t>(CNT_WORDS);
+  uint32_t* err = counters + CNT_ERR;
+  uint64_t* sA = bump.take<uint64_t>(s);
+  uint64_t* sB = bump.take<uint64_t>(s);
+  uint64_t* S = bump.take<uint64_t>(16);
+  uint32_t* counts = bump.take<uint32_t>((size_t)16 * g);
+  unsigned long long* offs = bump.take<unsigned long long>((size_t)16 * g);
+  GB_CUDA(cudaMemsetAsync(counters, 0, CNT_WORDS * sizeof(uint32_t), st));
+  GB_CUDA(sample_keys64((const uint8_t*)d_in, n, E, key->word[0], s, sA, st));
+  int rc = lsd_sort_keys(bump, sA, sB, nullptr, nullptr, s, 1, false, nullptr, err, st);
+  if (rc) return rc;
+  GB_CUDA(plain_splitters(sA, s, nsplit, S, counters + CNT_ITERS, nullptr, nullptr, st));
+  GB_CUDA(finalize_splitters(S, nsplit, st));
+  GB_CUDA(part_count((const uint8_t*)d_in, n, E, key->word[0], S, nsplit, counts, st));
+  std::vector<uint32_t> hc((size_t)P * g);
+  std::vector<uint64_t> hS(16, 0);
+  uint32_t herr = 0;
+  GB_CUDA(cudaMemcpyAsync(hc.data(), counts, hc.size() * 4, cudaMemcpyDeviceToHost, st));
+  if (nsplit) GB_CUDA(cudaMemcpyAsync(hS.data(), S, (size_t)nsplit * 8, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  if (herr) {
+    set_err("device check failed in the partition's splitter search: code %u", herr);
+    return GBSORT_ERR_INTERNAL;
+  }
+  std::vector<unsigned long long> ho((size_t)P * g);
+  std::vector<uint64_t> pstart(P + 1, 0);
+  uint64_t run = 0;
+  for (int q = 0; q < P; ++q) {
+    pstart[q] = run;
+    for (int ch = 0; ch < g; ++ch) {
+      ho[(size_t)q * g + ch] = run;
+      run += hc[(size_t)q * g + ch];
+    }
+  }
+  pstart[P] = run;
+  if (run != n) {
+    set_err("partition counts %llu records of %llu", (unsigned long long)run, (unsigned long long)n);
+    return GBSORT_ERR_INTERNAL;
+  }
+  auto range_of = [&](int q, uint64_t& lo, uint64_t& hi) {
+    lo = q == 0 ? 0ull : hS[q - 1];
+    hi = q == nsplit ? ~0ull : hS[q] - 1;
+  };
+  for (int q = 0; q < P; ++q) {
+    uint64_t lo, hi;
+    range_of(q, lo, hi);
+    if (pstart[q + 1] - pstart[q] > kPartMax && lo != hi) {
+      set_err("a key range of the partition holds %llu records (2^32 or more) of more than one key",
+              (unsigned long long)(pstart[q + 1] - pstart[q]));
+      return GBSORT_ERR_UNSUPPORTED;
+    }
+  }
+  GB_CUDA(cudaMemcpyAsync(offs, ho.data(), ho.size() * 8, cudaMemcpyHostToDevice, st));
+  GB_CUDA(part_scatter((const uint8_t*)d_in, c.part.as<uint8_t>(), n, E, key->word[0], S, nsplit, offs, err, st));
+  GB_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  if (herr) {
+    set_err("device check failed in the partition scatter: code %u", herr);
+    return GBSORT_ERR_INTERNAL;
+  }
+  for (int q = 0; q < P; ++q) {
+    const uint64_t a = pstart[q], m = pstart[q + 1] - pstart[q];
+    if (m == 0) continue;
+    uint64_t lo, hi;
+    range_of(q, lo, hi);
+    const uint8_t* src = c.part.as<uint8_t>() + (size_t)a * E;
+    uint8_t* dst = (uint8_t*)d_out + (size_t)a * E;
+    if (lo == hi) {  // one key: the partition kept input order, which is the stable order
+      GB_CUDA(cudaMemcpyAsync(dst, src, (size_t)m * E, cudaMemcpyDeviceToDevice, st));
+      continue;
+    }
+    rc = sort_device_dispatch(c, src, dst, m, E, key, method, st);
+    if (rc) return rc;
+  }
+  GB_CUDA(cudaStreamSynchronize(st));
+  return GBSORT_OK;
+}
+
 int sort_device_locked(Context& c, const void* d_in, void* d_out, size_t nmemb, size_t elsize,
                        const gbsort_key_desc* key, int method, cudaStream_t st) {
   const unsigned long long l0 = launch_count();
+  // GBSORT_VERIFY: multiset hashes of the input before and the output after
+  // the sort must agree (the reference's checksum, mpsort-mpi.c:148-159)
+  const bool verify = (method & GBSORT_VERIFY) != 0 && nmemb > 0;
+  method &= ~GBSORT_VERIFY;
+  unsigned long long* vh = nullptr;
+  if (verify) {
+    GB_CUDA(c.vh.ensure(2 * sizeof(unsigned long long)));
+    vh = c.vh.as<unsigned long long>();
+    GB_CUDA(multiset_hash(d_in, nmemb, (uint32_t)elsize, vh, st));
+  }
   int rc = sort_device_dispatch(c, d_in, d_out, nmemb, elsize, key, method, st);
+  if (rc == GBSORT_OK && verify) {
+    unsigned long long h[2];
+    GB_CUDA(multiset_hash(d_out, nmemb, (uint32_t)elsize, vh + 1, st));
+    GB_CUDA(cudaMemcpyAsync(h, vh, sizeof h, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    if (h[0] != h[1]) {
+      set_err("self-check failed: the output is not a permutation of the input records (multiset hash %016llx, "
+              "input %016llx)", h[1], h[0]);
+      rc = GBSORT_ERR_INTERNAL;
+    }
+  }
   if (rc == GBSORT_OK) g_stats.launches = (uint32_t)(launch_count() - l0);
   return rc;
 }
@@ -836,13 +965,20 @@ int sort_device_dispatch(Context& c, const void* d_in, void* d_out, size_t nmemb
     g_stats = gbsort_stats{};
     return GBSORT_OK;
   }
-  if (nmemb >= 0xffffffffull || elsize == 0 || elsize > (1u << 20)) {
-    set_err("nmemb must be < 2^32 and elsize in [1, 2^20]");
+  if (elsize == 0 || elsize > (1u << 20)) {
+    set_err("elsize must be in [1, 2^20]");
     return GBSORT_ERR_BAD_ARG;
   }
   if (!key_ok(key, elsize)) {
     set_err("bad key descriptor");
     return GBSORT_ERR_BAD_ARG;
+  }
+  if (nmemb >= 0xffffffffull) {  // 64-bit record counts: a first stable partition into key ranges
+    if (!hsort_layout_ok(d_in, d_out, (uint32_t)elsize, key)) {
+      set_err("sorts of 2^32 records or more need a one-word key at a 4-byte offset and a record size of 8-64 bytes");
+      return GBSORT_ERR_UNSUPPORTED;
+    }
+    return run_partitioned(c, d_in, d_out, nmemb, (uint32_t)elsize, key, method, st);
   }
   const uint32_t n = (uint32_t)nmemb, E = (uint32_t)elsize;
   bool hs_ok = hsort_layout_ok(d_in, d_out, E, key);
@@ -1312,7 +1448,8 @@ int gbsort_release(void) {
   if (rc) return rc;
   std::lock_guard<std::mutex> lk(c->mu);
   cudaStreamSynchronize(c->stream);
-  DevBuf* bufs[] = {&c->A, &c->B, &c->hin, &c->hout, &c->keysA, &c->keysB, &c->idxA, &c->idxB, &c->small, &c->radix};
+  DevBuf* bufs[] = {&c->A, &c->B, &c->hin, &c->hout, &c->keysA, &c->keysB, &c->idxA, &c->idxB, &c->small, &c->radix,
+                    &c->part, &c->vh};
   for (DevBuf* b : bufs) b->release();
   return GBSORT_OK;
 }
@@ -1497,7 +1634,7 @@ int gbsort_plan_create(gbsort_plan** plan, size_t nmemb, size_t elsize, const gb
   int rc = get_ctx(&probe);  // checks for a device
   if (rc) return rc;
   gbsort_plan* p = new gbsort_plan();
-  rc = ctx_init(p->ctx, probe->device);
+  rc = ctx_init(p->ctx, probe->device, false);
   if (rc == GBSORT_OK && cudaEventCreateWithFlags(&p->done, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
     rc = GBSORT_ERR_CUDA;
@@ -1656,6 +1793,79 @@ void mpsort_omp(void* base, size_t nmemb, size_t size, void (*radix)(const void*
 }
 
 int mpsort_last_status(void) { return g_mpsort_status; }
+
+// One-process forms of the reference's MPI entry points: the communicator is
+// not read.  As in the reference with one rank, `base` ends sorted (its
+// first, local sort) and so does `out` (outnmemb must equal nmemb).  With
+// the descriptor radix the sort is self-checked like the reference's: a
+// multiset hash of the records before and after, in place of its byte sum.
+void mpsort_mpi_newarray_impl(void* base, size_t nmemb, void* out, size_t outnmemb, size_t elsize,
+                              void (*radix)(const void* ptr, void* radix, void* arg), size_t rsize, void* arg,
+                              intptr_t comm, int line, const char* file) {
+  (void)comm;
+  int rc = GBSORT_OK;
+  if (outnmemb != nmemb) {
+    set_err("input and output size mismatch: %zu (in) != %zu (out)", nmemb, outnmemb);
+    rc = GBSORT_ERR_BAD_ARG;
+  } else if (nmemb > 0) {
+    if (radix == mpsort_radix_desc) {
+      const gbsort_key_desc* d = (const gbsort_key_desc*)arg;
+      if (!d || rsize != 8u * d->nwords) rc = GBSORT_ERR_BAD_ARG;
+      else rc = gbsort_sort_host(base, base, nmemb, elsize, d, GBSORT_AUTO | GBSORT_VERIFY);
+    } else {
+      rc = gbsort_sort_radix_host(base, nmemb, elsize, radix, rsize, arg);
+    }
+    if (rc == GBSORT_OK && out != base) memcpy(out, base, nmemb * elsize);
+  }
+  g_mpsort_status = rc;
+  if (rc != GBSORT_OK)
+    fprintf(stderr, "mpsort_mpi (%s:%d): GPU sort failed (%s): %s\n", file ? file : "?", line,
+            gbsort_status_string(rc), g_err);
+}
+
+void mpsort_mpi_impl(void* base, size_t nmemb, size_t elsize, void (*radix)(const void* ptr, void* radix, void* arg),
+                     size_t rsize, void* arg, intptr_t comm, int line, const char* file) {
+  mpsort_mpi_newarray_impl(base, nmemb, base, nmemb, elsize, radix, rsize, arg, comm, line, file);
+}
+
+void mpsort_mpi_report_last_run(void) {
+  static const char* names[6] = {"splitters", "count", "scan", "scatter", "split", "local"};
+  const gbsort_stats& st = g_stats;
+  printf("mpsort (GB300) last run: method %d, %u buckets, %u launches\n", st.method, st.nbuckets, st.launches);
+  for (int i = 0; i < 6; ++i) printf("%s %.4f ms\n", names[i], st.stage_ms[i]);
+}
+
+int gbsort_take_device(const void* d_source, size_t nsource, size_t elsize, const int64_t* d_index, size_t nindex,
+                       void* d_out, void* stream) {
+  if (elsize == 0 || elsize > (1u << 20) || (nindex && (!d_index || !d_out || (nsource && !d_source))))
+    return GBSORT_ERR_BAD_ARG;
+  Context* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  GB_CUDA(c->vh.ensure(2 * sizeof(unsigned long long)));
+  unsigned long long* bad = c->vh.as<unsigned long long>();
+  GB_CUDA(take_records(d_source, nsource, (uint32_t)elsize, d_index, nindex, d_out, bad, st));
+  unsigned long long hb = 0;
+  GB_CUDA(cudaMemcpyAsync(&hb, bad, sizeof hb, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  if (hb) {
+    set_err("index %llu is out of range for %zu source records", hb - 1, nsource);
+    return GBSORT_ERR_BAD_ARG;
+  }
+  return GBSORT_OK;
+}
+
+int gbsort_multiset_hash_device(const void* d_records, size_t nmemb, size_t elsize, uint64_t* d_hash, void* stream) {
+  if (!d_hash || (nmemb && !d_records) || elsize == 0 || elsize > (1u << 20)) return GBSORT_ERR_BAD_ARG;
+  Context* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  GB_CUDA(multiset_hash(d_records, nmemb, (uint32_t)elsize, (unsigned long long*)d_hash, st));
+  return GBSORT_OK;
+}
 
 void mpsort_mpi_set_options(int options) {
   std::lock_guard<std::mutex> lk(g_opt_mu);

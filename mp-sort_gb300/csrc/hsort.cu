@@ -592,6 +592,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
   }
   for (uint32_t t0 = cb; t0 < ce; t0 += T) {
     const uint32_t nvalid = min((uint32_t)T, ce - t0);
+    if (threadIdx.x == 0 && t0 + 2 * T < ce)
+      prefetch_l2_range(p.in + (size_t)(t0 + 2 * T) * E, min((uint32_t)T, ce - t0 - 2 * T) * E);
     uint32_t rec[RPT][EW];
     uint32_t bkt[RPT], rank[RPT];
 #pragma unroll
@@ -1525,6 +1527,8 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
   const uint32_t g_me = threadIdx.x;
   for (uint32_t t0 = 0; t0 < m; t0 += T) {
     const uint32_t nvalid = min((uint32_t)T, m - t0);
+    // the tile after next heads for L2 (its loads below then wait on L2, not DRAM)
+    if (threadIdx.x == 0 && t0 + 2 * T < m) prefetch_l2_range(src + (size_t)(t0 + 2 * T) * E, min((uint32_t)T, m - t0 - 2 * T) * E);
     uint32_t rec[RPT][EW];
     uint32_t grp[RPT], rank[RPT], lead[RPT];
 #pragma unroll

@@ -17,6 +17,34 @@ namespace gb {
 void note_launches(int k);
 unsigned long long launch_count();
 
+// Streaming multiprocessors of the current device.
+int num_sms();
+
+// ---- verify.cu: multiset hash, and the first partition of huge sorts ------
+// *out = sum over the n records of a 64-bit mix of each record's bytes
+// (order-independent; equal multisets of records give equal sums).
+cudaError_t multiset_hash(const void* rec, uint64_t n, uint32_t elsize, unsigned long long* out, cudaStream_t st);
+// s keys at evenly spaced records i * n / s of n (64-bit) records.
+cudaError_t sample_keys64(const uint8_t* rec, uint64_t n, uint32_t elsize, gbsort_key_word key, uint32_t s,
+                          uint64_t* out, cudaStream_t st);
+// Chunks of the partition kernels; counts are [part][chunk].
+int part_grid();
+// Records per (part, chunk) for nsplit <= 14 sorted splitters (part =
+// #{splitters <= key}).
+cudaError_t part_count(const uint8_t* rec, uint64_t n, uint32_t elsize, gbsort_key_word key, const uint64_t* S,
+                       int nsplit, uint32_t* counts, cudaStream_t st);
+// Stable scatter of every record to offsets[part][chunk] + its rank among
+// its chunk's records of that part.
+cudaError_t part_scatter(const uint8_t* rec, uint8_t* out, uint64_t n, uint32_t elsize, gbsort_key_word key,
+                         const uint64_t* S, int nsplit, const unsigned long long* offsets, uint32_t* err,
+                         cudaStream_t st);
+
+// ---- take.cu --------------------------------------------------------------
+// out[i] = src[index[i]] for nidx records of elsize bytes; *bad receives the
+// first position whose index lies outside [0, nsrc), plus one (0: none).
+cudaError_t take_records(const void* src, uint64_t nsrc, uint32_t elsize, const int64_t* index, uint64_t nidx,
+                         void* out, unsigned long long* bad, cudaStream_t st);
+
 // ---- scan.cu --------------------------------------------------------------
 // Exclusive prefix sum of n uint32 values (n <= 2^24); `tmp` needs
 // scan_tmp_words(n) words.  out may alias in.

@@ -16,6 +16,7 @@ MAX_KEY_WORDS = 4
 
 OK, ERR_BAD_ARG, ERR_OOM, ERR_CUDA, ERR_NO_DEVICE, ERR_INTERNAL, ERR_UNSUPPORTED = range(7)
 METHODS = {"auto": 0, "plain": 1, "learned": 2, "lsd": 3}
+VERIFY = 0x100  # GBSORT_VERIFY: self-checked sort (multiset hash of input and output)
 METHOD_NAMES = {v: k for k, v in METHODS.items()}
 
 
@@ -88,6 +89,11 @@ SIGNATURES = {
     "gbsort_debug_model": (_I, [_P, _U32, _I, _I, _P, _U32, _P, _P, _P, _P, _P]),
     "gbsort_debug_bisect": (_I, [_P, _U32, _I, _P, _P, _P, _P]),
     "gbsort_debug_lookback": (_I, [_U32, _U32, _U32]),
+    "gbsort_multiset_hash_device": (_I, [_P, _SZ, _SZ, _P, _P]),
+    "gbsort_take_device": (_I, [_P, _SZ, _SZ, _P, _SZ, _P, _P]),
+    "mpsort_mpi_newarray_impl": (None, [_P, _SZ, _P, _SZ, _SZ, _P, _SZ, _P, ctypes.c_ssize_t, _I, ctypes.c_char_p]),
+    "mpsort_mpi_impl": (None, [_P, _SZ, _SZ, _P, _SZ, _P, ctypes.c_ssize_t, _I, ctypes.c_char_p]),
+    "mpsort_mpi_report_last_run": (None, []),
     "gbsort_plan_create": (_I, [_P, _SZ, _SZ, _P, _I]),
     "gbsort_plan_sort": (_I, [_P, _P, _P, _P]),
     "gbsort_plan_wait": (_I, [_P]),

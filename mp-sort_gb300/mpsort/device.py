@@ -2,7 +2,8 @@
 
 Pointers are plain integers (e.g. ``torch.Tensor.data_ptr()``) and streams
 are ``cudaStream_t`` values as integers (e.g. ``torch.cuda.Stream.cuda_stream``);
-0 selects the library's own stream.  Every call returns once the work is
+0 selects the library's own stream, which orders after work issued earlier on
+the legacy default stream (torch's default stream).  Every call returns once the work is
 enqueued on that stream.
 """
 import ctypes
@@ -16,12 +17,29 @@ def _desc(dtype, orderby):
     return _lib.key_desc(dtype, orderby)
 
 
-def sort(d_in, d_out, n, dtype, orderby, method="auto", stream=0):
-    """Sort n records of `dtype` from d_in into d_out by field `orderby`."""
+def sort(d_in, d_out, n, dtype, orderby, method="auto", stream=0, verify=False):
+    """Sort n records of `dtype` from d_in into d_out by field `orderby`.
+    verify=True hashes the records before and after (and waits); a result
+    that is not a permutation of the input raises GBSortError."""
     dtype = numpy.dtype(dtype)
     desc = _desc(dtype, orderby)
-    _lib.check(_lib.lib().gbsort_sort_device(d_in, d_out, n, dtype.itemsize, ctypes.byref(desc),
-                                             _lib.METHODS[method], stream or None))
+    m = _lib.METHODS[method] | (_lib.VERIFY if verify else 0)
+    _lib.check(_lib.lib().gbsort_sort_device(d_in, d_out, n, dtype.itemsize, ctypes.byref(desc), m, stream or None))
+
+
+def take(d_source, nsource, d_index, nindex, dtype, d_out, stream=0):
+    """out[i] = source[index[i]] for device records of `dtype` and int64
+    device indices (waits; an index outside the source raises GBSortError)."""
+    dtype = numpy.dtype(dtype)
+    _lib.check(_lib.lib().gbsort_take_device(d_source, nsource, dtype.itemsize, d_index, nindex, d_out,
+                                             stream or None))
+
+
+def multiset_hash(d_records, n, dtype, d_hash, stream=0):
+    """Order-independent 64-bit hash of n device records into the uint64 at
+    d_hash (device memory); equal multisets of records hash equally."""
+    dtype = numpy.dtype(dtype)
+    _lib.check(_lib.lib().gbsort_multiset_hash_device(d_records, n, dtype.itemsize, d_hash, stream or None))
 
 
 class Plan:
