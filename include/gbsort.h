@@ -150,6 +150,15 @@ GBSORT_API int gbsort_cdf_forward_backward(const uint64_t *x, uint32_t s, uint64
                                 int lbits, const float *y, float *loss, float *pred,
                                 float *grad);
 
+/* The gradient the model's training steps use, at knots y (host arrays as
+ * above): T y - b, where the tridiagonal T and the vector b come from one
+ * pass of the statistics kernel over the sorted keys (the loss is quadratic
+ * in the knots, so this equals the backward pass's gradient; the training
+ * runs all its steps from T and b without reading the keys again).
+ * lbits <= 13.  For checking against the CPU oracle. */
+GBSORT_API int gbsort_cdf_train_gradient(const uint64_t *x, uint32_t s, uint64_t kmin, uint64_t kmax, int lbits,
+                                         const float *y, float *grad);
+
 /* Learned-lookup probe (host arrays): trains the CDF model on the sample,
  * derives its splitters (nbuckets - 1 of them, returned in `splitters`) and
  * looks every key up twice -- with the model plus its search window, and

@@ -7,8 +7,10 @@
 //
 //   k_cdf_forward   -- F(x_i) and the loss
 //   k_cdf_backward  -- dLoss/dy_j (each sample feeds its two knots)
-//   k_cdf_curvature -- diagonal of the Gauss-Newton matrix (preconditioner)
-//   k_cdf_step      -- damped Jacobi-preconditioned gradient step
+//   k_cdf_stats     -- the tridiagonal normal matrix T and vector b of the
+//                      least-squares fit, so that dLoss/dy = T y - b
+//   k_cdf_epochs    -- every damped Jacobi-preconditioned gradient step in
+//                      one CTA from T and b (no further pass over the sample)
 //   k_cdf_project   -- non-decreasing knots in [0, 1] (cumulative max)
 //   k_cdf_splitters -- S_j = least key with predicted bucket >= j + 1
 //   k_cdf_heavy     -- keys covering a whole bucket of the sample get their
@@ -103,22 +105,97 @@ __global__ void k_cdf_backward(const uint64_t* __restrict__ x, uint32_t s, CdfSh
   }
 }
 
-__global__ void k_cdf_curvature(const uint64_t* __restrict__ x, uint32_t s, CdfShape sh, float* __restrict__ h) {
+// Sufficient statistics of the fit.  The loss is quadratic in the knots:
+// with a_i = (1 - frac_i) e_leaf + frac_i e_{leaf+1},
+//   dLoss/dy = T y - b,  T = (2/s) sum_i a_i a_i^T,  b = (2/s) sum_i r_i a_i,
+// T tridiagonal (diag[j]; off[j] couples knots j and j + 1) and its diagonal
+// the Gauss-Newton curvature a training step divides by.  One pass over the
+// sample gives T and b; every training step after it touches only the
+// knots (k_cdf_epochs), with the same gradient k_cdf_backward computes
+// from the sample.
+__global__ void k_cdf_stats(const uint64_t* __restrict__ x, uint32_t s, CdfShape sh, float* __restrict__ diag,
+                            float* __restrict__ off, float* __restrict__ b) {
   sh = resolve_shape(sh);
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s; i += gridDim.x * blockDim.x) {
-    uint32_t leaf;
-    float frac;
-    features(x[i], sh.kmin, sh.lshift, sh.lbits, leaf, frac);
-    atomicAdd(&h[leaf], 2.f * (1.f - frac) * (1.f - frac) / (float)s);
-    atomicAdd(&h[leaf + 1], 2.f * frac * frac / (float)s);
+  const float c = 2.f / (float)s;
+  for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < s; i0 += gridDim.x * blockDim.x) {
+    const uint32_t i = i0 + threadIdx.x;
+    const bool v = i < s;
+    uint32_t leaf = 0xffffffffu;
+    float d0 = 0.f, d1 = 0.f, o = 0.f, b0 = 0.f, b1 = 0.f;
+    if (v) {
+      float f;
+      features(x[i], sh.kmin, sh.lshift, sh.lbits, leaf, f);
+      const float r = (float)i / (float)s;
+      d0 = c * (1.f - f) * (1.f - f);
+      d1 = c * f * f;
+      o = c * (1.f - f) * f;
+      b0 = c * r * (1.f - f);
+      b1 = c * r * f;
+    }
+    // lanes of one leaf add up before the atomics (the sample is sorted)
+    const uint32_t peers = __match_any_sync(GB_FULL_MASK, leaf);
+    float a[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    for (uint32_t m = peers; m; m &= m - 1) {
+      const int l = __ffs(m) - 1;
+      a[0] += __shfl_sync(peers, d0, l);
+      a[1] += __shfl_sync(peers, d1, l);
+      a[2] += __shfl_sync(peers, o, l);
+      a[3] += __shfl_sync(peers, b0, l);
+      a[4] += __shfl_sync(peers, b1, l);
+    }
+    if (v && (peers & lanemask_lt()) == 0) {
+      atomicAdd(&diag[leaf], a[0]);
+      atomicAdd(&diag[leaf + 1], a[1]);
+      atomicAdd(&off[leaf], a[2]);
+      atomicAdd(&b[leaf], a[3]);
+      atomicAdd(&b[leaf + 1], a[4]);
+    }
   }
 }
 
-__global__ void k_cdf_step(float* __restrict__ y, const float* __restrict__ grad, const float* __restrict__ h,
-                           int nknots, float lr) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j <= 0 || j >= nknots - 1) return;  // F(kmin) = 0 and F(end) = 1 stay fixed
-  y[j] -= lr * grad[j] / (h[j] + 1e-12f);
+// (T y - b)_j from the statistics; off has nknots - 1 entries.
+__device__ __forceinline__ float stat_gradient(const float* y, const float* diag, const float* off, const float* b,
+                                               int j, int nknots) {
+  float g = diag[j] * y[j] - b[j];
+  if (j > 0) g += off[j - 1] * y[j - 1];
+  if (j + 1 < nknots) g += off[j] * y[j + 1];
+  return g;
+}
+
+// `epochs` damped Jacobi-preconditioned gradient steps on the knots in one
+// CTA: the end knots stay fixed (F(kmin) = 0, F(end) = 1), every other
+// knot moves by -lr * g_j / diag_j, all from the previous epoch's knots.
+__global__ void __launch_bounds__(1024) k_cdf_epochs(float* __restrict__ y, const float* __restrict__ diag,
+                                                     const float* __restrict__ off, const float* __restrict__ b,
+                                                     int nknots, int epochs, float lr) {
+  extern __shared__ float sy[];
+  for (int j = threadIdx.x; j < nknots; j += blockDim.x) sy[j] = y[j];
+  __syncthreads();
+  constexpr int kMaxPer = 8;  // knots per thread: nknots <= 8 * 1024 + 1
+  for (int e = 0; e < epochs; ++e) {
+    float nv[kMaxPer];
+#pragma unroll
+    for (int q = 0; q < kMaxPer; ++q) {
+      const int j = threadIdx.x + q * blockDim.x;
+      nv[q] = 0.f;
+      if (j > 0 && j < nknots - 1) nv[q] = sy[j] - lr * stat_gradient(sy, diag, off, b, j, nknots) / (diag[j] + 1e-12f);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < kMaxPer; ++q) {
+      const int j = threadIdx.x + q * blockDim.x;
+      if (j > 0 && j < nknots - 1) sy[j] = nv[q];
+    }
+    __syncthreads();
+  }
+  for (int j = threadIdx.x; j < nknots; j += blockDim.x) y[j] = sy[j];
+}
+
+__global__ void k_cdf_stat_grad(const float* __restrict__ y, const float* __restrict__ diag,
+                                const float* __restrict__ off, const float* __restrict__ b, int nknots,
+                                float* __restrict__ grad) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < nknots) grad[j] = stat_gradient(y, diag, off, b, j, nknots);
 }
 
 // Initial knots: the empirical CDF of the sample at every knot.
@@ -426,22 +503,42 @@ cudaError_t cdf_backward(const uint64_t* x, uint32_t s, const CdfShape& sh, cons
   return cudaGetLastError();
 }
 
+// Statistics T, b of the sample into w.h (diag), w.off, w.grad (b).
+static cudaError_t cdf_stats(const uint64_t* x, uint32_t s, const CdfShape& sh, CdfWork& w, cudaStream_t st) {
+  const int nk = (1 << sh.lbits) + 1;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(w.h, 0, sizeof(float) * nk, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(w.off, 0, sizeof(float) * nk, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(w.grad, 0, sizeof(float) * nk, st)) != cudaSuccess) return e;
+  k_cdf_stats<<<grid_for(s, 256), 256, 0, st>>>(x, s, sh, w.h, w.off, w.grad);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
 cudaError_t cdf_train(const uint64_t* x, uint32_t s, const CdfShape& sh, int epochs, float lr, CdfWork& w,
                       cudaStream_t st) {
   const int nk = (1 << sh.lbits) + 1;
+  if (nk > 8 * 1024 + 1) return cudaErrorInvalidValue;
   cudaError_t e;
   k_cdf_init<<<grid_for(nk, 256), 256, 0, st>>>(x, s, sh, w.y);
   note_launches(1);
-  if ((e = cudaMemsetAsync(w.h, 0, sizeof(float) * nk, st)) != cudaSuccess) return e;
-  k_cdf_curvature<<<grid_for(s, 256), 256, 0, st>>>(x, s, sh, w.h);
-  note_launches(1);
-  for (int it = 0; it < epochs; ++it) {
-    if ((e = cdf_backward(x, s, sh, w.y, w.grad, st)) != cudaSuccess) return e;
-    k_cdf_step<<<grid_for(nk, 256), 256, 0, st>>>(w.y, w.grad, w.h, nk, lr);
+  if ((e = cdf_stats(x, s, sh, w, st)) != cudaSuccess) return e;
+  if (epochs > 0) {
+    k_cdf_epochs<<<1, 1024, sizeof(float) * nk, st>>>(w.y, w.h, w.off, w.grad, nk, epochs, lr);
     note_launches(1);
   }
   if (w.loss && (e = cdf_forward(x, s, sh, w.y, nullptr, w.loss, st)) != cudaSuccess) return e;
   k_cdf_project<<<1, 1024, 0, st>>>(w.y, nk, w.knots);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t cdf_train_gradient(const uint64_t* x, uint32_t s, const CdfShape& sh, const float* y, float* grad,
+                               CdfWork& w, cudaStream_t st) {
+  const int nk = (1 << sh.lbits) + 1;
+  cudaError_t e;
+  if ((e = cdf_stats(x, s, sh, w, st)) != cudaSuccess) return e;
+  k_cdf_stat_grad<<<grid_for(nk, 256), 256, 0, st>>>(y, w.h, w.off, w.grad, nk, grad);
   note_launches(1);
   return cudaGetLastError();
 }

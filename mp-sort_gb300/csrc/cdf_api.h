@@ -18,8 +18,9 @@ struct CdfShape {
 
 struct CdfWork {   // device buffers of one training run
   float* y;        // knots, (1 << lbits) + 1
-  float* grad;     // same size
-  float* h;        // same size
+  float* grad;     // same size: b of the fit's statistics (dLoss/dy = T y - b)
+  float* h;        // same size: diagonal of T (the Gauss-Newton curvature)
+  float* off;      // same size: off-diagonal of T
   float2* knots;   // 1 << lbits pairs (y_j, y_{j+1}) after projection
   float* loss;     // 1 float (may be null)
 };
@@ -35,6 +36,10 @@ cudaError_t cdf_backward(const uint64_t* x, uint32_t s, const CdfShape& sh, cons
                          cudaStream_t st);
 cudaError_t cdf_train(const uint64_t* x, uint32_t s, const CdfShape& sh, int epochs, float lr, CdfWork& w,
                       cudaStream_t st);
+// The training's gradient at knots y (device, (1 << lbits) + 1 floats) into
+// grad: T y - b from one statistics pass over x (uses w's h, off, grad).
+cudaError_t cdf_train_gradient(const uint64_t* x, uint32_t s, const CdfShape& sh, const float* y, float* grad,
+                               CdfWork& w, cudaStream_t st);
 cudaError_t cdf_splitters(const uint64_t* x, uint32_t s, const CdfShape& sh, int nbuckets,
                           const float2* knots, uint64_t* S, cudaStream_t st);
 cudaError_t cdf_windows(const CdfShape& sh, int nbuckets, const float2* knots, const uint64_t* S,

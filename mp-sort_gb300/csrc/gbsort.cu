@@ -597,6 +597,7 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
       w.y = bump.take<float>(nleaf + 1);
       w.grad = bump.take<float>(nleaf + 1);
       w.h = bump.take<float>(nleaf + 1);
+      w.off = bump.take<float>(nleaf + 1);
       w.knots = bump.take<float2>(nleaf);
       w.loss = loss;
       uint32_t* win = bump.take<uint32_t>(nleaf);
@@ -629,6 +630,17 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
   }
   if (timing) GB_CUDA(cudaEventRecord(c.ev[1], st));
   const ModelDev* mp = lookup == LOOKUP_LEARNED ? &model : nullptr;
+  // the level-1 scatter: a learned sort enqueues it with the learned lookup
+  // and with the plain one, gated on the model's widest window -- wide
+  // windows (steep steps of heavy keys inside leaves) make the window search
+  // cost more than a binary search over splitters in shared memory -- and
+  // exactly one of the two does the work
+  auto scatter = [&](int c0, int c1, const uint32_t* skip) -> cudaError_t {
+    if (lookup != LOOKUP_LEARNED) return l1_scatter(p, lookup, S, nb, mp, counts, stats, st, c0, c1, skip);
+    cudaError_t e = l1_scatter(p, LOOKUP_LEARNED, S, nb, mp, counts, stats, st, c0, c1, skip, widest, 0);
+    if (e != cudaSuccess) return e;
+    return l1_scatter(p, LOOKUP_PLAIN, S, nb, nullptr, counts, stats, st, c0, c1, skip, widest, 1);
+  };
   // pipelined: each piece is counted and scattered into the reserved bucket
   // regions as soon as it has landed; if a bucket outgrows its region the
   // scatters stop and level 1 is redone exactly from the complete input
@@ -650,7 +662,7 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
         GB_CUDA(cudaStreamWaitEvent(st, c.pev[i], 0));
         GB_CUDA(l1_count(p, lookup, S, nb, mp, counts, stats, st, i * grid, (i + 1) * grid));
         GB_CUDA(region_offsets(counts, G, nb, region, cap, total, i * grid, (i + 1) * grid, overflow, st));
-        GB_CUDA(l1_scatter(p, lookup, S, nb, mp, counts, stats, st, i * grid, (i + 1) * grid, overflow));
+        GB_CUDA(scatter(i * grid, (i + 1) * grid, overflow));
       }
       GB_CUDA(cudaMemcpyAsync(&c.hc->c[CNT_OVERFLOW], overflow, 12, cudaMemcpyDeviceToHost, st));
     } else {  // regions would not fit 32-bit offsets: level 1 waits for the whole input
@@ -665,7 +677,7 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
       p.a_cap = n;
       GB_CUDA(l1_count(p, lookup, S, nb, mp, counts, stats, st));
       GB_CUDA(exclusive_scan_u32(counts, counts, (size_t)nb * G, scan_tmp, st));
-      GB_CUDA(l1_scatter(p, lookup, S, nb, mp, counts, stats, st));
+      GB_CUDA(scatter(0, -1, nullptr));
     }
     // the first output record of every wave of level-1 buckets
     for (int j = 0; j < waves; ++j) {
@@ -679,7 +691,7 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
     if (timing) GB_CUDA(cudaEventRecord(c.ev[2], st));
     GB_CUDA(exclusive_scan_u32(counts, counts, (size_t)nb * G, scan_tmp, st));
     if (timing) GB_CUDA(cudaEventRecord(c.ev[3], st));
-    GB_CUDA(l1_scatter(p, lookup, S, nb, mp, counts, stats, st));
+    GB_CUDA(scatter(0, -1, nullptr));
   }
   if (timing) GB_CUDA(cudaEventRecord(c.ev[4], st));
   static const bool trace = getenv("GBSORT_TRACE") != nullptr;
@@ -1262,6 +1274,32 @@ int gbsort_cdf_forward_backward(const uint64_t* x, uint32_t s, uint64_t kmin, ui
   return GBSORT_OK;
 }
 
+int gbsort_cdf_train_gradient(const uint64_t* x, uint32_t s, uint64_t kmin, uint64_t kmax, int lbits,
+                              const float* y, float* grad) {
+  if (!x || !y || !grad || s == 0 || lbits < 0 || lbits > 13) return GBSORT_ERR_BAD_ARG;
+  Context* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  const int nk = (1 << lbits) + 1;
+  GB_CUDA(c->small.ensure((size_t)s * 8 + (size_t)nk * 24 + (1 << 16)));
+  Bump bump{c->small.as<uint8_t>()};
+  uint64_t* dx = bump.take<uint64_t>(s);
+  float* dy = bump.take<float>(nk);
+  float* dg = bump.take<float>(nk);
+  CdfWork w{};
+  w.h = bump.take<float>(nk);
+  w.off = bump.take<float>(nk);
+  w.grad = bump.take<float>(nk);
+  cudaStream_t st = c->stream;
+  GB_CUDA(cudaMemcpyAsync(dx, x, (size_t)s * 8, cudaMemcpyHostToDevice, st));
+  GB_CUDA(cudaMemcpyAsync(dy, y, (size_t)nk * 4, cudaMemcpyHostToDevice, st));
+  GB_CUDA(cdf_train_gradient(dx, s, cdf_shape(kmin, kmax, lbits), dy, dg, w, st));
+  GB_CUDA(cudaMemcpyAsync(grad, dg, (size_t)nk * 4, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  return GBSORT_OK;
+}
+
 int gbsort_debug_bisect(const uint64_t* sorted, uint32_t s, int nsplit, uint64_t* splitters, int64_t* clt,
                         int64_t* cle, uint32_t* rounds) {
   if (!sorted || s == 0 || nsplit <= 0) return GBSORT_ERR_BAD_ARG;
@@ -1352,6 +1390,7 @@ int debug_model(const uint64_t* sample, uint32_t s, int nbuckets, int epochs, co
   w.y = bump.take<float>(nleaf + 1);
   w.grad = bump.take<float>(nleaf + 1);
   w.h = bump.take<float>(nleaf + 1);
+  w.off = bump.take<float>(nleaf + 1);
   w.knots = bump.take<float2>(nleaf);
   w.loss = bump.take<float>(1);
   uint32_t* win = bump.take<uint32_t>(nleaf);

@@ -539,8 +539,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
                                                              const uint32_t* __restrict__ offsets,
                                                              int nchunks, uint32_t* __restrict__ stats,
                                                              uint32_t c0, uint32_t c1,
-                                                             const uint32_t* __restrict__ skip_if) {
+                                                             const uint32_t* __restrict__ skip_if,
+                                                             const uint32_t* __restrict__ gate, int gate_wide) {
   if (skip_if && *skip_if) return;  // a reserved region overflowed: the exact path redoes level 1
+  // gate: a learned sort launches this kernel with both lookups; the one
+  // that does not suit the model's widest window (kWideWindow) returns
+  if (gate && (*gate > kWideWindow) != (gate_wide != 0)) return;
   model = resolve_model(model);
   uint32_t* err = stats + STAT_SLOTS;  // the error word follows the statistics
   constexpr int RPT = ScatterTile<EW>::kRpt, T = ScatterTile<EW>::kSize;
@@ -1908,7 +1912,7 @@ uint32_t hsort_chunk_begin(uint32_t n, int c, int chunks) {
 
 cudaError_t l1_scatter(const HsortParams& p, int lookup_kind, const uint64_t* splitters, int nbuckets,
                        const void* model, const uint32_t* offsets, uint32_t* stats, cudaStream_t stream, int c0,
-                       int c1, const uint32_t* skip_if) {
+                       int c1, const uint32_t* skip_if, const uint32_t* gate, int gate_wide) {
   const ModelDev m = model ? *(const ModelDev*)model : ModelDev{};
   const int g = p.chunks ? (int)p.chunks : hsort_grid(p.n);
   if (c1 < 0) c1 = g;
@@ -1923,7 +1927,7 @@ cudaError_t l1_scatter(const HsortParams& p, int lookup_kind, const uint64_t* sp
       if (e == cudaSuccess)
         k_l1_scatter<EW, LOOKUP_LEARNED><<<ctas, kThreads, sm, stream>>>(p, splitters, nbuckets, m, offsets, g,
                                                                                   stats, (uint32_t)c0, (uint32_t)c1,
-                                                                                  skip_if);
+                                                                                  skip_if, gate, gate_wide);
       note_launches(1);
     } else {
       size_t sm = l1_scatter_smem<EW, LOOKUP_PLAIN>(nbuckets, &m);
@@ -1931,7 +1935,7 @@ cudaError_t l1_scatter(const HsortParams& p, int lookup_kind, const uint64_t* sp
       if (e == cudaSuccess)
         k_l1_scatter<EW, LOOKUP_PLAIN><<<ctas, kThreads, sm, stream>>>(p, splitters, nbuckets, m, offsets, g,
                                                                                 stats, (uint32_t)c0, (uint32_t)c1,
-                                                                                skip_if);
+                                                                                skip_if, gate, gate_wide);
       note_launches(1);
     }
   });

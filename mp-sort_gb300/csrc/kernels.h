@@ -190,10 +190,13 @@ cudaError_t bucket_caps(const uint64_t* sorted_sample, uint32_t s, const uint64_
 cudaError_t region_offsets(uint32_t* counts, int chunks, int nbuckets, const uint32_t* region, const uint32_t* cap,
                            uint32_t* total, int c0, int c1, uint32_t* overflow, cudaStream_t stream);
 // Scatter of chunks [c0, c1) (c1 < 0: all) to offsets[bucket][chunk]; does
-// nothing if *skip_if is set (a region overflow).
+// nothing if *skip_if is set (a region overflow), nor, with a gate, unless
+// (*gate > kWideWindow) equals gate_wide (a learned sort launches the learned
+// and the plain lookup so gated on its widest window, and one of them runs).
 cudaError_t l1_scatter(const HsortParams& p, int lookup, const uint64_t* splitters, int nbuckets,
                        const void* model, const uint32_t* offsets, uint32_t* stats, cudaStream_t stream,
-                       int c0 = 0, int c1 = -1, const uint32_t* skip_if = nullptr);
+                       int c0 = 0, int c1 = -1, const uint32_t* skip_if = nullptr, const uint32_t* gate = nullptr,
+                       int gate_wide = 0);
 // Level-2 task lists (device memory).  A split round consumes split_in and
 // appends to split_out and local; build_tasks appends to split_out and local.
 struct TaskListsHost {

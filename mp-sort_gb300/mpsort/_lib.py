@@ -85,6 +85,7 @@ SIGNATURES = {
     "gbsort_sort_segments_device": (_I, [_P, _P, _P, _SZ, _SZ, _P, _I, _P]),
     "gbsort_merge_join_device": (_I, [_P, _SZ, _P, _SZ, _SZ, _P, _P, _P, _P, _P]),
     "gbsort_cdf_forward_backward": (_I, [_P, _U32, _U64, _U64, _I, _P, _P, _P, _P]),
+    "gbsort_cdf_train_gradient": (_I, [_P, _U32, _U64, _U64, _I, _P, _P]),
     "gbsort_debug_buckets": (_I, [_P, _U32, _I, _P, _U32, _P, _P, _P, _P]),
     "gbsort_debug_model": (_I, [_P, _U32, _I, _I, _P, _U32, _P, _P, _P, _P, _P]),
     "gbsort_debug_bisect": (_I, [_P, _U32, _I, _P, _P, _P, _P]),

@@ -159,6 +159,16 @@ def cdf_forward_backward(x, kmin, kmax, lbits, y):
     return float(loss[0]), pred, grad
 
 
+def cdf_train_gradient(x, kmin, kmax, lbits, y):
+    """The training's gradient T y - b (statistics pass) at knots y."""
+    x = numpy.ascontiguousarray(x, dtype=numpy.uint64)
+    y = numpy.ascontiguousarray(y, dtype=numpy.float32)
+    grad = numpy.zeros(len(y), numpy.float32)
+    _lib.check(_lib.lib().gbsort_cdf_train_gradient(x.ctypes.data, len(x), int(kmin), int(kmax), lbits,
+                                                    y.ctypes.data, grad.ctypes.data))
+    return grad
+
+
 def debug_buckets(sample, nbuckets, keys):
     """(full-search buckets, learned buckets, splitters, widest window)."""
     sample = numpy.ascontiguousarray(sample, dtype=numpy.uint64)

@@ -323,6 +323,9 @@ def test_cdf_forward_backward_matches_numpy(mp):
         assert abs(loss - l2) <= 1e-4 * max(1e-6, l2) + 1e-7
         numpy.testing.assert_allclose(pred, p2, rtol=1e-5, atol=1e-6)
         numpy.testing.assert_allclose(grad, g2, rtol=2e-3, atol=1e-7)
+        # the gradient the training steps use: T y - b from the statistics pass
+        gt = device.cdf_train_gradient(x, x[0], x[-1], lbits, y)
+        numpy.testing.assert_allclose(gt, g2, rtol=2e-3, atol=2e-6)
         # finite-difference check of the numpy gradient itself
         j = len(y) // 2
         h = 1e-3
