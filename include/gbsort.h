@@ -75,6 +75,9 @@ typedef struct gbsort_stats {
     uint32_t pipelined;          /* 1: a host sort sent its input up in pieces, sorting as they landed */
     uint32_t region_overflow;    /* pipelined: 0, or 1 + the first level-1 bucket that outgrew the
                                     region reserved for it from the sample (level 1 was then redone) */
+    uint32_t engine;             /* 1: level 2 (bucket splits, local sorts, copies) ran as one
+                                    persistent launch over a device task queue; stage_ms[4] then
+                                    holds all of level 2 and stage_ms[5] is 0 */
 } gbsort_stats;
 
 /* OR into `method`: hash the records (gbsort_multiset_hash_device) before
@@ -114,7 +117,8 @@ GBSORT_API int gbsort_take_device(const void *d_source, size_t nsource, size_t e
 GBSORT_API int gbsort_multiset_hash_device(const void *d_records, size_t nmemb, size_t elsize,
                                            uint64_t *d_hash, void *stream);
 
-/* Same, for host memory: in and out may be equal.  Blocks until done. */
+/* gbsort_sort_device for host memory: in and out may be equal.  Blocks
+ * until done. */
 GBSORT_API int gbsort_sort_host(const void *in, void *out, size_t nmemb, size_t elsize,
                      const gbsort_key_desc *key, int method);
 
@@ -237,20 +241,28 @@ GBSORT_API const char *gbsort_version(void);
 /* ---- autotuner --------------------------------------------------------------
  * gbsort_autotune times every candidate configuration -- the LSD path, and
  * the plain and learned histogram sorts at level-1 bucket caps of 512, 1024,
- * 2048 and 4096 -- on nmemb records of this layout (the caller's device
- * records, read only, or pseudo-random ones when d_records is NULL), returns
- * the fastest and stores it in the tuning table under (elsize, key width,
- * size class = bit length of nmemb).  Sorts with GBSORT_AUTO use the table
- * entry of the nearest size class within a factor of 4.  The table can be
- * set by hand, saved to and loaded from a text file (one entry per line:
- * elsize key_width size_class method max_buckets sample_per_bucket ms).
+ * 2048 and 4096, each with level 2 as split rounds and (records of 8-16
+ * bytes) as the persistent engine -- on nmemb records of this layout (the
+ * caller's device records, read only, or pseudo-random ones when d_records
+ * is NULL), returns the fastest and stores it in the tuning table under
+ * (elsize, key width, size class = bit length of nmemb).  Sorts with
+ * GBSORT_AUTO use the table entry of the nearest size class within a factor
+ * of 4.  The table can be set by hand, saved to and loaded from a text file
+ * (one entry per line: elsize key_width size_class method max_buckets
+ * sample_per_bucket ms level2; files without the level2 column load too).
  * No counterpart in the reference. */
+/* How level 2 of the histogram sort (bucket splits and local sorts) runs:
+ * as split rounds (one launch per round, then one for the local sorts) or as
+ * one persistent launch over a device task queue (records of 8-16 bytes). */
+enum { GBSORT_LEVEL2_DEFAULT = 0, GBSORT_LEVEL2_ROUNDS = 1, GBSORT_LEVEL2_ENGINE = 2 };
+
 typedef struct gbsort_tuning {
     int32_t method;              /* GBSORT_HISTOGRAM_PLAIN, _LEARNED or GBSORT_LSD */
     uint32_t max_buckets;        /* level-1 bucket cap: a power of two, 2..4096 (0: default) */
     uint32_t sample_per_bucket;  /* sampled keys per level-1 bucket, 16..1024 (0: 128) */
     float ms;                    /* measured time of this configuration */
-    uint32_t reserved[4];
+    uint32_t level2;             /* GBSORT_LEVEL2_* */
+    uint32_t reserved[3];
 } gbsort_tuning;
 GBSORT_API int gbsort_autotune(size_t nmemb, size_t elsize, const gbsort_key_desc *key,
                     const void *d_records, gbsort_tuning *best);

@@ -118,7 +118,8 @@ enum CounterSlot : int {
   CNT_HEAVY = 30,        // keys in the heavy-key table
   CNT_OVERFLOW = 31,     // a bucket outgrew its reserved region (pipelined host sort): bucket + 1,
                          // then its capacity and count (3 words)
-  CNT_WORDS = 64
+  CNT_ENGINE = 48,       // the level-2 engine's queue: tail, head, pending, kEngineCtlStride apart
+  CNT_WORDS = 128
 };
 
 // Bytes past the records of each scratch buffer: the staged local sorts copy
@@ -172,7 +173,7 @@ struct Context {
   std::mutex mu;
   // shape of the last enqueued histogram sort (for hsort_collect)
   uint32_t run_nbuckets = 0, run_sample = 0, run_lsd_passes = 0;
-  bool run_learned = false, run_timing = false, run_pipelined = false;
+  bool run_learned = false, run_timing = false, run_pipelined = false, run_engine = false;
 };
 
 std::mutex g_ctx_mu;
@@ -391,6 +392,7 @@ struct HsortRun {
 struct Knobs {
   int max_buckets = 0;        // level-1 bucket cap, a power of two up to 4096 (0: default)
   int sample_per_bucket = 0;  // sampled keys per level-1 bucket (0: 128)
+  int level2 = 0;             // GBSORT_LEVEL2_*: split rounds or the persistent engine (0: default)
 };
 
 // Level-1 bucket count: about 2048 records per bucket, at most the cap --
@@ -433,6 +435,7 @@ bool tuning_ok(const gbsort_tuning& t) {
     return false;
   if (t.max_buckets && (t.max_buckets < 2 || t.max_buckets > 4096 || (t.max_buckets & (t.max_buckets - 1))))
     return false;
+  if (t.level2 > GBSORT_LEVEL2_ENGINE) return false;
   return t.sample_per_bucket == 0 || (t.sample_per_bucket >= 16 && t.sample_per_bucket <= 1024);
 }
 // The entry of the nearest size class (within a factor of 4) for this layout.
@@ -462,18 +465,28 @@ struct Level2 {
   uint32_t* nlocal;
   uint32_t* work;
   uint32_t cap_split, cap_local;
+  SortTask* qtask;   // the persistent engine's queue (every task of level 2)
+  uint32_t* qready;
+  uint32_t* qctl;    // tail, head, pending
+  uint32_t qcap;
   static size_t bytes(uint32_t cap_split, uint32_t cap_local) {
-    return ((size_t)cap_split * 2 + cap_local) * sizeof(SortTask) + 4096;
+    const size_t q = (size_t)cap_split + cap_local;
+    return ((size_t)cap_split * 2 + cap_local) * sizeof(SortTask) + q * (sizeof(SortTask) + 4) + 8192;
   }
+  // counters: the run's counter array (CNT_WORDS)
   void carve(Bump& bump, uint32_t* counters, uint32_t cs, uint32_t cl) {
     cap_split = cs;
     cap_local = cl;
     split[0] = bump.take<SortTask>(cs);
     split[1] = bump.take<SortTask>(cs);
     local = bump.take<SortTask>(cl);
-    nsplit = counters;
-    nlocal = counters + 2;
-    work = counters + 3;
+    nsplit = counters + CNT_L2;
+    nlocal = counters + CNT_L2 + 2;
+    work = counters + CNT_L2 + 3;
+    qcap = cs + cl;
+    qtask = bump.take<SortTask>(qcap);
+    qready = bump.take<uint32_t>(qcap);
+    qctl = counters + CNT_ENGINE;
   }
   TaskListsHost round(int r) const {  // round r reads split[r&1], appends to split[(r+1)&1]
     TaskListsHost L;
@@ -493,9 +506,35 @@ constexpr uint64_t kAutoLsdMax = (uint64_t)1 << 23;  // method auto, untuned: LS
 constexpr int kSplitRounds = 16;  // every round narrows each re-split range; 64-bit keys need few
 constexpr int kCdfEpochs = 8;     // gradient steps of the CDF model
 
-// The split rounds, then one pass over every local task.  The initial tasks
-// must already be in split[0] (count in nsplit[0]).
+// Level 2 as the persistent engine or as split rounds.  The engine takes
+// records of 8-16 bytes with their tasks at final positions.  By default
+// batched segments use it (their uneven tasks leave rounds half idle:
+// configuration 3, 1.74e10 -> 2.05e10 records/s) and a single array keeps
+// the rounds (uniform keys, 1e9 x 16 B: rounds 24.8 ms, engine 28.0 ms --
+// the engine kernel holds both task bodies in one register budget); a
+// tuning entry or GBSORT_LEVEL2=rounds|engine overrides the default.
+bool use_engine(uint32_t elsize, int level2, bool segments) {
+  static const int env = [] {
+    const char* e = getenv("GBSORT_LEVEL2");
+    if (!e) return 0;
+    return strcmp(e, "engine") == 0 ? (int)GBSORT_LEVEL2_ENGINE
+                                    : (strcmp(e, "rounds") == 0 ? (int)GBSORT_LEVEL2_ROUNDS : 0);
+  }();
+  if (!engine_supported(elsize)) return false;
+  const int choice = env ? env : level2;
+  if (choice == GBSORT_LEVEL2_ENGINE) return true;
+  if (choice == GBSORT_LEVEL2_ROUNDS) return false;
+  return segments;
+}
+
+// Level 2 from the initial tasks in split[0] (count in nsplit[0]) and the
+// local list: one persistent engine launch, or the split rounds and then one
+// pass over every local task.
 int run_level2(const HsortParams& p, const Level2& l2, uint32_t* stats, uint32_t* err, cudaStream_t st) {
+  if (use_engine(p.elsize, 0, true)) {
+    GB_CUDA(run_engine(p, l2.round(0), l2.qtask, l2.qready, l2.qctl, l2.qcap, stats, err, st));
+    return GBSORT_OK;
+  }
   for (int r = 0; r < kSplitRounds; ++r) {
     TaskListsHost L = l2.round(r);
     GB_CUDA(cudaMemsetAsync(L.nsplit_out, 0, sizeof(uint32_t), st));
@@ -552,7 +591,7 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
   uint32_t* counts = bump.take<uint32_t>((size_t)nb * G);
   uint32_t* scan_tmp = bump.take<uint32_t>(scan_tmp_words((size_t)nb * G));
   Level2 l2;
-  l2.carve(bump, counters + CNT_L2, cap_split, cap_local);
+  l2.carve(bump, counters, cap_split, cap_local);
 
   HsortParams p{};
   p.in = (const uint8_t*)d_in;
@@ -708,6 +747,11 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
       else
         GB_CUDA(build_tasks(counts, G, S, nb, n, L, err, stats, st, j * nb / waves, (j + 1) * nb / waves));
     }
+    if (!hp && use_engine(elsize, knobs.level2, false)) {  // one persistent launch (a host sort's waves keep the rounds)
+      GB_CUDA(run_engine(p, l2.round(0), l2.qtask, l2.qready, l2.qctl, l2.qcap, stats, err, st));
+      if (timing) GB_CUDA(cudaEventRecord(c.ev[5], st));
+      continue;
+    }
     for (int r = 0; r < kSplitRounds; ++r) {
       TaskListsHost L = l2.round(r);
       GB_CUDA(cudaMemsetAsync(L.nsplit_out, 0, sizeof(uint32_t), st));
@@ -764,6 +808,7 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
   c.run_nbuckets = (uint32_t)nb;
   c.run_sample = s;
   c.run_learned = learned;
+  c.run_engine = !hp && use_engine(elsize, knobs.level2, false);
   c.run_timing = timing;
   c.run_pipelined = hp != nullptr;
   return GBSORT_OK;
@@ -777,9 +822,10 @@ int hsort_collect(Context& c) {
     set_err("device check failed: code %u", h[CNT_ERR]);
     return GBSORT_ERR_INTERNAL;
   }
-  const uint32_t left = h[CNT_L2 + (kSplitRounds & 1)];  // the last round's output list must be empty
+  // the last round's output list, or the engine's pending tasks, must be empty
+  const uint32_t left = c.run_engine ? h[CNT_ENGINE + 2 * kEngineCtlStride] : h[CNT_L2 + (kSplitRounds & 1)];
   if (left != 0) {
-    set_err("split rounds did not finish: %u tasks left", left);
+    set_err("level 2 did not finish: %u tasks left", left);
     return GBSORT_ERR_INTERNAL;
   }
   g_stats = gbsort_stats{};
@@ -803,6 +849,7 @@ int hsort_collect(Context& c) {
   g_stats.refined_splits = h[STAT_REFINED];
   g_stats.pipelined = c.run_pipelined ? 1u : 0u;
   g_stats.region_overflow = c.run_pipelined ? h[CNT_OVERFLOW] : 0u;
+  g_stats.engine = c.run_engine ? 1u : 0u;
   if (c.run_timing)
     for (int i = 0; i < 6; ++i) {
       float ms = 0.f;
@@ -833,6 +880,7 @@ int resolve_auto(uint32_t elsize, const gbsort_key_desc* key, uint64_t n, bool h
     if (hs_ok) {
       knobs->max_buckets = (int)t.max_buckets;
       knobs->sample_per_bucket = (int)t.sample_per_bucket;
+      knobs->level2 = (int)t.level2;
       return t.method;
     }
   }
@@ -1182,7 +1230,7 @@ int gbsort_sort_segments_device(const void* d_in, void* d_out, const uint64_t* s
   uint32_t* err = counters + CNT_ERR;
   uint64_t* offs = bump.take<uint64_t>(nseg + 1);
   Level2 l2;
-  l2.carve(bump, counters + CNT_L2, cap_split, cap_local);
+  l2.carve(bump, counters, cap_split, cap_local);
   GB_CUDA(cudaMemsetAsync(counters, 0, CNT_WORDS * sizeof(uint32_t), st));
   GB_CUDA(cudaMemcpyAsync(offs, seg_offsets, (nseg + 1) * 8, cudaMemcpyHostToDevice, st));
   GB_CUDA(cudaMemcpyAsync(c->A.p, d_in, (size_t)N * E, cudaMemcpyDeviceToDevice, st));
@@ -1202,9 +1250,9 @@ int gbsort_sort_segments_device(const void* d_in, void* d_out, const uint64_t* s
   GB_CUDA(cudaMemcpyAsync(c->hc->c, counters, CNT_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaStreamSynchronize(st));
   const uint32_t* h = c->hc->c;
-  if (h[CNT_ERR] || h[CNT_L2 + (kSplitRounds & 1)]) {
-    set_err("segmented sort device check failed: code %u, %u tasks left", h[CNT_ERR],
-            h[CNT_L2 + (kSplitRounds & 1)]);
+  const uint32_t left = use_engine(E, 0, true) ? h[CNT_ENGINE + 2 * kEngineCtlStride] : h[CNT_L2 + (kSplitRounds & 1)];
+  if (h[CNT_ERR] || left) {
+    set_err("segmented sort device check failed: code %u, %u tasks left", h[CNT_ERR], left);
     return GBSORT_ERR_INTERNAL;
   }
   g_stats = gbsort_stats{};
@@ -1215,6 +1263,7 @@ int gbsort_sort_segments_device(const void* d_in, void* d_out, const uint64_t* s
   g_stats.copies = h[STAT_COPY];
   g_stats.resplits = h[STAT_PUSHED];
   g_stats.bigbin_passes = h[STAT_BIGBIN];
+  g_stats.engine = use_engine(E, 0, true) ? 1u : 0u;
   return GBSORT_OK;
 }
 
@@ -1521,17 +1570,22 @@ int gbsort_autotune(size_t nmemb, size_t elsize, const gbsort_key_desc* key, con
   struct Cand {
     int method;
     int cap;
+    int level2;
   };
   std::vector<Cand> cands;
-  cands.push_back({GBSORT_LSD, 0});
+  cands.push_back({GBSORT_LSD, 0, GBSORT_LEVEL2_DEFAULT});
   if (hs_ok)
     for (int m : {GBSORT_HISTOGRAM_LEARNED, GBSORT_HISTOGRAM_PLAIN})
-      for (int cap : {512, 1024, 2048, 4096}) cands.push_back({m, cap});
+      for (int cap : {512, 1024, 2048, 4096}) {
+        cands.push_back({m, cap, GBSORT_LEVEL2_ROUNDS});
+        if (engine_supported(E)) cands.push_back({m, cap, GBSORT_LEVEL2_ENGINE});
+      }
   gbsort_tuning win{};
   win.ms = -1.f;
   for (const Cand& cd : cands) {
     Knobs k;
     k.max_buckets = cd.cap;
+    k.level2 = cd.level2;
     float ms_best = -1.f;
     for (int rep = 0; rep < 3; ++rep) {  // a warm-up, then the best of two
       GB_CUDA(cudaEventRecord(c->ev[7], st));
@@ -1552,6 +1606,7 @@ int gbsort_autotune(size_t nmemb, size_t elsize, const gbsort_key_desc* key, con
       win.method = cd.method;
       win.max_buckets = (uint32_t)cd.cap;
       win.sample_per_bucket = 0;
+      win.level2 = (uint32_t)cd.level2;
       win.ms = ms_best;
     }
   }
@@ -1595,11 +1650,11 @@ int gbsort_tuning_save(const char* path) {
     return GBSORT_ERR_BAD_ARG;
   }
   std::lock_guard<std::mutex> tl(g_tune_mu);
-  fprintf(f, "# gbsort tuning: elsize key_width size_class method max_buckets sample_per_bucket ms\n");
+  fprintf(f, "# gbsort tuning: elsize key_width size_class method max_buckets sample_per_bucket ms level2\n");
   for (const auto& kv : g_tune)
-    fprintf(f, "%u %u %u %d %u %u %.4f\n", (unsigned)(kv.first >> 16), (unsigned)((kv.first >> 8) & 0xff),
+    fprintf(f, "%u %u %u %d %u %u %.4f %u\n", (unsigned)(kv.first >> 16), (unsigned)((kv.first >> 8) & 0xff),
             (unsigned)(kv.first & 0xff), kv.second.method, kv.second.max_buckets, kv.second.sample_per_bucket,
-            kv.second.ms);
+            kv.second.ms, kv.second.level2);
   fclose(f);
   return GBSORT_OK;
 }
@@ -1616,10 +1671,11 @@ int gbsort_tuning_load(const char* path) {
   int rc = GBSORT_OK;
   while (fgets(line, sizeof line, f)) {
     if (line[0] == '#' || line[0] == '\n') continue;
-    unsigned el, wd, cls, mb, spb;
+    unsigned el, wd, cls, mb, spb, l2 = 0;
     int m;
     float ms;
-    if (sscanf(line, "%u %u %u %d %u %u %f", &el, &wd, &cls, &m, &mb, &spb, &ms) != 7 || (wd != 4 && wd != 8) ||
+    const int got = sscanf(line, "%u %u %u %d %u %u %f %u", &el, &wd, &cls, &m, &mb, &spb, &ms, &l2);
+    if ((got != 7 && got != 8) || (wd != 4 && wd != 8) ||
         cls > 64 || el == 0 || el > (1u << 20)) {
       rc = GBSORT_ERR_BAD_ARG;
       break;
@@ -1628,6 +1684,7 @@ int gbsort_tuning_load(const char* path) {
     t.method = m;
     t.max_buckets = mb;
     t.sample_per_bucket = spb;
+    t.level2 = l2;
     t.ms = ms;
     if (!tuning_ok(t)) {
       rc = GBSORT_ERR_BAD_ARG;

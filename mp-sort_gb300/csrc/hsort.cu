@@ -857,6 +857,7 @@ struct SplitSmem {
   uint32_t scan_tmp[kWarps];
   uint32_t task_id;
   SortTask next;
+  uint32_t emit_base;  // the engine's reservation for this split's groups
 };
 
 template <int NT = kThreads>
@@ -1364,8 +1365,95 @@ __device__ __forceinline__ void scan_bins(uint32_t* a, uint32_t* scan_tmp) {
 // Split of one large bucket: 4096 bins of its key range, grouped into at most
 // 256 runs of consecutive bins, a stable scatter src -> other by group, and
 // one task per group (local sort, copy, or another split).
-template <int EW>
-__device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& task, const TaskLists& L,
+// ---- the persistent engine's queue (the engine itself is further down) ----
+struct EngineQueue {
+  SortTask* task;     // [cap]
+  uint32_t* ready;    // [cap], zero before the launch
+  uint32_t* tail;     // tasks pushed
+  uint32_t* head;     // tasks claimed
+  uint32_t* pending;  // tasks pushed and not finished
+  uint32_t cap;       // (the three counters sit in separate cache lines)
+};
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+struct EngineSink {
+  const EngineQueue& q;
+  __device__ void push(const SortTask& t, uint32_t* err) const {
+    atomicAdd(q.pending, 1u);  // pending first: it never undercounts
+    const uint32_t at = atomicAdd(q.tail, 1u);
+    if (at >= q.cap) {
+      set_error(err, DEV_ERR_TASK_OVERFLOW);
+      atomicSub(q.pending, 1u);
+      return;
+    }
+    q.task[at] = t;
+    __threadfence();
+    st_release_u32(&q.ready[at], 1u);
+  }
+  __device__ void copy(uint32_t start, uint32_t cnt, uint64_t lo, uint64_t hi, uint32_t src_b, uint32_t* err) const {
+    for (uint32_t s0 = 0; s0 < cnt; s0 += kCopyPiece)
+      push(make_task(start + s0, min(kCopyPiece, cnt - s0), lo, hi, src_b != 0, true), err);
+  }
+  __device__ void local(const SortTask& t, uint32_t* err) const { push(t, err); }
+  __device__ void split(const SortTask& t, uint32_t* err) const { push(t, err); }
+};
+
+constexpr uint32_t kEngineWaitPolls = 1u << 24;
+
+// A split publishes all its groups with one reservation: a block scan of
+// every thread's task count, one atomic each on pending and tail, then the
+// tasks and their ready flags (instead of two atomics and a fence per task).
+// Every thread calls it with its own tasks: n of them, the i-th from make(i).
+template <typename Make>
+__device__ __forceinline__ void engine_emit(const EngineQueue& q, uint32_t n, Make&& make, uint32_t* base_slot,
+                                            uint32_t* scan_tmp, uint32_t* err) {
+  uint32_t total;
+  const uint32_t off = block_exclusive_scan<uint32_t>(n, scan_tmp, &total);
+  if (total == 0) return;
+  if (threadIdx.x == 0) {
+    atomicAdd(q.pending, total);  // before any flag: pending never undercounts
+    const uint32_t base = atomicAdd(q.tail, total);
+    *base_slot = base;
+    if (base + total > q.cap || base + total < base) {
+      set_error(err, DEV_ERR_TASK_OVERFLOW);
+      atomicSub(q.pending, base >= q.cap ? total : base + total - q.cap);
+    }
+  }
+  __syncthreads();
+  const uint32_t base = *base_slot;
+  for (uint32_t i = 0; i < n; ++i)
+    if (base + off + i < q.cap) q.task[base + off + i] = make(i);
+  __threadfence();
+  for (uint32_t i = 0; i < n; ++i)
+    if (base + off + i < q.cap) st_release_u32(&q.ready[base + off + i], 1u);
+  __syncthreads();
+}
+
+enum EngineState : uint32_t { ENGINE_HAVE = 0, ENGINE_DONE = 1 };
+
+// Where the tasks of a split go: the next round's lists (RoundSink) or the
+// persistent engine's queue (EngineSink, below).
+struct RoundSink {
+  const TaskLists& L;
+  __device__ void copy(uint32_t start, uint32_t cnt, uint64_t lo, uint64_t hi, uint32_t src_b, uint32_t* err) const {
+    push_copy(L, start, cnt, lo, hi, src_b, err);
+  }
+  __device__ void local(const SortTask& t, uint32_t* err) const { push(L.local, L.nlocal, L.cap_local, t, err); }
+  __device__ void split(const SortTask& t, uint32_t* err) const {
+    push(L.split_out, L.nsplit_out, L.cap_split, t, err);
+  }
+};
+
+template <int EW, typename Sink>
+__device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& task, const Sink& L,
                            uint32_t* stats, uint32_t* err) {
   constexpr uint32_t E = EW * 4;
   constexpr int RPT = Tile<EW>::kRpt, T = Tile<EW>::kSize;
@@ -1592,25 +1680,55 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
   }
   __threadfence_block();
   // one task per group
-  for (int g = threadIdx.x; g < kMaxGroups; g += kThreads) {
+  if constexpr (std::is_same<Sink, EngineSink>::value) {
+    // the groups go to the engine's queue in one reservation
+    static_assert(kMaxGroups == kThreads, "one group per thread");
+    const uint32_t g = threadIdx.x;
     const uint32_t g0 = sm.gstart[g], g1 = sm.gstart[g + 1];
-    if (g1 == g0) continue;
-    const uint32_t b0 = sm.gfirst[g], b1 = sm.gfirst[g + 1];
-    const uint32_t s = g1 - g0;
-    const uint64_t glo = refined ? fine_bin_lo(sm.hist, b0, blo, shift, nbins) : blo + ((uint64_t)b0 << shift);
-    const uint64_t ghi = b1 >= sm.gfirst[kMaxGroups] ? bhi  // (the number of bins there)
-                         : (refined ? fine_bin_lo(sm.hist, b1, blo, shift, nbins) : blo + ((uint64_t)b1 << shift)) - 1;
-    const uint32_t nsrc = in_b ? 0u : 1u;
-    if (glo == ghi || s == 1) {
-      push_copy(L, task.start + g0, s, glo, ghi, nsrc, err);
-    } else if (s <= (uint32_t)kLocalMax) {
-      push(L.local, L.nlocal, L.cap_local, make_task(task.start + g0, s, glo, ghi, nsrc != 0, false), err);
-    } else {
-      atomicAdd(stats + STAT_PUSHED, 1u);
-      push(L.split_out, L.nsplit_out, L.cap_split, make_task(task.start + g0, s, glo, ghi, nsrc != 0, false), err);
+    uint32_t n = 0, s = 0;
+    uint64_t glo = 0, ghi = 0;
+    bool cp = false;
+    if (g1 > g0) {
+      const uint32_t b0 = sm.gfirst[g], b1 = sm.gfirst[g + 1];
+      s = g1 - g0;
+      glo = refined ? fine_bin_lo(sm.hist, b0, blo, shift, nbins) : blo + ((uint64_t)b0 << shift);
+      ghi = b1 >= sm.gfirst[kMaxGroups] ? bhi
+            : (refined ? fine_bin_lo(sm.hist, b1, blo, shift, nbins) : blo + ((uint64_t)b1 << shift)) - 1;
+      cp = glo == ghi || s == 1;
+      n = cp ? (s + kCopyPiece - 1) / kCopyPiece : 1;
+      if (!cp && s > (uint32_t)kLocalMax) atomicAdd(stats + STAT_PUSHED, 1u);
     }
+    const bool nsrc_b = !in_b;
+    const uint32_t start = task.start + g0;
+    engine_emit(L.q, n,
+                [&](uint32_t i) {
+                  return cp ? make_task(start + i * kCopyPiece, min(kCopyPiece, s - i * kCopyPiece), glo, ghi,
+                                        nsrc_b, true)
+                            : make_task(start, s, glo, ghi, nsrc_b, false);
+                },
+                &sm.emit_base, sm.scan_tmp, err);
+    return;
+  } else {
+    for (int g = threadIdx.x; g < kMaxGroups; g += kThreads) {
+      const uint32_t g0 = sm.gstart[g], g1 = sm.gstart[g + 1];
+      if (g1 == g0) continue;
+      const uint32_t b0 = sm.gfirst[g], b1 = sm.gfirst[g + 1];
+      const uint32_t s = g1 - g0;
+      const uint64_t glo = refined ? fine_bin_lo(sm.hist, b0, blo, shift, nbins) : blo + ((uint64_t)b0 << shift);
+      const uint64_t ghi = b1 >= sm.gfirst[kMaxGroups] ? bhi  // (the number of bins there)
+                           : (refined ? fine_bin_lo(sm.hist, b1, blo, shift, nbins) : blo + ((uint64_t)b1 << shift)) - 1;
+      const uint32_t nsrc = in_b ? 0u : 1u;
+      if (glo == ghi || s == 1) {
+        L.copy(task.start + g0, s, glo, ghi, nsrc, err);
+      } else if (s <= (uint32_t)kLocalMax) {
+        L.local(make_task(task.start + g0, s, glo, ghi, nsrc != 0, false), err);
+      } else {
+        atomicAdd(stats + STAT_PUSHED, 1u);
+        L.split(make_task(task.start + g0, s, glo, ghi, nsrc != 0, false), err);
+      }
+    }
+    __syncthreads();
   }
-  __syncthreads();
 }
 
 template <int EW>
@@ -1654,7 +1772,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split(HsortParams p, TaskLists 
       continue;
     }
     if (threadIdx.x == 0) atomicAdd(stats + STAT_SPLIT, 1u);
-    split_task<EW>(sm, p, task, L, stats, err);
+    split_task<EW>(sm, p, task, RoundSink{L}, stats, err);
   }
 }
 
@@ -1805,6 +1923,224 @@ __global__ void __launch_bounds__(NT, 2) k_local_staged(HsortParams p, const Sor
       if (threadIdx.x == 0) atomicAdd(stats + STAT_LOCAL, 1u);
     }
     __syncthreads();
+  }
+}
+
+// ---------------------------------------------- persistent level-2 engine --
+// Level 2 as ONE persistent launch: two CTAs per SM take tasks from a device
+// queue in push order -- bucket splits, shared-memory local sorts and
+// single-key copies alike -- and a split appends its groups to the same
+// queue, so there are no rounds and no launch per round: a local task runs
+// as soon as a CTA is free after its split has published it.
+//   * a task becomes visible through its ready flag (written after the task,
+//     with release order); a CTA claims the next index with an atomic and
+//     waits for that flag;
+//   * `pending` counts tasks pushed and not finished; a split adds its
+//     children before it finishes, so pending reaches zero only when no task
+//     is left and none can come: a CTA waiting on a flag then stops;
+//   * every wait is bounded (about four seconds of polling, far above any
+//     task) and records DEV_ERR_TIMEOUT if it runs out;
+//   * shared memory: the split's and the local sort's arrays overlay each
+//     other; a local task's records come in by a bulk copy, started for the
+//     next task while the current local task sorts when that task is ready.
+// Tasks always lie at their final positions (no reserved regions), so the
+// order in which they run does not matter: their ranges are disjoint.
+// Control words of a CTA, outside the overlaid arrays.  The task to run
+// alternates between two slots (the running one is read by every thread
+// while thread 0 fills the other), so one barrier per task separates them.
+struct EngineCtl {
+  uint64_t bar[2];      // completion of the two record buffers' copies
+  SortTask task[2];     // the task to run
+  uint32_t state[2];    // ENGINE_*
+  uint32_t loaded[2];   // 1: the task's records are on their way into its buffer
+  uint32_t slot[2];     // the task's record buffer
+  SortTask next;        // the task claimed ahead, if it was ready
+  uint32_t next_idx;    // index claimed ahead (kNoClaim: none)
+  uint32_t next_ready;  // 1: `next` holds it
+  uint32_t next_loaded; // 1: its records are on their way
+  uint32_t parity;      // bit b: parity of the next completion of buffer b
+  uint32_t dirty;       // kDirty* below
+};
+// The overlaid arrays that must be zero when a task starts: the local
+// sort's bin counts (a split may have overwritten them) and the split's
+// warp-row ranking table (a local sort may have).
+constexpr uint32_t kDirtyBins = 1, kDirtyTable = 2;
+constexpr uint32_t kNoClaim = 0xffffffffu;
+
+template <int EW>
+__host__ __device__ constexpr size_t engine_ctl_offset() {
+  return ((sizeof(SplitSmem) > 2 * (size_t)staged_buf_bytes<EW>() + sizeof(LocalSmemP<kThreads>)
+               ? sizeof(SplitSmem)
+               : 2 * (size_t)staged_buf_bytes<EW>() + sizeof(LocalSmemP<kThreads>)) +
+          127) & ~(size_t)127;
+}
+template <int EW>
+constexpr size_t engine_smem_bytes() {
+  return engine_ctl_offset<EW>() + sizeof(EngineCtl);
+}
+
+// Thread 0: waits until task i is ready; false (and *state DONE) when it
+// will never come (pending reached zero first, or the wait ran out).
+__device__ __forceinline__ bool engine_wait(const EngineQueue& q, uint32_t i, uint32_t* err) {
+  if (i >= q.cap) return false;
+  for (uint32_t k = 0; k < kEngineWaitPolls; ++k) {
+    if (ld_acquire_u32(&q.ready[i])) return true;
+    if (ld_acquire_u32(q.pending) == 0) return ld_acquire_u32(&q.ready[i]) != 0;
+    __nanosleep(k < 64 ? 64 : 256);
+  }
+  set_error(err, DEV_ERR_TIMEOUT);
+  return false;
+}
+
+template <int EW>
+__device__ __forceinline__ bool engine_staged(const SortTask& t) {
+  return !(t.flags & TASK_COPY) && t.count > 1 && t.count <= (uint32_t)kLocalMax;
+}
+
+template <int EW>
+__global__ void __launch_bounds__(kThreads, 2) k_engine(HsortParams p, EngineQueue q, uint32_t* __restrict__ stats) {
+  constexpr uint32_t E = EW * 4;
+  constexpr uint32_t kBuf = staged_buf_bytes<EW>();
+  extern __shared__ __align__(128) uint8_t smem_raw[];
+  SplitSmem& ssm = *reinterpret_cast<SplitSmem*>(smem_raw);
+  uint8_t* rbuf = smem_raw;
+  LocalSmemP<kThreads>& lsm = *reinterpret_cast<LocalSmemP<kThreads>*>(smem_raw + 2 * kBuf);
+  EngineCtl& c = *reinterpret_cast<EngineCtl*>(smem_raw + engine_ctl_offset<EW>());
+  uint32_t* err = stats + STAT_SLOTS;
+  const EngineSink sink{q};
+  auto source = [&](const SortTask& t) { return ((t.flags & TASK_SRC_B) ? p.bufB : p.bufA) + (size_t)t.from * E; };
+  auto issue = [&](const SortTask& t, uint32_t slot) {  // thread 0
+    const uintptr_t a = (uintptr_t)source(t);
+    const uintptr_t a0 = a & ~(uintptr_t)15;
+    const uint32_t bytes = (uint32_t)(((a - a0) + (uintptr_t)t.count * E + 15) & ~(uintptr_t)15);
+    fence_proxy_async_smem();
+    bulk_load(rbuf + (size_t)slot * kBuf, (const void*)a0, bytes, &c.bar[slot]);
+  };
+  for (int i = threadIdx.x; i < kMaxGroups * kWarps; i += kThreads) ssm.gcnt[i] = 0;
+  if (threadIdx.x == 0) {
+    mbar_init(&c.bar[0], 1);
+    mbar_init(&c.bar[1], 1);
+    mbar_init_fence();
+    c.parity = 0;
+    c.dirty = kDirtyBins;  // the table is zeroed above; the bins are not
+    c.next_idx = kNoClaim;
+    c.next_ready = 0;
+    c.next_loaded = 0;
+    c.slot[0] = 0;
+    c.loaded[0] = 0;
+    const uint32_t i = atomicAdd(q.head, 1u);
+    c.state[0] = engine_wait(q, i, err) ? ENGINE_HAVE : ENGINE_DONE;
+    if (c.state[0] == ENGINE_HAVE) {
+      c.task[0] = q.task[i];
+      if (engine_staged<EW>(c.task[0])) {
+        issue(c.task[0], 0);
+        c.loaded[0] = 1;
+      }
+    }
+  }
+  __syncthreads();
+  for (uint32_t it = 0;; ++it) {
+    const uint32_t cur = it & 1u;
+    if (c.state[cur] == ENGINE_DONE) break;
+    const SortTask& task = c.task[cur];  // read where used (thread 0 fills the other slot meanwhile)
+    const uint32_t slot = c.slot[cur], loaded = c.loaded[cur];
+    const bool staged = engine_staged<EW>(task);
+    const bool copy = (task.flags & TASK_COPY) || task.count == 1;
+    const bool split = !staged && !copy;
+    if (staged && threadIdx.x == 0) {  // claim the next task now; its records come in during this sort
+      const uint32_t n = atomicAdd(q.head, 1u);
+      c.next_idx = n;
+      if (n < q.cap && ld_acquire_u32(&q.ready[n])) {
+        c.next = q.task[n];
+        c.next_ready = 1;
+        if (engine_staged<EW>(c.next)) {
+          issue(c.next, slot ^ 1);
+          c.next_loaded = 1;
+        }
+      }
+    }
+    uint8_t* out = p.out + (size_t)task.start * E;
+    if (copy) {
+      block_copy_ilp<EW>(source(task), out, task.count, kThreads);
+      if (threadIdx.x == 0) atomicAdd(stats + STAT_COPY, 1u);
+    } else if (split) {
+      if (c.dirty & kDirtyTable)  // the ranking table starts at zero (split_task's first barriers follow)
+        for (int i = threadIdx.x; i < kMaxGroups * kWarps / 16; i += kThreads)
+          reinterpret_cast<uint4*>(ssm.gcnt)[i] = make_uint4(0, 0, 0, 0);
+      if (threadIdx.x == 0) atomicAdd(stats + STAT_SPLIT, 1u);
+      split_task<EW>(ssm, p, task, sink, stats, err);
+      if (threadIdx.x == 0) c.dirty = kDirtyBins;
+    } else {
+      if (c.dirty & kDirtyBins)  // the local sort expects zero bins (the barrier below follows)
+        for (int i = threadIdx.x; i <= (1 << kLocalBits); i += kThreads) lsm.cnt[i] = 0;
+      const uint32_t par = (c.parity >> slot) & 1u;
+      bool ok = loaded ? mbar_wait_bounded(&c.bar[slot], par, kBulkWaitPolls) : false;
+      ok = __syncthreads_and(ok);
+      if (!ok) {  // the copy never completed: record it, wait once more for the copies in flight, stop
+        if (threadIdx.x == 0) set_error(err, DEV_ERR_TIMEOUT);
+        mbar_wait_bounded(&c.bar[slot], par, kBulkWaitPolls);
+        if (c.next_loaded) mbar_wait_bounded(&c.bar[slot ^ 1], (c.parity >> (slot ^ 1)) & 1u, kBulkWaitPolls);
+        return;
+      }
+      const uint8_t* rb = rbuf + (size_t)slot * kBuf + ((uintptr_t)source(task) & 15);
+      local_sort_staged<EW, kThreads>(lsm, rb, out, task.count, task.lo, task.hi, p.key, stats, err);
+      if (threadIdx.x == 0) {
+        c.parity ^= 1u << slot;
+        c.dirty = kDirtyTable;
+        atomicAdd(stats + STAT_LOCAL, 1u);
+      }
+    }
+    if (threadIdx.x == 0) {
+      // a split's children were pushed before it counts as finished (their
+      // pending increments come first, so pending cannot reach zero early)
+      if (split) __threadfence();
+      atomicSub(&*q.pending, 1u);
+      uint32_t n = c.next_idx;
+      bool have;
+      SortTask nt{};
+      if (n != kNoClaim && c.next_ready) {
+        nt = c.next;
+        have = true;
+      } else {
+        if (n == kNoClaim) n = atomicAdd(q.head, 1u);
+        have = engine_wait(q, n, err);
+        if (have) nt = q.task[n];
+      }
+      const uint32_t nxt = cur ^ 1u;
+      const uint32_t nslot = staged ? (slot ^ 1) : slot;  // after a local task, the other buffer
+      c.state[nxt] = have ? ENGINE_HAVE : ENGINE_DONE;
+      c.task[nxt] = nt;
+      c.slot[nxt] = nslot;
+      c.loaded[nxt] = c.next_loaded;
+      if (have && engine_staged<EW>(nt) && !c.next_loaded) {
+        issue(nt, nslot);
+        c.loaded[nxt] = 1;
+      }
+      c.next_idx = kNoClaim;
+      c.next_ready = 0;
+      c.next_loaded = 0;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_engine_seed(const SortTask* __restrict__ split, const uint32_t* __restrict__ nsplit,
+                              const SortTask* __restrict__ local, const uint32_t* __restrict__ nlocal,
+                              uint32_t cap_split, uint32_t cap_local, EngineQueue q, uint32_t* err) {
+  const uint32_t ns = min(*nsplit, cap_split), nl = min(*nlocal, cap_local);
+  const uint32_t total = ns + nl;
+  if (total > q.cap) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_error(err, DEV_ERR_TASK_OVERFLOW);
+    return;
+  }
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    q.task[i] = i < ns ? split[i] : local[i - ns];
+    q.ready[i] = 1u;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *q.tail = total;
+    *q.head = 0;
+    *q.pending = total;
   }
 }
 
@@ -2113,6 +2449,32 @@ cudaError_t run_local(const HsortParams& p, const SortTask* tasks, const uint32_
         k_local<EW><<<local_grid<EW>(), kLocalThreads, sm, stream>>>(p, tasks, ntasks, cap, work_counter, stats);
     }
     note_launches(1);
+  });
+  if (!ok) return cudaErrorInvalidValue;
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+bool engine_supported(uint32_t elsize) { return elsize % 4 == 0 && elsize / 4 >= 2 && elsize / 4 <= 4; }
+
+cudaError_t run_engine(const HsortParams& p, const TaskListsHost& seed, SortTask* qtask, uint32_t* qready,
+                       uint32_t* qctl, uint32_t qcap, uint32_t* stats, uint32_t* err, cudaStream_t stream) {
+  EngineQueue q{qtask, qready, qctl, qctl + kEngineCtlStride, qctl + 2 * kEngineCtlStride, qcap};
+  cudaError_t e = cudaMemsetAsync(qready, 0, sizeof(uint32_t) * qcap, stream);
+  if (e != cudaSuccess) return e;
+  k_engine_seed<<<num_sms() * 2, 256, 0, stream>>>(seed.split_in, seed.nsplit_in, seed.local, seed.nlocal,
+                                                   seed.cap_split, seed.cap_local, q, err);
+  note_launches(1);
+  bool ok = dispatch_ew(p.elsize, [&](auto ewc) {
+    constexpr int EW = decltype(ewc)::value;
+    if constexpr (EW >= 2 && EW <= 4) {
+      const size_t sm = engine_smem_bytes<EW>();
+      e = set_smem((const void*)k_engine<EW>, sm);
+      if (e == cudaSuccess) k_engine<EW><<<num_sms() * 2, kThreads, sm, stream>>>(p, q, stats);
+      note_launches(1);
+    } else {
+      e = cudaErrorInvalidValue;
+    }
   });
   if (!ok) return cudaErrorInvalidValue;
   if (e != cudaSuccess) return e;

@@ -225,5 +225,16 @@ cudaError_t run_split_round(const HsortParams& p, const TaskListsHost& lists, ui
                             uint32_t* stats, uint32_t* err, cudaStream_t stream);
 cudaError_t run_local(const HsortParams& p, const SortTask* tasks, const uint32_t* ntasks, uint32_t cap,
                       uint32_t* work_counter, uint32_t* stats, cudaStream_t stream);
+// The persistent level-2 engine (records of 8, 12 or 16 bytes): the tasks of
+// seed.split_in (count *seed.nsplit_in, largest first) then seed.local go
+// into the device queue (qtask / qready of qcap entries, qctl 3 words), and
+// one launch runs every split, local sort and copy, including the ones the
+// splits produce.  Tasks must lie at their final positions (no reserved
+// regions).  err: task overflow or a wait that ran out.
+bool engine_supported(uint32_t elsize);
+// qctl: tail, head and pending, kEngineCtlStride words apart (one cache line each).
+constexpr uint32_t kEngineCtlStride = 32;
+cudaError_t run_engine(const HsortParams& p, const TaskListsHost& seed, SortTask* qtask, uint32_t* qready,
+                       uint32_t* qctl, uint32_t qcap, uint32_t* stats, uint32_t* err, cudaStream_t stream);
 
 }  // namespace gb

@@ -41,7 +41,7 @@ class Stats(ctypes.Structure):
                 ("stage_ms", ctypes.c_float * 6), ("launches", ctypes.c_uint32),
                 ("splitter_fallback", ctypes.c_uint32), ("heavy_keys", ctypes.c_uint32),
                 ("refined_splits", ctypes.c_uint32), ("pipelined", ctypes.c_uint32),
-                ("region_overflow", ctypes.c_uint32)]
+                ("region_overflow", ctypes.c_uint32), ("engine", ctypes.c_uint32)]
 
     STAGES = ("splitters", "count", "scan", "scatter", "split", "local")
 
@@ -66,14 +66,19 @@ _U32 = ctypes.c_uint32
 _U64 = ctypes.c_uint64
 _I = ctypes.c_int
 
+LEVEL2 = {"default": 0, "rounds": 1, "engine": 2}
+LEVEL2_NAMES = {v: k for k, v in LEVEL2.items()}
+
+
 class Tuning(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int32), ("max_buckets", ctypes.c_uint32),
                 ("sample_per_bucket", ctypes.c_uint32), ("ms", ctypes.c_float),
-                ("reserved", ctypes.c_uint32 * 4)]
+                ("level2", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 3)]
 
     def as_dict(self):
         return {"method": METHOD_NAMES.get(self.method, self.method), "max_buckets": self.max_buckets,
-                "sample_per_bucket": self.sample_per_bucket, "ms": self.ms}
+                "sample_per_bucket": self.sample_per_bucket, "ms": self.ms,
+                "level2": LEVEL2_NAMES.get(self.level2, self.level2)}
 
 
 # name: (restype, argtypes)

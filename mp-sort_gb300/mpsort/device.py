@@ -85,10 +85,10 @@ def autotune(n, dtype, orderby, d_records=0):
     return t.as_dict()
 
 
-def tuning_set(n, dtype, orderby, method, max_buckets=0, sample_per_bucket=0):
+def tuning_set(n, dtype, orderby, method, max_buckets=0, sample_per_bucket=0, level2="default"):
     dtype = numpy.dtype(dtype)
     desc = _desc(dtype, orderby)
-    t = _lib.Tuning(_lib.METHODS[method], max_buckets, sample_per_bucket, 0.0)
+    t = _lib.Tuning(_lib.METHODS[method], max_buckets, sample_per_bucket, 0.0, _lib.LEVEL2[level2])
     _lib.check(_lib.lib().gbsort_tuning_set(n, dtype.itemsize, ctypes.byref(desc), ctypes.byref(t)))
 
 

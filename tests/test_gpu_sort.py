@@ -643,3 +643,32 @@ def test_lookback_wait_runs_out_and_reports(mp):
     assert L.gbsort_debug_lookback(n, 0xFFFFFFFF, 64) == 0
     rng = numpy.random.default_rng(3)
     check(mp, make([('key', 'u8'), ('val', 'i8')], 'key', 100_000, "uniform", rng), 'key', "lsd")
+
+
+# ------------------------------------------------- level 2: engine vs rounds --
+@pytest.mark.parametrize("level2", ["rounds", "engine"])
+@pytest.mark.parametrize("layout", [([('key', 'u8'), ('val', 'i8')], 'key'),
+                                    ([('key', 'i4'), ('payload', 'u4')], 'key'),
+                                    ([('key', 'u8'), ('value', 'f4')], 'key')])
+def test_level2_engine_and_rounds(mp, level2, layout):
+    """Level 2 as the persistent engine (one launch over a device task queue)
+    and as split rounds give the oracle's order on uniform, Zipf and
+    duplicate-heavy keys, for both splitter methods (selected through the
+    tuning table, as the autotuner would)."""
+    from mpsort import device
+    dtype, key = layout
+    n = 3_000_017
+    rng = numpy.random.default_rng(11)
+    device.tuning_clear()
+    try:
+        for dist in ("uniform", "zipf", "dups"):
+            a = make(dtype, key, n, dist, rng)
+            exp = O.numpy_sorted(a, key)
+            for method in ("plain", "learned"):
+                device.tuning_set(n, a.dtype, key, method, level2=level2)
+                out = numpy.empty_like(a)
+                mp.sort(a, key, out=out)
+                assert out.tobytes() == exp.tobytes(), (dist, method)
+                assert mp.last_stats()["engine"] == (1 if level2 == "engine" else 0)
+    finally:
+        device.tuning_clear()
