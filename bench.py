@@ -423,15 +423,27 @@ def run_config(args):
         buf, dt, offs = W.segments_3(torch)
         out = torch.empty_like(buf)
         n = int(offs[-1])
-        ms = timed(lambda: dev.sort_segments(buf.data_ptr(), out.data_ptr(), offs, dt, 'key', 'auto', sp), args.steps)
+        # the segment autotuner picks level 2 and the threshold for sorting a
+        # segment on its own; the batch is then one graph-captured plan
+        tuned = dev.autotune_segments(offs, dt, 'key', buf.data_ptr())
+        plan = dev.Plan(0, dt, 'key', segments=offs)
+
+        def plan_step():
+            plan.sort(buf.data_ptr(), out.data_ptr(), sp)
+            plan.wait()
+        ms = timed(plan_step, args.steps)
         stats = mpsort.last_stats()
+        ms_call = timed(lambda: dev.sort_segments(buf.data_ptr(), out.data_ptr(), offs, dt, 'key', 'auto', sp),
+                        args.steps)
 
         def per_array():
             for i in range(len(offs) - 1):
                 a, b = int(offs[i]), int(offs[i + 1])
                 dev.sort(buf.data_ptr() + a * 8, out.data_ptr() + a * 8, b - a, dt, 'key', 'plain', sp)
         ms_loop = timed(per_array, 1)
-        dev.sort_segments(buf.data_ptr(), out.data_ptr(), offs, dt, 'key', 'auto', sp)
+        out.zero_()
+        plan_step()
+        plan.close()
         torch.cuda.synchronize()
         seg_start = torch.zeros(n, dtype=torch.bool, device="cuda")
         seg_start[torch.from_numpy(offs[:-1].astype(numpy.int64)).cuda().clamp_(max=n - 1)] = True
@@ -449,7 +461,10 @@ def run_config(args):
             kind, cores = cpu_sort_seconds(host[:16].copy(), 'key', repeat=1)[1:]
             res["cpu_baseline"] = {"value": int(offs[k]) / t, "unit": UNIT, "cores": cores, "kind": kind,
                                    "sample": "the first %d arrays (%d records), one CPU sort per array" % (k, int(offs[k]))}
-        res.update(value=n / (ms / 1e3), n=n, nseg=len(offs) - 1, ms_per_step=ms,
+        res.update(value=n / (ms / 1e3), n=n, nseg=len(offs) - 1, ms_per_step=ms, graph=True,
+                   graph_kernel_launches=stats["launches"], level2_engine=bool(stats["engine"]),
+                   segments_sorted_alone=stats["sample"], tuned_entry=tuned,
+                   synchronous_call_records_per_s=n / (ms_call / 1e3),
                    per_array_loop_records_per_s=n / (ms_loop / 1e3), per_array_loop_ms=ms_loop,
                    parity=parity, sort_stats=stats)
     elif args.config == "4":

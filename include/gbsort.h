@@ -132,8 +132,13 @@ GBSORT_API int gbsort_sort_radix_host(void *base, size_t nmemb, size_t elsize,
 
 /* Batched sort of nseg independent segments in one pipeline: segment i is
  * records [seg_offsets[i], seg_offsets[i+1]) of d_in (device memory; the
- * offsets array is in host memory, nseg + 1 entries).  Each segment comes
- * out sorted in place of its range in d_out. */
+ * offsets array is in host memory, nseg + 1 entries, non-decreasing from 0,
+ * below 2^32 - 1 records in all).  Each segment comes out sorted in place of
+ * its range in d_out.  With a histogram-sort layout, segments above a size
+ * threshold (default 2^22 records, or the segment tuning entry's) take the
+ * whole-GPU sort one after the other and the rest share one level-2 pipeline
+ * (the persistent engine, or split rounds, as tuned) fed with one task per
+ * segment; otherwise each segment is sorted by the LSD path.  Waits. */
 GBSORT_API int gbsort_sort_segments_device(const void *d_in, void *d_out, const uint64_t *seg_offsets,
                                 size_t nseg, size_t elsize, const gbsort_key_desc *key,
                                 int method, void *stream);
@@ -272,6 +277,18 @@ GBSORT_API int gbsort_tuning_set(size_t nmemb, size_t elsize, const gbsort_key_d
 GBSORT_API int gbsort_tuning_get(size_t nmemb, size_t elsize, const gbsort_key_desc *key,
                       gbsort_tuning *t);
 GBSORT_API int gbsort_tuning_clear(void);
+/* gbsort_autotune_segments times segmented sorts of this batch (the
+ * caller's device records, read only, or pseudo-random ones) with level 2
+ * as split rounds and as the engine and with segment-size thresholds of
+ * 2^20, 2^22 and the largest segment (records of larger segments take the
+ * whole-GPU sort), returns the fastest and stores it under the batch's size
+ * class in a key space of its own (size_class + 128 in the tuning file, with
+ * the threshold in reserved[0], the file's ninth column).  Segmented sorts
+ * and segmented plans use that entry. */
+GBSORT_API int gbsort_autotune_segments(const uint64_t *seg_offsets, size_t nseg, size_t elsize,
+                             const gbsort_key_desc *key, const void *d_records, gbsort_tuning *best);
+GBSORT_API int gbsort_tuning_get_segments(size_t nmemb, size_t elsize, const gbsort_key_desc *key,
+                               gbsort_tuning *t);
 GBSORT_API int gbsort_tuning_save(const char *path);
 GBSORT_API int gbsort_tuning_load(const char *path);
 
@@ -296,6 +313,11 @@ GBSORT_API int gbsort_tuning_load(const char *path);
 typedef struct gbsort_plan gbsort_plan;
 GBSORT_API int gbsort_plan_create(gbsort_plan **plan, size_t nmemb, size_t elsize,
                        const gbsort_key_desc *key, int method);
+/* A plan for gbsort_sort_segments_device of a fixed batch (the offsets are
+ * copied; method GBSORT_AUTO, _HISTOGRAM_PLAIN or _LEARNED for the segments
+ * sorted on their own); needs a histogram-sort layout. */
+GBSORT_API int gbsort_plan_create_segments(gbsort_plan **plan, const uint64_t *seg_offsets, size_t nseg,
+                                size_t elsize, const gbsort_key_desc *key, int method);
 GBSORT_API int gbsort_plan_sort(gbsort_plan *plan, const void *d_in, void *d_out, void *stream);
 GBSORT_API int gbsort_plan_wait(gbsort_plan *plan);
 GBSORT_API int gbsort_plan_destroy(gbsort_plan *plan);

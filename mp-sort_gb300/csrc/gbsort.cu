@@ -165,6 +165,7 @@ struct Context {
   DevBuf small;            // splitters, counts, tasks, model, counters
   DevBuf radix;            // host radix bytes (callback path)
   DevBuf part;             // first partition of sorts of 2^32 records or more
+  DevBuf seg;              // segment offsets and error words of a segmented sort
   DevBuf vh;               // multiset hashes of a self-checked sort
   HostCounters* hc = nullptr;
   cudaEvent_t ev[8] = {};  // stage boundaries of the histogram sort
@@ -199,7 +200,7 @@ int ctx_init(Context& c, int dev, bool blocking) {
 
 void ctx_destroy(Context& c) {
   if (c.stream) cudaStreamSynchronize(c.stream);
-  DevBuf* bufs[] = {&c.A, &c.B, &c.hin, &c.hout, &c.keysA, &c.keysB, &c.idxA, &c.idxB, &c.small, &c.radix, &c.part, &c.vh};
+  DevBuf* bufs[] = {&c.A, &c.B, &c.hin, &c.hout, &c.keysA, &c.keysB, &c.idxA, &c.idxB, &c.small, &c.radix, &c.part, &c.vh, &c.seg};
   for (DevBuf* b : bufs) b->release();
   if (c.cstream) cudaStreamSynchronize(c.cstream);
   for (cudaEvent_t& e : c.ev)
@@ -544,6 +545,24 @@ int run_level2(const HsortParams& p, const Level2& l2, uint32_t* stats, uint32_t
   return GBSORT_OK;
 }
 
+uint32_t hsort_sample_size(uint32_t n, int nb, const Knobs& knobs) {
+  const uint64_t spb = knobs.sample_per_bucket ? (uint64_t)knobs.sample_per_bucket : 128;
+  return nb > 1 ? (uint32_t)std::min<uint64_t>(n, std::max<uint64_t>(4096, (uint64_t)nb * spb)) : 0;
+}
+
+// Bytes of the small device buffer a histogram sort of n records uses
+// (G: count chunks).
+size_t hsort_small_bytes(uint32_t n, const Knobs& knobs, int G) {
+  const int nb = choose_buckets(n, knobs);
+  const uint32_t s = hsort_sample_size(n, nb, knobs);
+  const uint32_t cap_split = (uint32_t)nb + n / 4096 + 4096;
+  const uint32_t cap_local = 4u * (uint32_t)nb + n / 512 + 65536;
+  const int nleaf = 1 << 11;
+  return (size_t)s * 16 + (size_t)nb * 8 + (size_t)nb * G * 8 + Level2::bytes(cap_split, cap_local) +
+         lsd_scratch_bytes(std::max<uint32_t>(s, 1), 1) + (size_t)nleaf * 64 + (size_t)nb * 24 + sizeof(HeavyTable) +
+         (4 << 20);
+}
+
 // Enqueues the whole histogram sort on `st` without waiting for the host
 // anywhere (so it can be captured into a CUDA graph); the device counters
 // end up in c.hc once the stream reaches the end.  hsort_collect reads them.
@@ -551,8 +570,7 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
                   bool learned, bool timing, const Knobs& knobs, cudaStream_t st, const HostPipe* hp = nullptr) {
   const int nb = choose_buckets(n, knobs);
   const int grid = hsort_grid(n);
-  const uint64_t spb = knobs.sample_per_bucket ? (uint64_t)knobs.sample_per_bucket : 128;
-  const uint32_t s = nb > 1 ? (uint32_t)std::min<uint64_t>(n, std::max<uint64_t>(4096, (uint64_t)nb * spb)) : 0;
+  const uint32_t s = hsort_sample_size(n, nb, knobs);
   // pipelined: the input goes up in pieces, each cut into `grid` count
   // chunks, and is scattered as it lands into bucket regions reserved from
   // the sample (kRegion*); scratch A holds the regions
@@ -574,10 +592,7 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
   const uint32_t cap_local = 4u * (uint32_t)nb + n / 512 + 65536;
   const int lbits = 11;
   const int nleaf = 1 << lbits;
-  size_t small_bytes = (size_t)s * 16 + (size_t)nb * 8 + (size_t)nb * G * 8 + Level2::bytes(cap_split, cap_local) +
-                       lsd_scratch_bytes(std::max<uint32_t>(s, 1), 1) + (size_t)nleaf * 64 + (size_t)nb * 24 +
-                       sizeof(HeavyTable) + (4 << 20);
-  GB_CUDA(c.small.ensure(small_bytes));
+  GB_CUDA(c.small.ensure(hsort_small_bytes(n, knobs, G)));
   Bump bump{c.small.as<uint8_t>()};
   uint32_t* counters = bump.take<uint32_t>(CNT_WORDS);
   uint32_t* stats = counters;
@@ -1179,22 +1194,195 @@ int gbsort_sort_radix_host(void* base, size_t nmemb, size_t elsize,
   return GBSORT_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// ------------------------------------------------------ segmented sorts ----
+// Shape of a batched segmented sort (its tuning entry: method / max_buckets
+// for the segments sorted on their own, level2 for the shared pipeline,
+// reserved[0] the size above which a segment is sorted on its own).
+struct SegKnobs {
+  int big_method = GBSORT_HISTOGRAM_LEARNED;
+  Knobs big;
+  int level2 = GBSORT_LEVEL2_DEFAULT;
+  uint64_t big_above = (uint64_t)1 << 22;  // records: a segment this large fills the GPU on its own
+};
+
+uint64_t seg_tune_key(uint32_t elsize, uint32_t width, uint64_t n) {
+  return tune_key(elsize, width, 0x80u | size_class(n));  // a key space of its own
+}
+
+SegKnobs seg_knobs(uint32_t elsize, const gbsort_key_desc* key, uint64_t n, int method) {
+  SegKnobs k;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(seg_tune_key(elsize, key->word[0].width, n));
+    if (it != g_tune.end()) {
+      const gbsort_tuning& t = it->second;
+      if (t.method == GBSORT_HISTOGRAM_PLAIN || t.method == GBSORT_HISTOGRAM_LEARNED) k.big_method = t.method;
+      k.big.max_buckets = (int)t.max_buckets;
+      k.level2 = (int)t.level2;
+      if (t.reserved[0]) k.big_above = t.reserved[0];
+    }
+  }
+  if (method == GBSORT_HISTOGRAM_PLAIN || method == GBSORT_HISTOGRAM_LEARNED) k.big_method = method;
+  return k;
+}
+
+// Device work of a segmented sort of the histogram-sort layouts, enqueued
+// on st without waiting for the host anywhere (graph plans capture it):
+// segments above k.big_above records take the whole-GPU histogram sort one
+// after the other; the rest share one level-2 pipeline (the persistent
+// engine by default) fed by one task per segment.  d_offs: the nseg + 1
+// offsets on the device; errs: 1 + (segments sorted on their own) device
+// words that receive each part's error word.  Buffers are sized once,
+// before anything is enqueued.
+int segments_enqueue(Context& c, const void* d_in, void* d_out, const std::vector<uint64_t>& offs,
+                     const uint64_t* d_offs, uint32_t E, const gbsort_key_desc* key, const SegKnobs& k,
+                     uint32_t* errs, cudaStream_t st) {
+  const size_t nseg = offs.size() - 1;
+  const uint32_t N = (uint32_t)offs[nseg];
+  const uint32_t cap_split = (uint32_t)nseg * 2 + N / 4096 + 4096;
+  const uint32_t cap_local = 4u * (uint32_t)nseg + N / 512 + 65536;
+  // the largest small-buffer layout of any part, before any work is enqueued
+  size_t small_need = Level2::bytes(cap_split, cap_local) + (1 << 20);
+  uint32_t nbig = 0;
+  for (size_t i = 0; i < nseg; ++i) {
+    const uint64_t m = offs[i + 1] - offs[i];
+    if (m > k.big_above) {
+      ++nbig;
+      small_need = std::max(small_need, hsort_small_bytes((uint32_t)m, k.big, hsort_grid((uint32_t)m)));
+    }
+  }
+  GB_CUDA(c.small.ensure(small_need));
+  GB_CUDA(c.A.ensure((size_t)N * E + kScratchSlack));
+  GB_CUDA(c.B.ensure((size_t)N * E + kScratchSlack));
+  uint32_t bi = 0;
+  uint64_t nbig_records = 0;
+  for (size_t i = 0; i < nseg; ++i) {
+    const uint64_t a = offs[i], m = offs[i + 1] - offs[i];
+    if (m <= k.big_above) continue;
+    int rc = hsort_enqueue(c, (const uint8_t*)d_in + a * E, (uint8_t*)d_out + a * E, (uint32_t)m, E, key,
+                           k.big_method == GBSORT_HISTOGRAM_LEARNED, false, k.big, st);
+    if (rc) return rc;
+    // this part's error word, and its unfinished tasks as an error, kept before the next part
+    uint32_t* cnt = c.small.as<uint32_t>();  // hsort_enqueue's counters come first in the small buffer
+    GB_CUDA(require_zero(c.run_engine ? cnt + CNT_ENGINE + 2 * kEngineCtlStride : cnt + CNT_L2 + (kSplitRounds & 1),
+                         cnt + CNT_ERR, st));
+    GB_CUDA(cudaMemcpyAsync(errs + 1 + bi, cnt + CNT_ERR, 4, cudaMemcpyDeviceToDevice, st));
+    ++bi;
+    nbig_records += m;
+  }
+  Bump bump{c.small.as<uint8_t>()};
+  uint32_t* counters = bump.take<uint32_t>(CNT_WORDS);
+  uint32_t* stats = counters;
+  uint32_t* err = counters + CNT_ERR;
+  Level2 l2;
+  l2.carve(bump, counters, cap_split, cap_local);
+  GB_CUDA(cudaMemsetAsync(counters, 0, CNT_WORDS * sizeof(uint32_t), st));
+  if (nbig_records < N) {
+    GB_CUDA(cudaMemcpyAsync(c.A.p, d_in, (size_t)N * E, cudaMemcpyDeviceToDevice, st));
+    GB_CUDA(segment_ranges(c.A.as<uint8_t>(), E, key->word[0], d_offs, (uint32_t)nseg, k.big_above, l2.split[0],
+                           l2.nsplit, cap_split, err, st));
+    HsortParams p{};
+    p.in = (const uint8_t*)d_in;
+    p.out = (uint8_t*)d_out;
+    p.bufA = c.A.as<uint8_t>();
+    p.bufB = c.B.as<uint8_t>();
+    p.n = N;
+    p.elsize = E;
+    p.key = key->word[0];
+    p.a_cap = N;
+    const bool engine = use_engine(E, k.level2, true);
+    if (engine) {
+      GB_CUDA(run_engine(p, l2.round(0), l2.qtask, l2.qready, l2.qctl, l2.qcap, stats, err, st));
+      GB_CUDA(require_zero(l2.qctl + 2 * kEngineCtlStride, err, st));
+    } else {
+      for (int r = 0; r < kSplitRounds; ++r) {
+        TaskListsHost L = l2.round(r);
+        GB_CUDA(cudaMemsetAsync(L.nsplit_out, 0, sizeof(uint32_t), st));
+        GB_CUDA(run_split_round(p, L, l2.work, stats, err, st));
+      }
+      GB_CUDA(run_local(p, l2.local, l2.nlocal, l2.cap_local, l2.work, stats, st));
+      GB_CUDA(require_zero(l2.nsplit + (kSplitRounds & 1), err, st));
+    }
+    c.run_engine = engine;
+  } else {
+    c.run_engine = false;
+  }
+  GB_CUDA(cudaMemcpyAsync(errs, err, 4, cudaMemcpyDeviceToDevice, st));
+  GB_CUDA(cudaMemcpyAsync(c.hc->c, counters, CNT_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  c.run_nbuckets = (uint32_t)nseg;
+  c.run_sample = nbig;
+  return GBSORT_OK;
+}
+
+// Status and statistics of a segmented sort once its stream reached the
+// end: the error words (h_errs, 1 + segments sorted on their own) and the
+// shared pipeline's counters.
+int segments_collect(Context& c, const uint32_t* h_errs, uint32_t nerrs) {
+  for (uint32_t i = 0; i < nerrs; ++i)
+    if (h_errs[i]) {
+      set_err("segmented sort device check failed: code %u (part %u)", h_errs[i], i);
+      return GBSORT_ERR_INTERNAL;
+    }
+  const uint32_t* h = c.hc->c;
+  g_stats = gbsort_stats{};
+  g_stats.method = GBSORT_HISTOGRAM_PLAIN;
+  g_stats.nbuckets = c.run_nbuckets;
+  g_stats.sample = c.run_sample;  // segments sorted on their own
+  g_stats.local_sorts = h[STAT_LOCAL];
+  g_stats.splits = h[STAT_SPLIT];
+  g_stats.copies = h[STAT_COPY];
+  g_stats.resplits = h[STAT_PUSHED];
+  g_stats.bigbin_passes = h[STAT_BIGBIN];
+  g_stats.engine = c.run_engine ? 1u : 0u;
+  return GBSORT_OK;
+}
+
+bool segments_args_ok(const uint64_t* seg_offsets, size_t nseg) {
+  if (!seg_offsets || seg_offsets[0] != 0 || seg_offsets[nseg] >= 0xffffffffull) return false;
+  for (size_t i = 0; i < nseg; ++i)
+    if (seg_offsets[i + 1] < seg_offsets[i]) return false;
+  return true;
+}
+
+// One segmented sort from start to finish on `st` (synchronises).
+int segments_run(Context& c, const void* d_in, void* d_out, const uint64_t* seg_offsets, size_t nseg, uint32_t E,
+                 const gbsort_key_desc* key, const SegKnobs& k, cudaStream_t st) {
+  std::vector<uint64_t> offs(seg_offsets, seg_offsets + nseg + 1);
+  uint32_t nbig = 0;
+  for (size_t i = 0; i < nseg; ++i) nbig += offs[i + 1] - offs[i] > k.big_above;
+  GB_CUDA(c.seg.ensure((nseg + 1) * 8 + (size_t)(nbig + 1) * 4 + 256));
+  uint64_t* d_offs = c.seg.as<uint64_t>();
+  uint32_t* errs = reinterpret_cast<uint32_t*>(d_offs + nseg + 1);
+  GB_CUDA(cudaMemcpyAsync(d_offs, offs.data(), (nseg + 1) * 8, cudaMemcpyHostToDevice, st));
+  GB_CUDA(cudaMemsetAsync(errs, 0, (size_t)(nbig + 1) * 4, st));
+  int rc = segments_enqueue(c, d_in, d_out, offs, d_offs, E, key, k, errs, st);
+  if (rc) return rc;
+  std::vector<uint32_t> h_errs(nbig + 1);
+  GB_CUDA(cudaMemcpyAsync(h_errs.data(), errs, h_errs.size() * 4, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  return segments_collect(c, h_errs.data(), nbig + 1);
+}
+
+}  // namespace
+
+extern "C" {
+
 int gbsort_sort_segments_device(const void* d_in, void* d_out, const uint64_t* seg_offsets, size_t nseg,
                                 size_t elsize, const gbsort_key_desc* key, int method, void* stream) {
   if (nseg == 0) return GBSORT_OK;
-  if (!seg_offsets || !d_in || !d_out) return GBSORT_ERR_BAD_ARG;
-  const uint64_t n = seg_offsets[nseg];
-  if (n == 0) return GBSORT_OK;
-  if (n >= 0xffffffffull || seg_offsets[0] != 0) return GBSORT_ERR_BAD_ARG;
-  for (size_t i = 0; i < nseg; ++i)
-    if (seg_offsets[i + 1] < seg_offsets[i]) return GBSORT_ERR_BAD_ARG;
+  if (!d_in || !d_out || !segments_args_ok(seg_offsets, nseg)) return GBSORT_ERR_BAD_ARG;
+  if (seg_offsets[nseg] == 0) return GBSORT_OK;
   if (!key_ok(key, elsize)) return GBSORT_ERR_BAD_ARG;
   Context* c = nullptr;
   int rc = get_ctx(&c);
   if (rc) return rc;
   std::lock_guard<std::mutex> lk(c->mu);
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-  const uint32_t E = (uint32_t)elsize, N = (uint32_t)n;
+  const uint32_t E = (uint32_t)elsize;
   if (!hsort_layout_ok(d_in, d_out, E, key) || method == GBSORT_LSD) {
     // generic path: one LSD sort per segment
     for (size_t i = 0; i < nseg; ++i) {
@@ -1206,64 +1394,69 @@ int gbsort_sort_segments_device(const void* d_in, void* d_out, const uint64_t* s
     }
     return GBSORT_OK;
   }
-  // Segments large enough to fill the GPU on their own go through the full
-  // histogram sort one at a time; the rest share one task pipeline.
-  const uint64_t kBigSegment = 1ull << 22;
-  uint64_t nbig = 0;
-  for (size_t i = 0; i < nseg; ++i) {
-    uint64_t a = seg_offsets[i], b = seg_offsets[i + 1];
-    if (b - a <= kBigSegment) continue;
-    rc = sort_device_locked(*c, (const uint8_t*)d_in + a * E, (uint8_t*)d_out + a * E, b - a, E, key,
-                            method == GBSORT_AUTO ? GBSORT_HISTOGRAM_LEARNED : method, st);
-    if (rc) return rc;
-    nbig += b - a;
-  }
-  if (nbig == n) return GBSORT_OK;
-  GB_CUDA(c->A.ensure((size_t)N * E + kScratchSlack));
-  GB_CUDA(c->B.ensure((size_t)N * E + kScratchSlack));
-  const uint32_t cap_split = (uint32_t)nseg * 2 + N / 4096 + 4096;
-  const uint32_t cap_local = 4u * (uint32_t)nseg + N / 512 + 65536;
-  GB_CUDA(c->small.ensure(Level2::bytes(cap_split, cap_local) + (nseg + 1) * 8 + (1 << 20)));
-  Bump bump{c->small.as<uint8_t>()};
-  uint32_t* counters = bump.take<uint32_t>(CNT_WORDS);
-  uint32_t* stats = counters;
-  uint32_t* err = counters + CNT_ERR;
-  uint64_t* offs = bump.take<uint64_t>(nseg + 1);
-  Level2 l2;
-  l2.carve(bump, counters, cap_split, cap_local);
-  GB_CUDA(cudaMemsetAsync(counters, 0, CNT_WORDS * sizeof(uint32_t), st));
-  GB_CUDA(cudaMemcpyAsync(offs, seg_offsets, (nseg + 1) * 8, cudaMemcpyHostToDevice, st));
-  GB_CUDA(cudaMemcpyAsync(c->A.p, d_in, (size_t)N * E, cudaMemcpyDeviceToDevice, st));
-  GB_CUDA(segment_ranges(c->A.as<uint8_t>(), E, key->word[0], offs, (uint32_t)nseg, kBigSegment, l2.split[0],
-                         l2.nsplit, cap_split, err, st));
-  HsortParams p{};
-  p.in = (const uint8_t*)d_in;
-  p.out = (uint8_t*)d_out;
-  p.bufA = c->A.as<uint8_t>();
-  p.bufB = c->B.as<uint8_t>();
-  p.n = N;
-  p.elsize = E;
-  p.key = key->word[0];
-  p.a_cap = N;
-  rc = run_level2(p, l2, stats, err, st);
+  const unsigned long long l0 = launch_count();
+  rc = segments_run(*c, d_in, d_out, seg_offsets, nseg, E, key, seg_knobs(E, key, seg_offsets[nseg], method), st);
+  if (rc == GBSORT_OK) g_stats.launches = (uint32_t)(launch_count() - l0);
+  return rc;
+}
+
+int gbsort_autotune_segments(const uint64_t* seg_offsets, size_t nseg, size_t elsize, const gbsort_key_desc* key,
+                             const void* d_records, gbsort_tuning* best) {
+  if (!best || nseg == 0 || !segments_args_ok(seg_offsets, nseg) || seg_offsets[nseg] == 0 ||
+      !key_ok(key, elsize) || key->nwords != 1)
+    return GBSORT_ERR_BAD_ARG;
+  Context* c = nullptr;
+  int rc = get_ctx(&c);
   if (rc) return rc;
-  GB_CUDA(cudaMemcpyAsync(c->hc->c, counters, CNT_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-  GB_CUDA(cudaStreamSynchronize(st));
-  const uint32_t* h = c->hc->c;
-  const uint32_t left = use_engine(E, 0, true) ? h[CNT_ENGINE + 2 * kEngineCtlStride] : h[CNT_L2 + (kSplitRounds & 1)];
-  if (h[CNT_ERR] || left) {
-    set_err("segmented sort device check failed: code %u, %u tasks left", h[CNT_ERR], left);
-    return GBSORT_ERR_INTERNAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaStream_t st = c->stream;
+  const uint32_t E = (uint32_t)elsize;
+  const uint64_t n = seg_offsets[nseg];
+  const size_t bytes = (size_t)n * E;
+  GB_CUDA(c->hout.ensure(bytes));
+  const void* in = d_records;
+  if (!in) {
+    GB_CUDA(c->hin.ensure(bytes));
+    GB_CUDA(fill_hash(c->hin.p, bytes, 0x5eed5eedull, st));
+    in = c->hin.p;
   }
-  g_stats = gbsort_stats{};
-  g_stats.method = GBSORT_HISTOGRAM_PLAIN;
-  g_stats.nbuckets = (uint32_t)nseg;
-  g_stats.local_sorts = h[STAT_LOCAL];
-  g_stats.splits = h[STAT_SPLIT];
-  g_stats.copies = h[STAT_COPY];
-  g_stats.resplits = h[STAT_PUSHED];
-  g_stats.bigbin_passes = h[STAT_BIGBIN];
-  g_stats.engine = use_engine(E, 0, true) ? 1u : 0u;
+  if (!hsort_layout_ok(in, c->hout.p, E, key)) {
+    set_err("segment tuning needs a histogram-sort layout");
+    return GBSORT_ERR_UNSUPPORTED;
+  }
+  uint64_t largest = 0;
+  for (size_t i = 0; i < nseg; ++i) largest = std::max(largest, seg_offsets[i + 1] - seg_offsets[i]);
+  gbsort_tuning win{};
+  win.ms = -1.f;
+  for (int level2 : {GBSORT_LEVEL2_ROUNDS, GBSORT_LEVEL2_ENGINE}) {
+    if (level2 == GBSORT_LEVEL2_ENGINE && !engine_supported(E)) continue;
+    for (uint64_t above : {(uint64_t)1 << 20, (uint64_t)1 << 22, largest}) {
+      SegKnobs k;
+      k.level2 = level2;
+      k.big_above = std::max<uint64_t>(above, 4096);
+      float best_ms = -1.f;
+      for (int rep = 0; rep < 3; ++rep) {  // a warm-up, then the best of two
+        GB_CUDA(cudaEventRecord(c->ev[7], st));
+        const int r = segments_run(*c, in, c->hout.p, seg_offsets, nseg, E, key, k, st);
+        if (r) return r;
+        GB_CUDA(cudaEventRecord(c->ev[6], st));
+        GB_CUDA(cudaEventSynchronize(c->ev[6]));
+        float ms = 0.f;
+        GB_CUDA(cudaEventElapsedTime(&ms, c->ev[7], c->ev[6]));
+        if (rep > 0 && (best_ms < 0.f || ms < best_ms)) best_ms = ms;
+      }
+      if (win.ms < 0.f || best_ms < win.ms) {
+        win.method = GBSORT_HISTOGRAM_LEARNED;
+        win.max_buckets = 0;
+        win.level2 = (uint32_t)level2;
+        win.reserved[0] = (uint32_t)std::min<uint64_t>(k.big_above, 0xffffffffull);
+        win.ms = best_ms;
+      }
+    }
+  }
+  *best = win;
+  std::lock_guard<std::mutex> tl(g_tune_mu);
+  g_tune[seg_tune_key(E, key->word[0].width, n)] = win;
   return GBSORT_OK;
 }
 
@@ -1537,7 +1730,7 @@ int gbsort_release(void) {
   std::lock_guard<std::mutex> lk(c->mu);
   cudaStreamSynchronize(c->stream);
   DevBuf* bufs[] = {&c->A, &c->B, &c->hin, &c->hout, &c->keysA, &c->keysB, &c->idxA, &c->idxB, &c->small, &c->radix,
-                    &c->part, &c->vh};
+                    &c->part, &c->vh, &c->seg};
   for (DevBuf* b : bufs) b->release();
   return GBSORT_OK;
 }
@@ -1635,6 +1828,16 @@ int gbsort_tuning_get(size_t nmemb, size_t elsize, const gbsort_key_desc* key, g
   return GBSORT_OK;
 }
 
+int gbsort_tuning_get_segments(size_t nmemb, size_t elsize, const gbsort_key_desc* key, gbsort_tuning* t) {
+  if (!t || !key_ok(key, elsize)) return GBSORT_ERR_BAD_ARG;
+  if (key->nwords != 1) return GBSORT_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> tl(g_tune_mu);
+  auto it = g_tune.find(seg_tune_key((uint32_t)elsize, key->word[0].width, nmemb));
+  if (it == g_tune.end()) return GBSORT_ERR_UNSUPPORTED;
+  *t = it->second;
+  return GBSORT_OK;
+}
+
 int gbsort_tuning_clear(void) {
   std::lock_guard<std::mutex> tl(g_tune_mu);
   g_tune.clear();
@@ -1650,11 +1853,12 @@ int gbsort_tuning_save(const char* path) {
     return GBSORT_ERR_BAD_ARG;
   }
   std::lock_guard<std::mutex> tl(g_tune_mu);
-  fprintf(f, "# gbsort tuning: elsize key_width size_class method max_buckets sample_per_bucket ms level2\n");
+  fprintf(f, "# gbsort tuning: elsize key_width size_class method max_buckets sample_per_bucket ms level2 "
+             "big_above (size_class + 128: segmented sorts)\n");
   for (const auto& kv : g_tune)
-    fprintf(f, "%u %u %u %d %u %u %.4f %u\n", (unsigned)(kv.first >> 16), (unsigned)((kv.first >> 8) & 0xff),
+    fprintf(f, "%u %u %u %d %u %u %.4f %u %u\n", (unsigned)(kv.first >> 16), (unsigned)((kv.first >> 8) & 0xff),
             (unsigned)(kv.first & 0xff), kv.second.method, kv.second.max_buckets, kv.second.sample_per_bucket,
-            kv.second.ms, kv.second.level2);
+            kv.second.ms, kv.second.level2, kv.second.reserved[0]);
   fclose(f);
   return GBSORT_OK;
 }
@@ -1671,12 +1875,11 @@ int gbsort_tuning_load(const char* path) {
   int rc = GBSORT_OK;
   while (fgets(line, sizeof line, f)) {
     if (line[0] == '#' || line[0] == '\n') continue;
-    unsigned el, wd, cls, mb, spb, l2 = 0;
+    unsigned el, wd, cls, mb, spb, l2 = 0, big = 0;
     int m;
     float ms;
-    const int got = sscanf(line, "%u %u %u %d %u %u %f %u", &el, &wd, &cls, &m, &mb, &spb, &ms, &l2);
-    if ((got != 7 && got != 8) || (wd != 4 && wd != 8) ||
-        cls > 64 || el == 0 || el > (1u << 20)) {
+    const int got = sscanf(line, "%u %u %u %d %u %u %f %u %u", &el, &wd, &cls, &m, &mb, &spb, &ms, &l2, &big);
+    if (got < 7 || (wd != 4 && wd != 8) || (cls & 0x7f) > 64 || cls > 0xff || el == 0 || el > (1u << 20)) {
       rc = GBSORT_ERR_BAD_ARG;
       break;
     }
@@ -1686,6 +1889,7 @@ int gbsort_tuning_load(const char* path) {
     t.sample_per_bucket = spb;
     t.level2 = l2;
     t.ms = ms;
+    t.reserved[0] = big;
     if (!tuning_ok(t)) {
       rc = GBSORT_ERR_BAD_ARG;
       break;
@@ -1716,16 +1920,15 @@ struct gbsort_plan {
   cudaEvent_t done = nullptr;
   uint32_t kernels = 0;              // kernel launches in the graph
   bool pending = false;
+  // segmented plans: the segment offsets (their device copy sits at the
+  // front of ctx.seg, the error words after it) and the pinned host copy of
+  // the error words
+  std::vector<uint64_t> segs;
+  uint32_t nerrs = 0;
+  uint32_t* herrs = nullptr;
 };
 
-int gbsort_plan_create(gbsort_plan** plan, size_t nmemb, size_t elsize, const gbsort_key_desc* key, int method) {
-  if (!plan) return GBSORT_ERR_BAD_ARG;
-  *plan = nullptr;
-  if (nmemb == 0 || nmemb >= 0xffffffffull || elsize == 0 || elsize > (1u << 20) || !key_ok(key, elsize) ||
-      method < GBSORT_AUTO || method > GBSORT_LSD) {
-    set_err("bad plan arguments");
-    return GBSORT_ERR_BAD_ARG;
-  }
+static int plan_new(gbsort_plan** plan, size_t nmemb, size_t elsize, const gbsort_key_desc* key, int method) {
   Context* probe = nullptr;
   int rc = get_ctx(&probe);  // checks for a device
   if (rc) return rc;
@@ -1748,13 +1951,66 @@ int gbsort_plan_create(gbsort_plan** plan, size_t nmemb, size_t elsize, const gb
   return GBSORT_OK;
 }
 
+int gbsort_plan_create(gbsort_plan** plan, size_t nmemb, size_t elsize, const gbsort_key_desc* key, int method) {
+  if (!plan) return GBSORT_ERR_BAD_ARG;
+  *plan = nullptr;
+  if (nmemb == 0 || nmemb >= 0xffffffffull || elsize == 0 || elsize > (1u << 20) || !key_ok(key, elsize) ||
+      method < GBSORT_AUTO || method > GBSORT_LSD) {
+    set_err("bad plan arguments");
+    return GBSORT_ERR_BAD_ARG;
+  }
+  return plan_new(plan, nmemb, elsize, key, method);
+}
+
+int gbsort_plan_create_segments(gbsort_plan** plan, const uint64_t* seg_offsets, size_t nseg, size_t elsize,
+                                const gbsort_key_desc* key, int method) {
+  if (!plan) return GBSORT_ERR_BAD_ARG;
+  *plan = nullptr;
+  if (nseg == 0 || !segments_args_ok(seg_offsets, nseg) || seg_offsets[nseg] == 0 || elsize == 0 ||
+      elsize > (1u << 20) || !key_ok(key, elsize) || key->nwords != 1 ||
+      (method != GBSORT_AUTO && method != GBSORT_HISTOGRAM_PLAIN && method != GBSORT_HISTOGRAM_LEARNED)) {
+    set_err("bad segmented plan arguments");
+    return GBSORT_ERR_BAD_ARG;
+  }
+  int rc = plan_new(plan, seg_offsets[nseg], elsize, key, method);
+  if (rc) return rc;
+  gbsort_plan* p = *plan;
+  p->segs.assign(seg_offsets, seg_offsets + nseg + 1);
+  // one error word for the shared pipeline and one per segment that may be
+  // sorted on its own (any segment above 4096 records, whatever the tuning)
+  uint32_t nbig = 0;
+  for (size_t i = 0; i < nseg; ++i) nbig += seg_offsets[i + 1] - seg_offsets[i] > 4096;
+  p->nerrs = nbig + 1;
+  Context& c = p->ctx;
+  if (c.seg.ensure((nseg + 1) * 8 + (size_t)p->nerrs * 4 + 256) != cudaSuccess ||
+      cudaMallocHost(&p->herrs, (size_t)p->nerrs * 4) != cudaSuccess ||
+      cudaMemcpy(c.seg.p, p->segs.data(), (nseg + 1) * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaGetLastError();
+    gbsort_plan_destroy(p);
+    *plan = nullptr;
+    set_err("segmented plan set-up failed");
+    return GBSORT_ERR_CUDA;
+  }
+  return GBSORT_OK;
+}
+
+constexpr int kResolvedSegments = -1;  // gbsort_plan::resolved of a segmented plan
+
 // Captures the pipeline for (in, out) into the plan's graph.
 static int plan_capture(gbsort_plan* p, const void* in, void* out) {
   Context& c = p->ctx;
   const uint32_t n = (uint32_t)p->nmemb, E = (uint32_t)p->elsize;
   const bool hs_ok = hsort_layout_ok(in, out, E, &p->key);
   Knobs knobs;
-  int m = p->method == GBSORT_AUTO ? resolve_auto(E, &p->key, n, hs_ok, &knobs) : p->method;
+  int m;
+  SegKnobs sk;
+  if (!p->segs.empty()) {
+    m = kResolvedSegments;
+    sk = seg_knobs(E, &p->key, n, p->method);
+    sk.big_above = std::max<uint64_t>(sk.big_above, 4096);  // the plan holds error words for these
+  } else {
+    m = p->method == GBSORT_AUTO ? resolve_auto(E, &p->key, n, hs_ok, &knobs) : p->method;
+  }
   if (m != GBSORT_LSD && !hs_ok) {
     set_err("histogram sort needs a one-word key at a 4-byte offset and a record size of 8-64 bytes");
     return GBSORT_ERR_UNSUPPORTED;
@@ -1762,9 +2018,19 @@ static int plan_capture(gbsort_plan* p, const void* in, void* out) {
   // relaxed capture: buffer growth (cudaMalloc) may happen while capturing
   GB_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeRelaxed));
   const unsigned long long l0 = launch_count();
-  int rc = m == GBSORT_LSD ? lsd_enqueue(c, in, out, n, E, &p->key, nullptr, 0, false, c.stream)
-                           : hsort_enqueue(c, in, out, n, E, &p->key, m == GBSORT_HISTOGRAM_LEARNED, false, knobs,
-                                           c.stream);
+  int rc;
+  if (m == kResolvedSegments) {
+    const uint64_t* d_offs = c.seg.as<uint64_t>();
+    uint32_t* errs = reinterpret_cast<uint32_t*>(c.seg.as<uint64_t>() + p->segs.size());
+    rc = cudaMemsetAsync(errs, 0, (size_t)p->nerrs * 4, c.stream) == cudaSuccess ? GBSORT_OK : GBSORT_ERR_CUDA;
+    if (!rc) rc = segments_enqueue(c, in, out, p->segs, d_offs, E, &p->key, sk, errs, c.stream);
+    if (!rc && cudaMemcpyAsync(p->herrs, errs, (size_t)p->nerrs * 4, cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
+      rc = GBSORT_ERR_CUDA;
+  } else {
+    rc = m == GBSORT_LSD ? lsd_enqueue(c, in, out, n, E, &p->key, nullptr, 0, false, c.stream)
+                         : hsort_enqueue(c, in, out, n, E, &p->key, m == GBSORT_HISTOGRAM_LEARNED, false, knobs,
+                                         c.stream);
+  }
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(c.stream, &g);
   if (rc || e != cudaSuccess) {
@@ -1823,7 +2089,9 @@ int gbsort_plan_wait(gbsort_plan* p) {
   if (!p->pending) return GBSORT_OK;
   p->pending = false;
   GB_CUDA(cudaEventSynchronize(p->done));
-  int rc = p->resolved == GBSORT_LSD ? lsd_collect(p->ctx) : hsort_collect(p->ctx);
+  int rc = p->resolved == kResolvedSegments ? segments_collect(p->ctx, p->herrs, p->nerrs)
+           : p->resolved == GBSORT_LSD       ? lsd_collect(p->ctx)
+                                             : hsort_collect(p->ctx);
   if (rc == GBSORT_OK) g_stats.launches = p->kernels;
   return rc;
 }
@@ -1834,6 +2102,7 @@ int gbsort_plan_destroy(gbsort_plan* p) {
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->graph) cudaGraphDestroy(p->graph);
   if (p->done) cudaEventDestroy(p->done);
+  if (p->herrs) cudaFreeHost(p->herrs);
   ctx_destroy(p->ctx);
   delete p;
   return GBSORT_OK;

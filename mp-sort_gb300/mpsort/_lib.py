@@ -78,7 +78,7 @@ class Tuning(ctypes.Structure):
     def as_dict(self):
         return {"method": METHOD_NAMES.get(self.method, self.method), "max_buckets": self.max_buckets,
                 "sample_per_bucket": self.sample_per_bucket, "ms": self.ms,
-                "level2": LEVEL2_NAMES.get(self.level2, self.level2)}
+                "level2": LEVEL2_NAMES.get(self.level2, self.level2), "big_above": self.reserved[0]}
 
 
 # name: (restype, argtypes)
@@ -101,12 +101,15 @@ SIGNATURES = {
     "mpsort_mpi_impl": (None, [_P, _SZ, _SZ, _P, _SZ, _P, ctypes.c_ssize_t, _I, ctypes.c_char_p]),
     "mpsort_mpi_report_last_run": (None, []),
     "gbsort_plan_create": (_I, [_P, _SZ, _SZ, _P, _I]),
+    "gbsort_plan_create_segments": (_I, [_P, _P, _SZ, _SZ, _P, _I]),
     "gbsort_plan_sort": (_I, [_P, _P, _P, _P]),
     "gbsort_plan_wait": (_I, [_P]),
     "gbsort_plan_destroy": (_I, [_P]),
     "gbsort_autotune": (_I, [_SZ, _SZ, _P, _P, _P]),
     "gbsort_tuning_set": (_I, [_SZ, _SZ, _P, _P]),
     "gbsort_tuning_get": (_I, [_SZ, _SZ, _P, _P]),
+    "gbsort_autotune_segments": (_I, [_P, _SZ, _SZ, _P, _P, _P]),
+    "gbsort_tuning_get_segments": (_I, [_SZ, _SZ, _P, _P]),
     "gbsort_tuning_clear": (_I, []),
     "gbsort_tuning_save": (_I, [ctypes.c_char_p]),
     "gbsort_tuning_load": (_I, [ctypes.c_char_p]),

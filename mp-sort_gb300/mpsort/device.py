@@ -46,14 +46,22 @@ class Plan:
     """The sort of n records of `dtype` by `orderby` captured as one CUDA
     graph: ``plan.sort(d_in, d_out, stream)`` enqueues it (one graph launch,
     no host synchronisation), ``plan.wait()`` waits and raises on a device
-    error.  The graph is re-captured when the buffers change."""
+    error.  The graph is re-captured when the buffers change.  With
+    `segments` (nseg + 1 offsets) the plan is the segmented sort of that
+    batch (``sort_segments``) and `n` is ignored."""
 
-    def __init__(self, n, dtype, orderby, method="auto"):
+    def __init__(self, n, dtype, orderby, method="auto", segments=None):
         dtype = numpy.dtype(dtype)
         self._desc = _desc(dtype, orderby)
         self._h = ctypes.c_void_p()
-        _lib.check(_lib.lib().gbsort_plan_create(ctypes.byref(self._h), n, dtype.itemsize,
-                                                 ctypes.byref(self._desc), _lib.METHODS[method]))
+        if segments is None:
+            _lib.check(_lib.lib().gbsort_plan_create(ctypes.byref(self._h), n, dtype.itemsize,
+                                                     ctypes.byref(self._desc), _lib.METHODS[method]))
+        else:
+            offs = numpy.ascontiguousarray(segments, dtype=numpy.uint64)
+            _lib.check(_lib.lib().gbsort_plan_create_segments(ctypes.byref(self._h), offs.ctypes.data,
+                                                              len(offs) - 1, dtype.itemsize,
+                                                              ctypes.byref(self._desc), _lib.METHODS[method]))
 
     def sort(self, d_in, d_out, stream=0):
         _lib.check(_lib.lib().gbsort_plan_sort(self._h, d_in, d_out, stream or None))
@@ -82,6 +90,31 @@ def autotune(n, dtype, orderby, d_records=0):
     t = _lib.Tuning()
     _lib.check(_lib.lib().gbsort_autotune(n, dtype.itemsize, ctypes.byref(desc), d_records or None,
                                           ctypes.byref(t)))
+    return t.as_dict()
+
+
+def autotune_segments(offsets, dtype, orderby, d_records=0):
+    """Time segmented sorts of this batch (level 2 as rounds / engine, three
+    thresholds for sorting a segment on its own) and store the fastest in the
+    segment tuning table.  Returns it as a dict."""
+    dtype = numpy.dtype(dtype)
+    desc = _desc(dtype, orderby)
+    offs = numpy.ascontiguousarray(offsets, dtype=numpy.uint64)
+    t = _lib.Tuning()
+    _lib.check(_lib.lib().gbsort_autotune_segments(offs.ctypes.data, len(offs) - 1, dtype.itemsize,
+                                                   ctypes.byref(desc), d_records or None, ctypes.byref(t)))
+    return t.as_dict()
+
+
+def tuning_get_segments(n, dtype, orderby):
+    """The segment tuning entry for batches of n records, or None."""
+    dtype = numpy.dtype(dtype)
+    desc = _desc(dtype, orderby)
+    t = _lib.Tuning()
+    rc = _lib.lib().gbsort_tuning_get_segments(n, dtype.itemsize, ctypes.byref(desc), ctypes.byref(t))
+    if rc == 6:
+        return None
+    _lib.check(rc)
     return t.as_dict()
 
 

@@ -418,6 +418,72 @@ def test_segments(mp, big):
         assert got[lo:hi].tobytes() == O.numpy_sorted(a[lo:hi], 'key').tobytes(), i
 
 
+def test_segments_plan_and_tuning(mp, tmp_path):
+    """A segmented plan (one graph launch per replay) against the oracle per
+    segment, through the tuned entry the segment autotuner stores: replays
+    on two output buffers (the second re-captures), the tuning entry's
+    threshold and level-2 choice honoured, and the tuning file round trip."""
+    import torch
+    import mpsort
+    from mpsort import device
+    rng = numpy.random.default_rng(15)
+    sizes = numpy.concatenate([[0, 1, 4096, 4097, 70_000, 1_500_000], rng.integers(0, 30_000, 300),
+                               [2_100_000, 5000]])
+    offs = numpy.concatenate([[0], numpy.cumsum(sizes)]).astype(numpy.uint64)
+    n = int(offs[-1])
+    dt = numpy.dtype([('key', 'u8'), ('payload', 'u8')])
+    a = numpy.zeros(n, dt)
+    a['key'] = rng.integers(0, 2**64 - 1, n, dtype=numpy.uint64)
+    a['key'][::7] = rng.integers(0, 9, len(a['key'][::7]))
+    a['payload'] = numpy.arange(n)
+    din = torch.from_numpy(a.view(numpy.uint8).copy()).cuda()
+    outs = [torch.empty_like(din), torch.empty_like(din)]
+    device.tuning_clear()
+    try:
+        best = device.autotune_segments(offs, dt, 'key', din.data_ptr())
+        assert best["level2"] in ("rounds", "engine") and best["big_above"] >= 1 << 20 and best["ms"] > 0
+        assert device.tuning_get_segments(n, dt, 'key') == best
+        # a hand-set entry: segments above 10^6 records sorted on their own, level 2 as rounds
+        path = tmp_path / "tune.txt"
+        device.tuning_save(path)
+        text = path.read_text().splitlines()
+        seg = [l for l in text if not l.startswith('#') and int(l.split()[2]) >= 128]
+        assert len(seg) == 1 and int(seg[0].split()[8]) == best["big_above"]
+        f = seg[0].split()
+        f[7], f[8] = "1", "1000000"
+        path.write_text("\n".join(text + [" ".join(f)]) + "\n")
+        device.tuning_clear()
+        device.tuning_load(path)
+        assert device.tuning_get_segments(n, dt, 'key')["big_above"] == 1_000_000
+        plan = device.Plan(0, dt, 'key', segments=offs)
+        for rep in range(3):
+            out = outs[rep % 2]
+            out.zero_()
+            plan.sort(din.data_ptr(), out.data_ptr())
+            plan.wait()
+            st = mpsort.last_stats()
+            assert st["engine"] == 0 and st["sample"] == 2      # two segments above 10^6, level 2 as rounds
+            assert st["launches"] >= 4
+            got = out.cpu().numpy().view(dt)
+            for i in range(len(sizes)):
+                lo, hi = int(offs[i]), int(offs[i + 1])
+                assert got[lo:hi].tobytes() == O.numpy_sorted(a[lo:hi], 'key').tobytes(), (rep, i)
+        plan.close()
+        # the engine and the default threshold through the synchronous call
+        device.tuning_clear()
+        outs[0].zero_()
+        device.sort_segments(din.data_ptr(), outs[0].data_ptr(), offs, dt, 'key')
+        torch.cuda.synchronize()
+        st = mpsort.last_stats()
+        assert st["engine"] == 1 and st["sample"] == 0
+        got = outs[0].cpu().numpy().view(dt)
+        for i in range(len(sizes)):
+            lo, hi = int(offs[i]), int(offs[i + 1])
+            assert got[lo:hi].tobytes() == O.numpy_sorted(a[lo:hi], 'key').tobytes(), i
+    finally:
+        device.tuning_clear()
+
+
 def test_merge_join(mp):
     import torch
     from mpsort import device
