@@ -68,6 +68,9 @@ constexpr uint32_t kCrowded = GB_SPLIT_CROWDED;  // records of a split bin that 
 // read costs more than the re-splits it saves (small segments sit in L2).
 constexpr uint32_t kRefineMin = 1u << 17;
 constexpr int kMaxGroups = 512;        // sub-buckets per split
+constexpr int kGroupBits = 9;          // bits of a group id
+static_assert((1 << kGroupBits) == kMaxGroups, "group ids fill kGroupBits");
+constexpr int kMaxBucketBits = 12;     // bits of a level-1 bucket id (at most 4096 buckets)
 constexpr uint32_t kCopyPiece = 1u << 16;
 
 __host__ __device__ __forceinline__ uint32_t chunk_begin(uint32_t n, uint32_t c, uint32_t g) {
@@ -428,20 +431,19 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_count(HsortParams p, const u
 constexpr uint32_t kNoBucket = 0xffffffffu;
 static_assert(kWarps == 16, "a table row is one 16-byte vector");
 
-// Ids are below `nbuckets`, so labels need bitlen(nbuckets - 1) bits.
-// Padding items sit above every real item of their row (the valid items of
-// a tile are a prefix), so they may share a label with real items: they are
-// masked out of every count.
-template <int RPT>
+// Ids are below 2^BITS (BITS unrolled ballots match them).  Padding items
+// sit above every real item of their row (the valid items of a tile are a
+// prefix), so they may share a label with real items: they are masked out
+// of every count.
+template <int RPT, int BITS>
 __device__ __forceinline__ void warp_ranks(const uint32_t (&bkt)[RPT], uint32_t (&rank)[RPT], uint32_t (&lead)[RPT],
-                                           uint8_t* cnt, uint32_t nbuckets) {
+                                           uint8_t* cnt) {
   static_assert(RPT <= 7, "per-warp counts must fit a byte");
   const uint32_t w = warp_id(), lane = lane_id();
-  const int bits = nbuckets > 1 ? 32 - __clz(nbuckets - 1) : 0;
 #pragma unroll
   for (int r = 0; r < RPT; ++r) {
     const uint32_t valid = __ballot_sync(GB_FULL_MASK, bkt[r] != kNoBucket);
-    const uint32_t peers = match_bits_rt(bkt[r] & (nbuckets - 1), bits) & valid;
+    const uint32_t peers = match_bits<BITS>(bkt[r]) & valid;
     const uint32_t leader = __ffs(peers) - 1;
     uint32_t old = 0;
     if (lane == leader && bkt[r] != kNoBucket) {
@@ -456,24 +458,25 @@ __device__ __forceinline__ void warp_ranks(const uint32_t (&bkt)[RPT], uint32_t 
   }
 }
 
+// Selectors of the earlier warps' bytes of a table row: entry w has byte j
+// set to 1 for j < w (warp-uniform reads of the constant bank).
+#define GB_EARLIER(n) ((n) <= 0 ? 0u : (n) >= 4 ? 0x01010101u : (0x01010101u >> (8 * (4 - (n)))))
+#define GB_EARLIER_ROW(w) {GB_EARLIER(w), GB_EARLIER((w) - 4), GB_EARLIER((w) - 8), GB_EARLIER((w) - 12)}
+__constant__ uint4 kEarlierWarps[kWarps] = {
+    GB_EARLIER_ROW(0),  GB_EARLIER_ROW(1),  GB_EARLIER_ROW(2),  GB_EARLIER_ROW(3),
+    GB_EARLIER_ROW(4),  GB_EARLIER_ROW(5),  GB_EARLIER_ROW(6),  GB_EARLIER_ROW(7),
+    GB_EARLIER_ROW(8),  GB_EARLIER_ROW(9),  GB_EARLIER_ROW(10), GB_EARLIER_ROW(11),
+    GB_EARLIER_ROW(12), GB_EARLIER_ROW(13), GB_EARLIER_ROW(14), GB_EARLIER_ROW(15)};
+#undef GB_EARLIER_ROW
+#undef GB_EARLIER
+
 __device__ __forceinline__ uint32_t tile_rank(uint32_t b, uint32_t rank, const uint8_t* cnt, uint32_t& all) {
-  const uint32_t w = warp_id();
   const uint4 x = *reinterpret_cast<const uint4*>(cnt + (size_t)b * kWarps);
-  const uint32_t wd[4] = {x.x, x.y, x.z, x.w};
-  // byte j of the row (warp j's count) counts when j < w: byte dot products
-  // with 0x01 selectors sum them
-  uint32_t before = 0, tot = 0;
-#pragma unroll
-  for (int v = 0; v < 4; ++v) {
-    const int j0 = v * 4;
-    uint32_t keep = 0;
-    if (j0 + 4 <= (int)w) keep = 0x01010101u;
-    else if (j0 < (int)w) keep = 0x01010101u >> (8 * (4 - ((int)w - j0)));
-    tot = __dp4a(wd[v], 0x01010101u, tot);
-    before = __dp4a(wd[v], keep, before);
-  }
-  all = tot;
-  return before + rank;
+  const uint4 k = kEarlierWarps[warp_id()];
+  // byte dot products: with 0x01 selectors the row's total, with this
+  // warp's selectors the counts of the warps before it
+  all = __dp4a(x.w, 0x01010101u, __dp4a(x.z, 0x01010101u, __dp4a(x.y, 0x01010101u, __dp4a(x.x, 0x01010101u, 0u))));
+  return __dp4a(x.w, k.w, __dp4a(x.z, k.z, __dp4a(x.y, k.y, __dp4a(x.x, k.x, rank))));
 }
 
 template <int RPT>
@@ -624,7 +627,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const
     }
     // 1. ranks within the warp, in (r, lane) order
     uint32_t lead[RPT];
-    warp_ranks<RPT>(bkt, rank, lead, cnt, (uint32_t)nbuckets);
+    warp_ranks<RPT, kMaxBucketBits>(bkt, rank, lead, cnt);
     __syncthreads();
     // 2. rank in the tile = counts of the earlier warps + rank in the warp
     uint32_t tot[RPT], hold[RPT];
@@ -1640,7 +1643,7 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
         grp[r] = sm.gmap[bin];
       }
     }
-    warp_ranks<RPT>(grp, rank, lead, sm.gcnt, (uint32_t)kMaxGroups);
+    warp_ranks<RPT, kGroupBits>(grp, rank, lead, sm.gcnt);
     __syncthreads();
     uint32_t gtot;
     tile_rank(g_me, 0, sm.gcnt, gtot);  // this thread's group: records in the tile
@@ -2249,6 +2252,7 @@ uint32_t hsort_chunk_begin(uint32_t n, int c, int chunks) {
 cudaError_t l1_scatter(const HsortParams& p, int lookup_kind, const uint64_t* splitters, int nbuckets,
                        const void* model, const uint32_t* offsets, uint32_t* stats, cudaStream_t stream, int c0,
                        int c1, const uint32_t* skip_if, const uint32_t* gate, int gate_wide) {
+  if (nbuckets < 1 || nbuckets > (1 << kMaxBucketBits)) return cudaErrorInvalidValue;  // ids rank in 12 bits
   const ModelDev m = model ? *(const ModelDev*)model : ModelDev{};
   const int g = p.chunks ? (int)p.chunks : hsort_grid(p.n);
   if (c1 < 0) c1 = g;
