@@ -271,6 +271,24 @@ size_t lsd_scratch_bytes(uint32_t n, int nwords) {
   return (size_t)2 * 8 * 256 * 4 * nwords + (size_t)lsd_tiles(n) * 256 * 8 + 4096;
 }
 
+// The LSD digits (word, shift) a sort runs, least significant first: all
+// of them, or (with the histograms on the host) those whose histogram does
+// not put every key in one bin.
+void lsd_pass_list(int nwords, uint32_t n, const std::vector<uint32_t>* h, std::vector<int>& pass_word,
+                   std::vector<int>& pass_shift) {
+  for (int w = 0; w < nwords; ++w)
+    for (int d = 0; d < 8; ++d) {
+      bool trivial = false;
+      if (h)
+        for (int b = 0; b < 256; ++b)
+          if ((*h)[((size_t)w * 8 + d) * 256 + b] == n) trivial = true;
+      if (!trivial) {
+        pass_word.push_back(w);
+        pass_shift.push_back(8 * d);
+      }
+    }
+}
+
 // Sorts key words (and idx) in place in keys / idx, ping-ponging through
 // keys2 / idx2, one one-sweep pass per 8-bit digit.  With skip_trivial the
 // digit histograms are read back (one synchronisation) and digits whose
@@ -291,17 +309,7 @@ int lsd_sort_keys(Bump& bump, uint64_t* keys, uint64_t* keys2, uint32_t* idx, ui
     GB_CUDA(cudaMemcpyAsync(h.data(), hist, h.size() * 4, cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
   }
-  for (int w = 0; w < nwords; ++w)
-    for (int d = 0; d < 8; ++d) {
-      bool trivial = false;
-      if (skip_trivial)
-        for (int b = 0; b < 256; ++b)
-          if (h[((size_t)w * 8 + d) * 256 + b] == n) trivial = true;
-      if (!trivial) {
-        pass_word.push_back(w);
-        pass_shift.push_back(8 * d);
-      }
-    }
+  lsd_pass_list(nwords, n, skip_trivial ? &h : nullptr, pass_word, pass_shift);
   uint64_t* kin = keys;
   uint64_t* kout = keys2;
   uint32_t* iin = idx;
@@ -321,12 +329,65 @@ int lsd_sort_keys(Bump& bump, uint64_t* keys, uint64_t* keys2, uint32_t* idx, ui
   return GBSORT_OK;
 }
 
+// LSD over records of 8-32 bytes that carry themselves through the digit
+// passes (lsd_record_pass), ping-ponging through scratch A / B so that the
+// last pass writes d_out.
+int lsd_records_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize,
+                        const gbsort_key_desc* key, bool skip_trivial, cudaStream_t st) {
+  const int nwords = (int)key->nwords;
+  const size_t bytes = (size_t)n * elsize;
+  GB_CUDA(c.A.ensure(bytes + kScratchSlack));
+  GB_CUDA(c.B.ensure(bytes + kScratchSlack));
+  GB_CUDA(c.small.ensure((size_t)2 * 8 * 256 * 4 * nwords + (size_t)lsd_record_tiles(n, elsize) * 256 * 8 +
+                         CNT_WORDS * 4 + 8192));
+  Bump bump{c.small.as<uint8_t>()};
+  uint32_t* counters = bump.take<uint32_t>(CNT_WORDS);
+  uint32_t* err = counters + CNT_ERR;
+  uint32_t* hist = bump.take<uint32_t>((size_t)8 * 256 * nwords);
+  uint32_t* starts = bump.take<uint32_t>((size_t)8 * 256 * nwords);
+  unsigned long long* status = bump.take<unsigned long long>((size_t)lsd_record_tiles(n, elsize) * 256);
+  uint32_t* ticket = bump.take<uint32_t>(1);
+  GB_CUDA(cudaMemsetAsync(counters, 0, CNT_WORDS * sizeof(uint32_t), st));
+  GB_CUDA(lsd_record_histograms(d_in, n, elsize, *key, hist, st));
+  GB_CUDA(lsd_digit_starts(hist, nwords, starts, st));
+  std::vector<uint32_t> h;
+  if (skip_trivial) {
+    h.resize((size_t)8 * 256 * nwords);
+    GB_CUDA(cudaMemcpyAsync(h.data(), hist, h.size() * 4, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+  }
+  std::vector<int> pass_word, pass_shift;
+  lsd_pass_list(nwords, n, skip_trivial ? &h : nullptr, pass_word, pass_shift);
+  const size_t P = pass_word.size();
+  const void* src = d_in;
+  for (size_t p = 0; p < P; ++p) {
+    void* dst = p + 1 == P ? d_out : (p % 2 == 0 ? c.A.p : c.B.p);
+    if (dst == src) dst = c.A.p;  // one pass, in place: through A, then home
+    const uint32_t* st_d = starts + ((size_t)pass_word[p] * 8 + pass_shift[p] / 8) * 256;
+    GB_CUDA(lsd_record_pass(src, dst, n, elsize, *key, pass_word[p], pass_shift[p], st_d, status, ticket, err,
+                            st));
+    src = dst;
+  }
+  if (src != d_out) GB_CUDA(cudaMemcpyAsync(d_out, src, bytes, cudaMemcpyDeviceToDevice, st));
+  GB_CUDA(cudaMemcpyAsync(c.hc->c, counters, CNT_WORDS * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  c.run_lsd_passes = (uint32_t)P;
+  return GBSORT_OK;
+}
+
 // Generic path over device records: keys from the descriptor (or from radix
-// bytes already on the device), LSD, then one gather into d_out.  With
+// bytes already on the device), LSD, then one gather into d_out -- or, with
+// GBSORT_LSD_RECORDS=1 and records of 8-32 bytes, passes that carry the
+// records themselves (fewer bytes, more time on this GPU: opt-in).  With
 // skip_trivial, constant digits are found on the host (one synchronisation)
 // and skipped; without, nothing waits for the host (graph capture).
 int lsd_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize, const gbsort_key_desc* key,
                 const uint8_t* d_radix, uint32_t rsize, bool skip_trivial, cudaStream_t st) {
+  static const bool records = [] {
+    const char* e = getenv("GBSORT_LSD_RECORDS");
+    return e && atoi(e) == 1;
+  }();
+  if (!d_radix && records && lsd_records_supported(elsize, d_in, d_out, *key))
+    return lsd_records_enqueue(c, d_in, d_out, n, elsize, key, skip_trivial, st);
   const int nwords = d_radix ? (int)((rsize + 7) / 8) : (int)key->nwords;
   GB_CUDA(c.keysA.ensure(sizeof(uint64_t) * (size_t)n * nwords));
   GB_CUDA(c.keysB.ensure(sizeof(uint64_t) * (size_t)n * nwords));

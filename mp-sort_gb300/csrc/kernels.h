@@ -68,6 +68,18 @@ cudaError_t lsd_digit_histograms(const uint64_t* keys, uint32_t n, int nwords, u
 cudaError_t lsd_digit_starts(const uint32_t* hist, int nwords, uint32_t* starts, cudaStream_t stream);
 // Tiles of one LSD pass over n keys (status words needed: 256 per tile).
 uint32_t lsd_tiles(uint32_t n);
+// Record-carrying LSD passes (records of 8-32 bytes in 4-byte words, key
+// words at 4-byte offsets, buffers aligned to the record's vector size):
+// the digit histograms of every key word read from the records, and one
+// stable pass that moves whole records by one digit.  Tiles of 2048 or
+// 4096 records; status holds lsd_record_tiles(n, elsize) * 256 words.
+bool lsd_records_supported(uint32_t elsize, const void* in, const void* out, const gbsort_key_desc& key);
+uint32_t lsd_record_tiles(uint32_t n, uint32_t elsize);
+cudaError_t lsd_record_histograms(const void* in, uint32_t n, uint32_t elsize, const gbsort_key_desc& key,
+                                  uint32_t* hist, cudaStream_t stream);
+cudaError_t lsd_record_pass(const void* in, void* out, uint32_t n, uint32_t elsize, const gbsort_key_desc& key,
+                            int word, int shift, const uint32_t* starts, unsigned long long* status,
+                            uint32_t* ticket, uint32_t* err, cudaStream_t stream);
 // One one-sweep LSD pass on digit (word, shift): stable scatter of all key
 // words (and idx, if not null) with offsets from starts (256 entries of this
 // digit) plus a decoupled look-back over the tiles; status and ticket are

@@ -194,6 +194,170 @@ __global__ void __launch_bounds__(kThreads) k_lsd_onesweep(const uint64_t* __res
   }
 }
 
+// ------------------------------------------------ record-carrying passes --
+// Records of 8-32 bytes (4-byte words, key words at 4-byte offsets) can be
+// moved by the digit passes themselves: each pass reads whole records in
+// input order, ranks them by the digit of one key word taken from the
+// registers, stages them in digit order in shared memory and writes them
+// out in runs.  No key arrays, no index, no final gather (whose reads by
+// index are random and fetch about a DRAM line per record): 2E bytes per
+// record per pass.  Measured on 16-byte records the passes still take
+// longer than key + index passes plus the gather (the one-tile-per-CTA
+// passes are latency-bound, not bandwidth-bound), so this form is opt-in
+// (GBSORT_LSD_RECORDS=1).
+template <int EW, int NT = 256>
+struct RecPass {
+  static constexpr int kRpt = EW <= 4 ? 8 : 4;
+  static constexpr int kTile = NT * kRpt;
+  using V = typename std::conditional<EW % 4 == 0, uint4, typename std::conditional<EW % 2 == 0, uint2,
+                                                                                  uint32_t>::type>::type;
+  static constexpr int kVw = sizeof(V) / 4;       // words per vector
+  static constexpr int kVpr = EW / kVw;           // vectors per record
+  static constexpr size_t kSmem = (size_t)kTile * (EW * 4 + 1);
+};
+
+template <int EW>
+__device__ __forceinline__ void rec_load(const uint8_t* p, uint32_t (&r)[EW]) {
+  using V = typename RecPass<EW>::V;
+  constexpr int VW = RecPass<EW>::kVw;
+#pragma unroll
+  for (int i = 0; i < RecPass<EW>::kVpr; ++i) {
+    const V v = reinterpret_cast<const V*>(p)[i];
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(&v);
+#pragma unroll
+    for (int j = 0; j < VW; ++j) r[i * VW + j] = w[j];
+  }
+}
+
+template <int EW>
+__device__ __forceinline__ void rec_store(uint8_t* p, const uint32_t (&r)[EW]) {
+  using V = typename RecPass<EW>::V;
+  constexpr int VW = RecPass<EW>::kVw;
+#pragma unroll
+  for (int i = 0; i < RecPass<EW>::kVpr; ++i) {
+    V v;
+    uint32_t* w = reinterpret_cast<uint32_t*>(&v);
+#pragma unroll
+    for (int j = 0; j < VW; ++j) w[j] = r[i * VW + j];
+    reinterpret_cast<V*>(p)[i] = v;
+  }
+}
+
+// Histograms of all 8 digits of every key word, read from the records.
+template <int EW>
+__global__ void __launch_bounds__(kThreads) k_record_digit_hist(const uint8_t* __restrict__ in, uint32_t n,
+                                                                 gbsort_key_desc key,
+                                                                 uint32_t* __restrict__ hist) {
+  __shared__ uint32_t h[4 * 8 * 256];
+  const int nw = (int)key.nwords;
+  for (int i = threadIdx.x; i < nw * 8 * 256; i += kThreads) h[i] = 0;
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    uint32_t r[EW];
+    rec_load<EW>(in + (size_t)i * (EW * 4), r);
+    for (int w = 0; w < nw; ++w) {
+      const uint64_t k = key_from_regs<EW>(r, key.word[w]);
+#pragma unroll
+      for (int d = 0; d < 8; ++d) atomicAdd(&h[(w * 8 + d) * 256 + ((k >> (8 * d)) & 255)], 1u);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nw * 8 * 256; i += kThreads)
+    if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+// One record-carrying pass on digit (word, shift); status holds
+// tiles * 256 zeroed words, *ticket starts at 0 (as k_lsd_onesweep).
+template <int EW, int NT>
+__global__ void __launch_bounds__(NT, 3) k_lsd_records(const uint8_t* __restrict__ in,
+                                                                     uint8_t* __restrict__ out, uint32_t n,
+                                                                     gbsort_key_word kw, int shift,
+                                                                     const uint32_t* __restrict__ starts,
+                                                                     unsigned long long* status, uint32_t* ticket,
+                                                                     uint32_t* err, uint32_t spin_limit) {
+  static_assert(NT >= 256, "one thread per digit in the look-back");
+  constexpr int RPT = RecPass<EW, NT>::kRpt, T = RecPass<EW, NT>::kTile;
+  constexpr uint32_t E = EW * 4;
+  using Rank = BlockRank<RPT, 8, NT>;
+  using V = typename RecPass<EW, NT>::V;
+  constexpr int VPR = RecPass<EW, NT>::kVpr;
+  __shared__ uint16_t hist[Rank::kCounters];
+  __shared__ uint32_t scan_tmp[NT / 32];
+  __shared__ uint32_t start[257];
+  __shared__ uint32_t base[256];
+  __shared__ uint32_t tile_s;
+  extern __shared__ __align__(16) uint8_t smem[];
+  uint8_t* stage = smem;                     // [T] records, digit order
+  uint8_t* sdig = smem + (size_t)T * E;      // [T] their digits
+
+  if (threadIdx.x == 0) tile_s = atomicAdd(ticket, 1u);
+  __syncthreads();
+  const uint32_t tile = tile_s;
+  const uint32_t t = tile * (uint32_t)T;
+  const uint32_t nvalid = min((uint32_t)T, n - t);
+  const uint32_t w = warp_id(), lane = lane_id();
+  uint32_t rec[RPT][EW];
+  uint32_t digit[RPT], pos[RPT];
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) {
+    const uint32_t e = w * 32 * RPT + r * 32 + lane;
+    digit[r] = 255u;  // padding items take the last digit and rank after every real item
+    if (e < nvalid) {
+      rec_load<EW>(in + (size_t)(t + e) * E, rec[r]);
+      digit[r] = (uint32_t)(key_from_regs<EW>(rec[r], kw) >> shift) & 255u;
+    }
+  }
+  Rank::rank(digit, pos, hist, scan_tmp, start);
+#pragma unroll
+  for (int r = 0; r < RPT; ++r)
+    if (pos[r] < nvalid) {
+      rec_store<EW>(stage + (size_t)pos[r] * E, rec[r]);
+      sdig[pos[r]] = (uint8_t)digit[r];
+    }
+  if (threadIdx.x < 256) {
+    const uint32_t d = threadIdx.x;
+    uint32_t cnt = start[d + 1] - start[d];
+    if (d == 255) cnt -= (uint32_t)T - nvalid;
+    unsigned long long* mine = status + (size_t)tile * 256 + d;
+    unsigned long long excl = 0;
+    if (tile == 0) {
+      st_relaxed(mine, kStatPrefix | cnt);
+    } else {
+      st_relaxed(mine, kStatAgg | cnt);
+      uint32_t j = tile - 1, spins = 0;
+      for (;;) {
+        const unsigned long long v = ld_relaxed(status + (size_t)j * 256 + d);
+        const unsigned long long f = v & ~kStatValue;
+        if (f == 0) {  // tile j has not published yet
+          if (++spins > spin_limit) {
+            set_error(err, DEV_ERR_TIMEOUT);
+            break;
+          }
+          __nanosleep(spins < 32 ? 32 : 256);
+          continue;
+        }
+        excl += v & kStatValue;
+        if (f == kStatPrefix || j == 0) break;
+        --j;
+      }
+      st_relaxed(mine, kStatPrefix | (excl + cnt));
+    }
+    base[d] = starts[d] + (uint32_t)excl - start[d];
+  }
+  __syncthreads();
+  // runs of equal digits go to consecutive output slots; consecutive threads
+  // take consecutive vectors of consecutive records
+  for (uint32_t f = threadIdx.x; f < nvalid * VPR; f += NT) {
+    const uint32_t i = f / VPR, q = f % VPR;
+    const uint32_t dest = base[sdig[i]] + i;
+    if (dest >= n) {
+      set_error(err, DEV_ERR_COUNT_MISMATCH);
+      continue;
+    }
+    reinterpret_cast<V*>(out + (size_t)dest * E)[q] = reinterpret_cast<const V*>(stage + (size_t)i * E)[q];
+  }
+}
+
 // Pseudo-random bytes: word i of the buffer is a 64-bit mix of (i, seed).
 __global__ void k_fill_hash(uint32_t* __restrict__ p, uint64_t nwords, uint64_t seed) {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nwords;
@@ -278,6 +442,75 @@ cudaError_t lsd_digit_starts(const uint32_t* hist, int nwords, uint32_t* starts,
 }
 
 uint32_t lsd_tiles(uint32_t n) { return (uint32_t)(((uint64_t)n + kLsdTile - 1) / kLsdTile); }
+
+template <typename F>
+static bool dispatch_rec_ew(uint32_t elsize, F&& f) {
+  switch (elsize / 4) {
+    case 2: f(std::integral_constant<int, 2>()); return true;
+    case 3: f(std::integral_constant<int, 3>()); return true;
+    case 4: f(std::integral_constant<int, 4>()); return true;
+    case 5: f(std::integral_constant<int, 5>()); return true;
+    case 6: f(std::integral_constant<int, 6>()); return true;
+    case 7: f(std::integral_constant<int, 7>()); return true;
+    case 8: f(std::integral_constant<int, 8>()); return true;
+    default: return false;
+  }
+}
+
+bool lsd_records_supported(uint32_t elsize, const void* in, const void* out, const gbsort_key_desc& key) {
+  if (elsize % 4 || elsize < 8 || elsize > 32 || key.nwords < 1 || key.nwords > 4) return false;
+  for (uint32_t w = 0; w < key.nwords; ++w)
+    if (key.word[w].offset % 4 || key.word[w].offset + key.word[w].width > elsize) return false;
+  const uint32_t vec = elsize % 16 == 0 ? 16 : (elsize % 8 == 0 ? 8 : 4);
+  return ((uintptr_t)in | (uintptr_t)out) % vec == 0;
+}
+
+// Threads per CTA of the record passes: 256 (tiles of 8 or 4 records per
+// thread; four CTAs per SM) beat 512 (two per SM) by 1.3x on 1e9 x 16 B.
+constexpr int kRecThreads = 256;
+
+uint32_t lsd_record_tiles(uint32_t n, uint32_t elsize) {
+  uint32_t tile = 0;
+  dispatch_rec_ew(elsize, [&](auto ewc) { tile = RecPass<decltype(ewc)::value, kRecThreads>::kTile; });
+  return tile ? (uint32_t)(((uint64_t)n + tile - 1) / tile) : 0;
+}
+
+cudaError_t lsd_record_histograms(const void* in, uint32_t n, uint32_t elsize, const gbsort_key_desc& key,
+                                  uint32_t* hist, cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(uint32_t) * 8 * 256 * key.nwords, stream);
+  if (e != cudaSuccess || n == 0) return e;
+  const bool ok = dispatch_rec_ew(elsize, [&](auto ewc) {
+    constexpr int EW = decltype(ewc)::value;
+    k_record_digit_hist<EW><<<blocks_for(n, kThreads), kThreads, 0, stream>>>((const uint8_t*)in, n, key, hist);
+  });
+  if (!ok) return cudaErrorInvalidValue;
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t lsd_record_pass(const void* in, void* out, uint32_t n, uint32_t elsize, const gbsort_key_desc& key,
+                            int word, int shift, const uint32_t* starts, unsigned long long* status,
+                            uint32_t* ticket, uint32_t* err, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  const uint32_t tiles = lsd_record_tiles(n, elsize);
+  cudaError_t e = cudaMemsetAsync(status, 0, sizeof(unsigned long long) * 256 * (size_t)tiles, stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ticket, 0, sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return e;
+  auto launch = [&](auto kern, size_t smem, int nt) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      kern<<<tiles, nt, smem, stream>>>((const uint8_t*)in, (uint8_t*)out, n, key.word[word], shift, starts, status,
+                                        ticket, err, kLookbackSpins);
+  };
+  const bool ok = dispatch_rec_ew(elsize, [&](auto ewc) {
+    constexpr int EW = decltype(ewc)::value;
+    launch(k_lsd_records<EW, kRecThreads>, RecPass<EW, kRecThreads>::kSmem, kRecThreads);
+  });
+  if (!ok) return cudaErrorInvalidValue;
+  if (e != cudaSuccess) return e;
+  note_launches(1);
+  return cudaGetLastError();
+}
 
 template <int NW, bool IDX>
 static cudaError_t launch_onesweep(const uint64_t* keys_in, const uint32_t* idx_in, uint64_t* keys_out,

@@ -5,6 +5,7 @@ the stable order by radix (stdlib/msort.c keeps ties in input order), so
 the expected result is unique.
 """
 import ctypes
+import os
 
 import numpy
 import pytest
@@ -13,6 +14,7 @@ import oracle as O
 from conftest import golden_cases
 
 pytestmark = pytest.mark.gpu
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 METHODS = ["plain", "learned", "lsd"]
 
@@ -164,6 +166,61 @@ def test_generic_path_layouts(mp, n):
         info = numpy.iinfo(f.dtype)
         a[key] = rng.integers(max(info.min, -20), min(info.max, 20), f.shape)
         check(mp, a, key, "auto")
+
+
+def test_lsd_record_passes(mp, tmp_path):
+    """The LSD passes that carry records of 8-32 bytes (GBSORT_LSD_RECORDS=1,
+    read at load time, so in a child process) give the same bytes as the
+    default key + index passes and gather, which this process runs.  The
+    child also sorts one case in place on the device in one pass (only one
+    digit varies, found by the constant-digit check at >= 2^22 records)."""
+    import subprocess
+    import sys
+    rng = numpy.random.default_rng(21)
+    cases = {
+        "r16": make([('key', 'u8'), ('v', 'i8')], 'key', 300_001, "dups", rng),
+        "r12": make([('key', 'i8'), ('v', 'u4')], 'key', 70_001, "uniform", rng),
+        "r24": numpy.zeros(50_000, numpy.dtype([('k', ('u8', 2)), ('v', 'u8')])),
+        "r32": numpy.zeros(40_000, numpy.dtype([('k', ('i8', 4))])),
+    }
+    cases["r24"]['k'] = rng.integers(0, 50, cases["r24"]['k'].shape, dtype=numpy.uint64)
+    cases["r24"]['v'] = numpy.arange(50_000)
+    cases["r32"]['k'] = rng.integers(-5, 5, cases["r32"]['k'].shape)
+    keys = {"r16": 'key', "r12": 'key', "r24": 'k', "r32": 'k'}
+    for name, a in cases.items():
+        numpy.save(tmp_path / (name + "_in.npy"), a)
+        out = check(mp, a, keys[name], "lsd")
+        assert mp.last_stats()["lsd_passes"] == 8 * (a.dtype[keys[name]].itemsize // 8)
+        numpy.save(tmp_path / (name + "_default.npy"), out)
+    # one pass, in place on the device: keys below 256 in 8-byte records
+    dt8 = numpy.dtype([('key', 'u8')])
+    big = numpy.zeros((1 << 22) + 5, dt8)
+    big['key'] = numpy.arange(len(big), dtype=numpy.uint64)[::-1] % 251
+    numpy.save(tmp_path / "big_in.npy", big)
+    numpy.save(tmp_path / "big_exp.npy", O.numpy_sorted(big, 'key'))
+    script = (
+        "import sys, numpy, torch\n"
+        "sys.path[:0] = %r\n"
+        "import mpsort\n"
+        "from mpsort import device\n"
+        "t = %r\n"
+        "for name, key in %r.items():\n"
+        "    a = numpy.load(t + '/' + name + '_in.npy')\n"
+        "    out = numpy.empty_like(a)\n"
+        "    mpsort.sort(a, key, out=out, method='lsd')\n"
+        "    numpy.save(t + '/' + name + '_records.npy', out)\n"
+        "big = numpy.load(t + '/big_in.npy')\n"
+        "d = torch.from_numpy(big.view(numpy.uint8).copy()).cuda()\n"
+        "device.sort(d.data_ptr(), d.data_ptr(), len(big), big.dtype, 'key', 'lsd')\n"
+        "torch.cuda.synchronize()\n"
+        "assert mpsort.last_stats()['lsd_passes'] == 1\n"
+        "assert d.cpu().numpy().tobytes() == numpy.load(t + '/big_exp.npy').tobytes()\n"
+        % ([os.path.join(REPO, "mp-sort_gb300"), os.path.join(REPO, "oracle")], str(tmp_path), keys))
+    env = dict(os.environ, GBSORT_LSD_RECORDS="1")
+    subprocess.run([sys.executable, "-c", script], env=env, check=True, timeout=600)
+    for name in cases:
+        assert numpy.load(tmp_path / (name + "_records.npy")).tobytes() == \
+            numpy.load(tmp_path / (name + "_default.npy")).tobytes(), name
 
 
 def test_in_place_and_aliasing(mp):
