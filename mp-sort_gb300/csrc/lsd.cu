@@ -23,8 +23,14 @@ namespace gb {
 
 namespace {
 
-constexpr int kLsdRpt = 8;                      // items per thread per tile
-constexpr int kLsdTile = kThreads * kLsdRpt;    // 4096
+#ifndef GB_LSD_THREADS
+#define GB_LSD_THREADS 512
+#endif
+// Key + index passes: 512-thread CTAs (tiles of 4096) measured 5% faster on
+// 1e9 x 16 B than 256-thread ones (tiles of 2048).
+constexpr int kLsdThreads = GB_LSD_THREADS;
+constexpr int kLsdRpt = 8;                          // items per thread per tile
+constexpr int kLsdTile = kLsdThreads * kLsdRpt;     // 4096
 
 __global__ void k_extract_keys(const uint8_t* __restrict__ rec, uint32_t n, uint32_t elsize,
                                gbsort_key_desc key, int aligned4, uint64_t* __restrict__ keys,
@@ -95,7 +101,7 @@ __device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long lon
 // One LSD pass on digit (word, shift).  starts[d] = first output slot of
 // digit d; status holds ntiles * 256 zeroed words; *ticket starts at 0.
 template <int NW, bool IDX>
-__global__ void __launch_bounds__(kThreads) k_lsd_onesweep(const uint64_t* __restrict__ keys_in,
+__global__ void __launch_bounds__(kLsdThreads) k_lsd_onesweep(const uint64_t* __restrict__ keys_in,
                                                             const uint32_t* __restrict__ idx_in,
                                                             uint64_t* __restrict__ keys_out,
                                                             uint32_t* __restrict__ idx_out, uint32_t n, int word,
@@ -103,9 +109,10 @@ __global__ void __launch_bounds__(kThreads) k_lsd_onesweep(const uint64_t* __res
                                                             unsigned long long* status, uint32_t* ticket,
                                                             uint32_t* err, uint32_t spin_limit,
                                                             uint32_t withhold_tile) {
-  using Rank = BlockRank<kLsdRpt, 8>;
+  using Rank = BlockRank<kLsdRpt, 8, kLsdThreads>;
+  static_assert(kLsdThreads >= 256, "one thread per digit in the look-back");
   __shared__ uint16_t hist[Rank::kCounters];
-  __shared__ uint32_t scan_tmp[kWarps];
+  __shared__ uint32_t scan_tmp[kLsdThreads / 32];
   __shared__ uint32_t start[257];
   __shared__ uint32_t base[256];
   __shared__ uint32_t tile_s;
@@ -181,7 +188,7 @@ __global__ void __launch_bounds__(kThreads) k_lsd_onesweep(const uint64_t* __res
   }
   __syncthreads();
   // runs of equal digits go to consecutive output slots
-  for (uint32_t i = threadIdx.x; i < nvalid; i += kThreads) {
+  for (uint32_t i = threadIdx.x; i < nvalid; i += kLsdThreads) {
     const uint32_t d = (uint32_t)(skeys[word * kLsdTile + i] >> shift) & 255u;
     const uint32_t dest = base[d] + i;
     if (dest >= n) {
@@ -521,7 +528,7 @@ static cudaError_t launch_onesweep(const uint64_t* keys_in, const uint32_t* idx_
   cudaError_t e = cudaFuncSetAttribute(k_lsd_onesweep<NW, IDX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
-  k_lsd_onesweep<NW, IDX><<<lsd_tiles(n), kThreads, smem, stream>>>(keys_in, idx_in, keys_out, idx_out, n, word,
+  k_lsd_onesweep<NW, IDX><<<lsd_tiles(n), kLsdThreads, smem, stream>>>(keys_in, idx_in, keys_out, idx_out, n, word,
                                                                      shift, starts, status, ticket, err,
                                                                      spin_limit, withhold_tile);
   return cudaGetLastError();
