@@ -460,16 +460,21 @@ struct Knobs {
 // Level-1 bucket count: about 2048 records per bucket, at most the cap --
 // the knob, else GBSORT_MAX_BUCKETS (a power of two up to 4096), else 2048.
 // Fewer, larger buckets keep the scatter's runs long enough to fill whole
-// DRAM sectors; the bucket splits then carry more of the work.
-int choose_buckets(uint32_t n, const Knobs& k) {
+// DRAM sectors; the bucket splits then carry more of the work.  4096
+// buckets (1e9 x 16 B) help uniform keys (44.5 against 46.6 ms: smaller
+// splits) but not sorted-with-swaps (36.2 / 34.3 ms), Zipf (62.8 / 55.7 ms)
+// or 40-byte records (69.3 / 60.1 ms): the 16-byte scatter's ranking table
+// and held sectors then leave room for one CTA per SM only.
+int choose_buckets(uint32_t n, uint32_t elsize, const Knobs& k) {
   if (n <= 4096) return 1;
   static int env_cap = -1;
   if (env_cap < 0) {
     const char* e = getenv("GBSORT_MAX_BUCKETS");
     int v = e ? atoi(e) : 0;
-    env_cap = (v >= 2 && v <= 4096 && (v & (v - 1)) == 0) ? v : 2048;
+    env_cap = (v >= 2 && v <= 4096 && (v & (v - 1)) == 0) ? v : 0;
   }
-  const int cap = k.max_buckets ? k.max_buckets : env_cap;
+  (void)elsize;
+  const int cap = k.max_buckets ? k.max_buckets : env_cap ? env_cap : 2048;
   uint64_t want = ((uint64_t)n + 2047) / 2048;
   uint32_t nb = pow2_ceil(want);
   return (int)std::min<uint32_t>(nb, (uint32_t)cap);
@@ -613,8 +618,8 @@ uint32_t hsort_sample_size(uint32_t n, int nb, const Knobs& knobs) {
 
 // Bytes of the small device buffer a histogram sort of n records uses
 // (G: count chunks).
-size_t hsort_small_bytes(uint32_t n, const Knobs& knobs, int G) {
-  const int nb = choose_buckets(n, knobs);
+size_t hsort_small_bytes(uint32_t n, uint32_t elsize, const Knobs& knobs, int G) {
+  const int nb = choose_buckets(n, elsize, knobs);
   const uint32_t s = hsort_sample_size(n, nb, knobs);
   const uint32_t cap_split = (uint32_t)nb + n / 4096 + 4096;
   const uint32_t cap_local = 4u * (uint32_t)nb + n / 512 + 65536;
@@ -629,7 +634,7 @@ size_t hsort_small_bytes(uint32_t n, const Knobs& knobs, int G) {
 // end up in c.hc once the stream reaches the end.  hsort_collect reads them.
 int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_t elsize, const gbsort_key_desc* key,
                   bool learned, bool timing, const Knobs& knobs, cudaStream_t st, const HostPipe* hp = nullptr) {
-  const int nb = choose_buckets(n, knobs);
+  const int nb = choose_buckets(n, elsize, knobs);
   const int grid = hsort_grid(n);
   const uint32_t s = hsort_sample_size(n, nb, knobs);
   // pipelined: the input goes up in pieces, each cut into `grid` count
@@ -653,7 +658,7 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
   const uint32_t cap_local = 4u * (uint32_t)nb + n / 512 + 65536;
   const int lbits = 11;
   const int nleaf = 1 << lbits;
-  GB_CUDA(c.small.ensure(hsort_small_bytes(n, knobs, G)));
+  GB_CUDA(c.small.ensure(hsort_small_bytes(n, elsize, knobs, G)));
   Bump bump{c.small.as<uint8_t>()};
   uint32_t* counters = bump.take<uint32_t>(CNT_WORDS);
   uint32_t* stats = counters;
@@ -1313,7 +1318,7 @@ int segments_enqueue(Context& c, const void* d_in, void* d_out, const std::vecto
     const uint64_t m = offs[i + 1] - offs[i];
     if (m > k.big_above) {
       ++nbig;
-      small_need = std::max(small_need, hsort_small_bytes((uint32_t)m, k.big, hsort_grid((uint32_t)m)));
+      small_need = std::max(small_need, hsort_small_bytes((uint32_t)m, E, k.big, hsort_grid((uint32_t)m)));
     }
   }
   GB_CUDA(c.small.ensure(small_need));

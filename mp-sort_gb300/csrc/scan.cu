@@ -75,17 +75,31 @@ __global__ void __launch_bounds__(kThreads) k_segment_scan(const uint32_t* in, u
 
 }  // namespace
 
-size_t scan_tmp_words(size_t n) { return (n + kSeg - 1) / kSeg + 1; }
+// Words of scratch for a scan of n elements: the segment sums, plus (above
+// kSeg segments) the scratch of scanning those sums the same way.
+size_t scan_tmp_words(size_t n) {
+  const size_t nseg = (n + kSeg - 1) / kSeg;
+  return nseg <= (size_t)kSeg ? nseg + 1 : nseg + scan_tmp_words(nseg);
+}
 
+// Exclusive scan of n counts (out may alias in): segment sums, a scan of the
+// sums (one block, or the same scan again over the sums when there are more
+// than kSeg of them), then each segment scanned from its base.
 cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n, uint32_t* tmp,
                                cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
-  size_t nseg = (n + kSeg - 1) / kSeg;
-  if (nseg > (size_t)kSeg) return cudaErrorInvalidValue;
+  const size_t nseg = (n + kSeg - 1) / kSeg;
+  if (nseg > (size_t)0x7fffffff) return cudaErrorInvalidValue;
   k_segment_sums<<<(unsigned)nseg, kThreads, 0, stream>>>(in, n, tmp);
-  k_scan_sums<<<1, kThreads, 0, stream>>>(tmp, (int)nseg);
+  note_launches(2);
+  if (nseg <= (size_t)kSeg) {
+    k_scan_sums<<<1, kThreads, 0, stream>>>(tmp, (int)nseg);
+    note_launches(1);
+  } else {
+    const cudaError_t e = exclusive_scan_u32(tmp, tmp, nseg, tmp + nseg, stream);
+    if (e != cudaSuccess) return e;
+  }
   k_segment_scan<<<(unsigned)nseg, kThreads, 0, stream>>>(in, out, n, tmp);
-  note_launches(3);
   return cudaGetLastError();
 }
 
