@@ -39,7 +39,7 @@ STAGE_KERNELS = {  # stage_ms key -> (kernel, algorithmic bytes per record, ncu 
     "count": ("k_l1_count", E, "l1_count_16B.md"),
     "scatter": ("k_l1_scatter", 2 * E, "l1_scatter_16B.md"),
     "split": ("k_split", 2 * E, "split_16B.md"),
-    "local": ("k_local", 2 * E, "local_16B.md"),
+    "local": ("k_local_staged", 2 * E, "local_16B.md"),
 }
 PIPELINE_BYTES_PER_RECORD = 2 * 2 * E
 

@@ -498,6 +498,9 @@ struct Tile {
 #ifndef GB_SCATTER_PREFETCH
 #define GB_SCATTER_PREFETCH 1
 #endif
+#ifndef GB_SCATTER_CTAS
+#define GB_SCATTER_CTAS 2  // level-1 scatter CTAs per SM (the register budget follows)
+#endif
 // Tile of the level-1 scatter: up to GB_SCATTER_RPT / EW records per thread.
 template <int EW>
 struct ScatterTile {
@@ -537,7 +540,7 @@ __device__ __forceinline__ void store_sector(uint8_t* p, const uint4& a, const u
 // bucket) and written together with its partner, the next tile's first
 // record of that bucket; slots still held at the chunk's end are flushed.
 template <int EW, int LK>
-__global__ void __launch_bounds__(kThreads, 2) k_l1_scatter(HsortParams p, const uint64_t* __restrict__ S,
+__global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortParams p, const uint64_t* __restrict__ S,
                                                              int nbuckets, ModelDev model,
                                                              const uint32_t* __restrict__ offsets,
                                                              int nchunks, uint32_t* __restrict__ stats,
@@ -846,9 +849,30 @@ struct LocalSmemT {
 };
 constexpr int kSplitTileBytes = kThreads * 64;  // a scatter tile: kThreads * RPT records of <= 16 / RPT words
 static_assert(kFineBins * 4 <= kSplitTileBytes, "the fine histogram fits the staging tile");
-struct SplitSmem {
-  __align__(16) uint8_t stage[kSplitTileBytes];  // the tile in group order
-  uint16_t sgrp[kThreads * 4];                   // group of each staged record
+// Staged splits (records of 8-16 bytes): the bucket streams through two
+// tile buffers filled by bulk asynchronous copies, each a tile's bytes plus
+// the 16-byte rounding of both its ends.
+constexpr int kSplitBufBytes = 24576 + 128;
+constexpr int kSplitStageBytes = 2 * kSplitBufBytes;
+static_assert(kSplitStageBytes >= kSplitTileBytes, "the staging area holds an unstaged tile");
+template <int EW>
+__host__ __device__ constexpr bool split_staged() {
+  return EW >= 2 && EW <= 4;
+}
+// Records per staged tile: 24 KB of 16-byte records, 2048 smaller ones.
+template <int EW>
+__host__ __device__ constexpr int staged_split_tile() {
+  return EW == 4 ? 1536 : 2048;
+}
+// Shared memory of a split; SB: bytes of the staging area (kSplitTileBytes,
+// or kSplitStageBytes for staged splits -- the unstaged splits and the
+// engine keep the smaller one, which leaves L1 more room for their loads).
+template <int SB>
+struct SplitSmemT {
+  static constexpr bool kStaged = SB > kSplitTileBytes;
+  __align__(128) uint8_t stage[SB];  // the tile in group order, or two staged tiles
+  uint16_t sgrp[kThreads * 4];                // group of each record in group order
+  uint16_t perm[kStaged ? kThreads * 4 : 1];  // staged: input slot of each record in group order
   uint32_t goff[kMaxGroups];                     // first staged slot of each group
   uint32_t hist[kSplitBins];  // bin counts; for refined bins then (first fine bin << 4 | sub-bin bits)
   uint16_t gmap[kFineBins];
@@ -861,7 +885,12 @@ struct SplitSmem {
   uint32_t task_id;
   SortTask next;
   uint32_t emit_base;  // the engine's reservation for this split's groups
+  uint64_t bar[2];     // staged tiles: completion of each buffer's copy
 };
+using SplitSmem = SplitSmemT<kSplitTileBytes>;
+using SplitSmemStaged = SplitSmemT<kSplitStageBytes>;
+template <int EW>
+using SplitSmemOf = typename std::conditional<split_staged<EW>(), SplitSmemStaged, SplitSmem>::type;
 
 template <int NT = kThreads>
 __device__ __forceinline__ void block_minmax(uint64_t& mn, uint64_t& mx, uint64_t* red) {
@@ -1455,9 +1484,68 @@ struct RoundSink {
   }
 };
 
-template <int EW, typename Sink>
-__device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& task, const Sink& L,
-                           uint32_t* stats, uint32_t* err) {
+// A bucket's records streamed through the split's two staging buffers:
+// thread 0 keeps the next two tiles in flight (bulk asynchronous copies of
+// the tiles' 16-byte aligned byte ranges; the rounding reads at most 15
+// bytes on either side, inside the scratch allocation), every thread waits
+// for each tile in turn.  par holds each buffer's next completion parity,
+// the same in every thread (every thread waits for every tile).
+template <int EW>
+struct SplitTiles {
+  static constexpr uint32_t E = EW * 4;
+  static constexpr uint32_t T = staged_split_tile<EW>();
+  static_assert(T * E + 32 <= (uint32_t)kSplitBufBytes, "a staged tile fits its buffer");
+  const uint8_t* src;
+  uint32_t m;
+  SplitSmemStaged& sm;
+  uint32_t& par;
+
+  __device__ __forceinline__ void issue(uint32_t i) const {  // thread 0: tile i into buffer i & 1
+    const uint32_t t0 = i * T;
+    const uint32_t cnt = min(T, m - t0);
+    const uintptr_t a = (uintptr_t)(src + (size_t)t0 * E);
+    const uintptr_t a0 = a & ~(uintptr_t)15;
+    const uint32_t bytes = (uint32_t)(((a - a0) + (uintptr_t)cnt * E + 15) & ~(uintptr_t)15);
+    bulk_load(sm.stage + (size_t)(i & 1) * kSplitBufBytes, (const void*)a0, bytes, &sm.bar[i & 1]);
+  }
+  // After a barrier that ends every thread's use of both buffers.
+  __device__ __forceinline__ void start() const {
+    if (threadIdx.x == 0) {
+      fence_proxy_async_smem();
+      issue(0);
+      if (T < m) issue(1);
+    }
+  }
+  // Waits for tile i (with a barrier); its first record, or nullptr if the
+  // wait ran out -- then DEV_ERR_TIMEOUT is set and the CTA's copies still
+  // in flight have been waited for, and the caller must leave.
+  __device__ __forceinline__ const uint8_t* wait(uint32_t i, uint32_t* err) const {
+    const uint32_t b = i & 1;
+    const bool ok = __syncthreads_and(mbar_wait_bounded(&sm.bar[b], (par >> b) & 1u, kBulkWaitPolls));
+    if (!ok) {
+      if (threadIdx.x == 0) set_error(err, DEV_ERR_TIMEOUT);
+      mbar_wait_bounded(&sm.bar[b], (par >> b) & 1u, kBulkWaitPolls);
+      if ((i + 1) * T < m) mbar_wait_bounded(&sm.bar[b ^ 1], (par >> (b ^ 1)) & 1u, kBulkWaitPolls);
+      return nullptr;
+    }
+    par ^= 1u << b;
+    return sm.stage + (size_t)b * kSplitBufBytes + ((uintptr_t)src & 15);
+  }
+  // After a barrier that ends every thread's use of tile i: its buffer takes tile i + 2.
+  __device__ __forceinline__ void release(uint32_t i) const {
+    if (threadIdx.x == 0 && (i + 2) * T < m) {
+      fence_proxy_async_smem();
+      issue(i + 2);
+    }
+  }
+};
+
+// One bucket split.  STAGED: the histogram and scatter passes stream the
+// bucket through shared memory (SplitTiles) instead of loading records
+// into registers; false if a staged wait ran out (the CTA must leave).
+template <int EW, bool STAGED, typename Sink, typename SM>
+__device__ bool split_task(SM& sm, const HsortParams& p, const SortTask& task, const Sink& L,
+                           uint32_t* stats, uint32_t* err, uint32_t& par) {
   constexpr uint32_t E = EW * 4;
   constexpr int RPT = Tile<EW>::kRpt, T = Tile<EW>::kSize;
   const bool in_b = (task.flags & TASK_SRC_B) != 0;
@@ -1477,27 +1565,35 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
     for (int i = threadIdx.x; i < kSplitBins; i += kThreads) sm.hist[i] = 0;
     __syncthreads();
     uint64_t mn = ~0ull, mx = 0;
-    constexpr int U = 8;  // keys in flight per thread
-    for (uint32_t i0 = 0; i0 < m; i0 += kThreads * U) {
-      uint64_t kk[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        uint32_t i = i0 + u * kThreads + threadIdx.x;
-        kk[u] = i < m ? key_at(src, i, E, p.key) : 0;
+    auto add = [&](uint64_t key) {
+      mn = key < mn ? key : mn;
+      mx = key > mx ? key : mx;
+      const uint64_t x = key > blo ? key - blo : 0;
+      atomicAdd(&sm.hist[(uint32_t)min(x >> shift, (uint64_t)(nbins - 1))], 1u);
+    };
+    if constexpr (STAGED) {
+      const SplitTiles<EW> tiles{src, m, sm, par};
+      tiles.start();
+      for (uint32_t i = 0; i * tiles.T < m; ++i) {
+        const uint8_t* rb = tiles.wait(i, err);
+        if (!rb) return false;
+        const uint32_t nvalid = min(tiles.T, m - i * tiles.T);
+        for (uint32_t e = threadIdx.x; e < nvalid; e += kThreads) add(load_key_aligned4(rb + (size_t)e * E, p.key));
+        __syncthreads();
+        tiles.release(i);
       }
+    } else {
+      constexpr int U = 8;  // keys in flight per thread
+      for (uint32_t i0 = 0; i0 < m; i0 += kThreads * U) {
+        uint64_t kk[U];
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        uint32_t i = i0 + u * kThreads + threadIdx.x;
-        bool v = i < m;
-        uint32_t bin = 0xffffffffu;
-        if (v) {
-          uint64_t key = kk[u];
-          mn = key < mn ? key : mn;
-          mx = key > mx ? key : mx;
-          uint64_t x = key > blo ? key - blo : 0;
-          bin = (uint32_t)min(x >> shift, (uint64_t)(nbins - 1));
+        for (int u = 0; u < U; ++u) {
+          uint32_t i = i0 + u * kThreads + threadIdx.x;
+          kk[u] = i < m ? key_at(src, i, E, p.key) : 0;
         }
-        if (v) atomicAdd(&sm.hist[bin], 1u);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (i0 + u * kThreads + threadIdx.x < m) add(kk[u]);
       }
     }
     block_minmax(mn, mx, sm.red);
@@ -1620,6 +1716,73 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
   static_assert(kMaxGroups == kThreads, "one group per thread in the tile scan");
   static_assert(T <= kThreads * 4 && T * E <= kSplitTileBytes, "tile staging size");
   const uint32_t g_me = threadIdx.x;
+  if constexpr (STAGED) {
+    // the tile arrives in input order; its records leave from there in group
+    // order through perm (input slot of each group-ordered record)
+    constexpr int SRPT = staged_split_tile<EW>() / kThreads;
+    static_assert(SRPT * kThreads == staged_split_tile<EW>() && SRPT <= 4, "staged tile shape");
+    using V = typename std::conditional<E % 16 == 0, uint4,
+                                        typename std::conditional<E % 8 == 0, uint2, uint32_t>::type>::type;
+    constexpr uint32_t VPR = E / sizeof(V);
+    const SplitTiles<EW> tiles{src, m, sm, par};
+    tiles.start();
+    for (uint32_t i = 0; i * tiles.T < m; ++i) {
+      const uint32_t nvalid = min(tiles.T, m - i * tiles.T);
+      const uint8_t* rb = tiles.wait(i, err);  // (a barrier: the last tile's rows are clear)
+      if (!rb) return false;
+      uint32_t grp[SRPT], rank[SRPT], lead[SRPT];
+#pragma unroll
+      for (int r = 0; r < SRPT; ++r) {
+        const uint32_t e = w * 32 * SRPT + r * 32 + lane;
+        grp[r] = kNoBucket;
+        if (e < nvalid) {
+          const uint64_t key = load_key_aligned4(rb + (size_t)e * E, p.key);
+          uint32_t bin;
+          if (refined) {
+            bin = fine_bin(sm.hist, key, blo, shift, nbins);
+          } else {
+            const uint64_t x = key > blo ? key - blo : 0;
+            bin = (uint32_t)min(x >> shift, (uint64_t)(nbins - 1));
+          }
+          grp[r] = sm.gmap[bin];
+        }
+      }
+      warp_ranks<SRPT, kGroupBits>(grp, rank, lead, sm.gcnt);
+      __syncthreads();
+      uint32_t gtot;
+      tile_rank(g_me, 0, sm.gcnt, gtot);
+      const uint32_t goff = block_exclusive_scan<uint32_t>(gtot, sm.scan_tmp, nullptr);
+      sm.goff[g_me] = goff;
+      __syncthreads();
+#pragma unroll
+      for (int r = 0; r < SRPT; ++r) {
+        if (grp[r] == kNoBucket) continue;
+        uint32_t all;
+        const uint32_t slot = sm.goff[grp[r]] + tile_rank(grp[r], rank[r], sm.gcnt, all);
+        if (slot >= nvalid) {  // impossible with consistent ranks
+          set_error(err, DEV_ERR_COUNT_MISMATCH);
+          continue;
+        }
+        sm.perm[slot] = (uint16_t)(w * 32 * SRPT + r * 32 + lane);
+        sm.sgrp[slot] = (uint16_t)grp[r];
+      }
+      __syncthreads();
+      for (uint32_t f = threadIdx.x; f < nvalid * VPR; f += kThreads) {
+        const uint32_t j = f / VPR, qw = f % VPR;
+        const uint32_t g = sm.sgrp[j] & (kMaxGroups - 1);
+        const uint32_t from = min((uint32_t)sm.perm[j], nvalid - 1);
+        const uint32_t dest = sm.cursor[g] + (j - sm.goff[g]);
+        if (dest < m)
+          reinterpret_cast<V*>(oth + (size_t)dest * E)[qw] = reinterpret_cast<const V*>(rb + (size_t)from * E)[qw];
+        else set_error(err, DEV_ERR_COUNT_MISMATCH);
+      }
+      __syncthreads();
+      tiles.release(i);
+      sm.cursor[g_me] += gtot;
+      clear_rows<SRPT>(grp, lead, sm.gcnt);
+    }
+    __syncthreads();
+  } else
   for (uint32_t t0 = 0; t0 < m; t0 += T) {
     const uint32_t nvalid = min((uint32_t)T, m - t0);
     // the tile after next heads for L2 (its loads below then wait on L2, not DRAM)
@@ -1710,7 +1873,7 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
                             : make_task(start, s, glo, ghi, nsrc_b, false);
                 },
                 &sm.emit_base, sm.scan_tmp, err);
-    return;
+    return true;
   } else {
     for (int g = threadIdx.x; g < kMaxGroups; g += kThreads) {
       const uint32_t g0 = sm.gstart[g], g1 = sm.gstart[g + 1];
@@ -1732,15 +1895,22 @@ __device__ void split_task(SplitSmem& sm, const HsortParams& p, const SortTask& 
     }
     __syncthreads();
   }
+  return true;
 }
 
 template <int EW>
 __global__ void __launch_bounds__(kThreads, 2) k_split(HsortParams p, TaskLists L, uint32_t* __restrict__ work,
                                                         uint32_t* __restrict__ stats, uint32_t* __restrict__ err) {
-  extern __shared__ __align__(16) uint8_t smem_raw[];
-  SplitSmem& sm = *reinterpret_cast<SplitSmem*>(smem_raw);
+  extern __shared__ __align__(128) uint8_t smem_raw[];
+  SplitSmemOf<EW>& sm = *reinterpret_cast<SplitSmemOf<EW>*>(smem_raw);
   const uint32_t nt = min(*L.nsplit_in, L.cap_split);
   for (int i = threadIdx.x; i < kMaxGroups * kWarps; i += kThreads) sm.gcnt[i] = 0;
+  if (threadIdx.x == 0) {
+    mbar_init(&sm.bar[0], 1);
+    mbar_init(&sm.bar[1], 1);
+    mbar_init_fence();
+  }
+  uint32_t par = 0;  // next completion parity of each staging buffer
   for (;;) {
     if (threadIdx.x == 0) {
       uint32_t id = atomicAdd(work, 1u);
@@ -1775,7 +1945,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split(HsortParams p, TaskLists 
       continue;
     }
     if (threadIdx.x == 0) atomicAdd(stats + STAT_SPLIT, 1u);
-    split_task<EW>(sm, p, task, RoundSink{L}, stats, err);
+    if (!split_task<EW, split_staged<EW>()>(sm, p, task, RoundSink{L}, stats, err, par)) return;
   }
 }
 
@@ -2071,7 +2241,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_engine(HsortParams p, EngineQue
         for (int i = threadIdx.x; i < kMaxGroups * kWarps / 16; i += kThreads)
           reinterpret_cast<uint4*>(ssm.gcnt)[i] = make_uint4(0, 0, 0, 0);
       if (threadIdx.x == 0) atomicAdd(stats + STAT_SPLIT, 1u);
-      split_task<EW>(ssm, p, task, sink, stats, err);
+      uint32_t unused_par = 0;
+      split_task<EW, false>(ssm, p, task, sink, stats, err, unused_par);
       if (threadIdx.x == 0) c.dirty = kDirtyBins;
     } else {
       if (c.dirty & kDirtyBins)  // the local sort expects zero bins (the barrier below follows)
@@ -2257,7 +2428,7 @@ cudaError_t l1_scatter(const HsortParams& p, int lookup_kind, const uint64_t* sp
   const int g = p.chunks ? (int)p.chunks : hsort_grid(p.n);
   if (c1 < 0) c1 = g;
   if (c1 <= c0) return cudaSuccess;
-  const int ctas = std::min(hsort_grid(p.n), c1 - c0);
+  const int ctas = std::min(std::min(hsort_grid(p.n), num_sms() * GB_SCATTER_CTAS), c1 - c0);
   cudaError_t e = cudaSuccess;
   bool ok = dispatch_ew(p.elsize, [&](auto ewc) {
     constexpr int EW = decltype(ewc)::value;
@@ -2423,7 +2594,7 @@ cudaError_t run_split_round(const HsortParams& p, const TaskListsHost& lists, ui
   if (e != cudaSuccess) return e;
   bool ok = dispatch_ew(p.elsize, [&](auto ewc) {
     constexpr int EW = decltype(ewc)::value;
-    size_t sm = sizeof(SplitSmem);
+    size_t sm = sizeof(SplitSmemOf<EW>);
     e = set_smem((const void*)k_split<EW>, sm);
     if (e == cudaSuccess)
       k_split<EW><<<split_grid(), kThreads, sm, stream>>>(p, lists_of(lists), work_counter, stats, err);
