@@ -97,8 +97,16 @@ __device__ __forceinline__ uint32_t reg_select(const uint32_t (&a)[N], uint32_t 
 }
 
 // Key of a record held in registers as E_WORDS 32-bit words.
+// A 64-bit key first in the record takes a branch of its own (uniform over
+// the grid): no word selection (1e9 x 16 B level-1 scatter 17.9 -> 17.5 ms).
 template <int E_WORDS>
 __device__ __forceinline__ uint64_t key_from_regs(const uint32_t (&r)[E_WORDS], const gbsort_key_word& w) {
+  if constexpr (E_WORDS >= 2) {
+    if (w.offset == 0 && w.width == 8) {
+      const uint64_t raw = (uint64_t)r[0] | ((uint64_t)r[1] << 32);
+      return w.is_signed ? raw ^ 0x8000000000000000ull : raw;
+    }
+  }
   uint32_t k = w.offset >> 2;
   uint64_t raw = reg_select<E_WORDS>(r, k);
   if (w.width == 8) raw |= (uint64_t)reg_select<E_WORDS>(r, k + 1) << 32;

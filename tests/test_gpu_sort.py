@@ -752,6 +752,36 @@ def test_host_sort_pipelined_pinned(mp, method, dist, regions, monkeypatch):
     assert hin.tobytes() == exp.tobytes()
 
 
+@pytest.mark.parametrize("regions", [True, False])
+def test_host_sort_pipelined_4096_buckets(mp, regions, monkeypatch):
+    """A tuning entry of 4096 level-1 buckets for a pipelined host sort: its
+    (bucket x chunk) count matrix (4096 buckets x 16 pieces x 304 chunks,
+    19.9M cells) is past one block's scan of the segment sums, so the count
+    scan takes its second level.  Same stable order as the oracle's."""
+    import torch
+    from mpsort import device
+    if not regions:
+        monkeypatch.setenv("GBSORT_NO_REGIONS", "1")
+    rng = numpy.random.default_rng(53)
+    dt = numpy.dtype([('key', 'u8'), ('val', 'i8')])
+    n = 10_000_000
+    a = make(dt, 'key', n, "uniform", rng)
+    pin_in = torch.empty(n * dt.itemsize, dtype=torch.uint8, pin_memory=True)
+    pin_out = torch.empty_like(pin_in, pin_memory=True)
+    hin = pin_in.numpy().view(dt)
+    hout = pin_out.numpy().view(dt)
+    hin[:] = a
+    device.tuning_clear()
+    device.tuning_set(n, dt, 'key', "learned", max_buckets=4096)
+    try:
+        mp.sort(hin, 'key', out=hout, method="auto")
+        st = mp.last_stats()
+    finally:
+        device.tuning_clear()
+    assert st["nbuckets"] == 4096 and st["pipelined"] == 1, st
+    assert hout.tobytes() == O.numpy_sorted(a, 'key').tobytes()
+
+
 # ----------------------------------------------- bounded look-back wait --
 def test_lookback_wait_runs_out_and_reports(mp):
     """One LSD pass in which a tile never publishes its counts: the next
