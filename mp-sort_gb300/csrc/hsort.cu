@@ -400,6 +400,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_l1_count(HsortParams p, const u
   extern __shared__ __align__(16) uint8_t smem[];
   LookupSmem L;
   uint32_t* hist = reinterpret_cast<uint32_t*>(load_lookup<LK>(smem, S, nbuckets, model, L));
+  if constexpr (LK == LOOKUP_LEARNED) {
+    // the learned lookup's window searches read splitters from shared
+    // memory here too (the count has room for them): keys next to heavy-key
+    // steps have wide windows (Zipf keys, 1e9 x 16 B: count 8.7 -> 7.9 ms;
+    // 5e8 x 40 B Morton keys 3.8 -> 3.4 ms)
+    uint64_t* Ss = reinterpret_cast<uint64_t*>(hist + ((nbuckets + 1) & ~1));
+    for (int i = threadIdx.x; i < nbuckets - 1; i += kThreads) Ss[i] = S[i];
+    L.S = Ss;
+  }
   for (int i = threadIdx.x; i < nbuckets; i += kThreads) hist[i] = 0;
   __syncthreads();
   const uint32_t hprobes = p.heavy ? p.heavy->probes : 0;
@@ -2397,7 +2406,8 @@ cudaError_t l1_count(const HsortParams& p, int lookup_kind, const uint64_t* spli
   if (c1 <= c0) return cudaSuccess;
   cudaError_t e;
   if (lookup_kind == LOOKUP_LEARNED) {
-    size_t sm = lookup_smem_bytes<LOOKUP_LEARNED>(nbuckets, &m) + 4 * (size_t)nbuckets;
+    size_t sm = lookup_smem_bytes<LOOKUP_LEARNED>(nbuckets, &m) + 4 * (size_t)((nbuckets + 1) & ~1) +
+                8 * (size_t)nbuckets;
     if ((e = set_smem((const void*)k_l1_count<LOOKUP_LEARNED>, sm)) != cudaSuccess) return e;
     k_l1_count<LOOKUP_LEARNED><<<c1 - c0, kThreads, sm, stream>>>(p, splitters, nbuckets, m, counts, stats,
                                                                   (uint32_t)c0, (uint32_t)g);
