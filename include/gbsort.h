@@ -78,6 +78,10 @@ typedef struct gbsort_stats {
     uint32_t engine;             /* 1: level 2 (bucket splits, local sorts, copies) ran as one
                                     persistent launch over a device task queue; stage_ms[4] then
                                     holds all of level 2 and stage_ms[5] is 0 */
+    uint32_t uniform_splits;     /* level-1 buckets of 8-16 byte records split into equal key ranges
+                                    without a histogram pass (smooth keys) */
+    uint32_t uniform_fallbacks;  /* such attempts in which a group outgrew its region: the bucket was
+                                    then split by its histogram (same result) */
 } gbsort_stats;
 
 /* OR into `method`: hash the records (gbsort_multiset_hash_device) before

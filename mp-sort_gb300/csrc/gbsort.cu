@@ -116,6 +116,7 @@ enum CounterSlot : int {
   CNT_L2 = 24,           // level-2 task counters: nsplit[2], nlocal, work
   CNT_FALLBACK = 28,     // the learned splitters were rejected
   CNT_HEAVY = 30,        // keys in the heavy-key table
+  CNT_UNIFORM = 36,      // uniform bucket splits: tried, then failed (2 words)
   CNT_OVERFLOW = 31,     // a bucket outgrew its reserved region (pipelined host sort): bucket + 1,
                          // then its capacity and count (3 words)
   CNT_ENGINE = 48,       // the level-2 engine's queue: tail, head, pending, kEngineCtlStride apart
@@ -652,8 +653,13 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
     if (region_fit) a_cap64 = (uint64_t)reserved;
   }
   const uint32_t a_cap = (uint32_t)std::max<uint64_t>(a_cap64, n);
+  // areas: the split rounds of records of 8-16 bytes give each level-1
+  // bucket an area of scratch B a quarter larger than the bucket (uniform
+  // splits scatter into regions there); the persistent engine does not
+  const bool areas = elsize % 4 == 0 && elsize >= 8 && elsize <= 16 && n <= kSplitAreaMaxN &&
+                     (hp || !use_engine(elsize, knobs.level2, false));
   GB_CUDA(c.A.ensure((size_t)a_cap * elsize + kScratchSlack));
-  GB_CUDA(c.B.ensure((size_t)n * elsize + kScratchSlack));
+  GB_CUDA(c.B.ensure((size_t)(areas ? split_area(n) : n) * elsize + kScratchSlack));
   const uint32_t cap_split = (uint32_t)nb + n / 4096 + 4096;
   const uint32_t cap_local = 4u * (uint32_t)nb + n / 512 + 65536;
   const int lbits = 11;
@@ -684,6 +690,11 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
   p.key = key->word[0];
   p.a_cap = a_cap;
   p.chunks = (uint32_t)G;
+  p.areas = areas ? 1u : 0u;
+  static const bool uniform_off = getenv("GBSORT_UNIFORM_SPLITS") && atoi(getenv("GBSORT_UNIFORM_SPLITS")) == 0;
+  p.uniform = areas && !uniform_off ? counters + CNT_UNIFORM : nullptr;
+  p.gate_widest = counters + CNT_WIDEST;
+  p.gate_heavy = counters + CNT_HEAVY;
 
   ModelDev model{};
   int lookup = LOOKUP_PLAIN;
@@ -931,6 +942,8 @@ int hsort_collect(Context& c) {
   g_stats.pipelined = c.run_pipelined ? 1u : 0u;
   g_stats.region_overflow = c.run_pipelined ? h[CNT_OVERFLOW] : 0u;
   g_stats.engine = c.run_engine ? 1u : 0u;
+  g_stats.uniform_splits = h[CNT_UNIFORM] - h[CNT_UNIFORM + 1];
+  g_stats.uniform_fallbacks = h[CNT_UNIFORM + 1];
   if (c.run_timing)
     for (int i = 0; i < 6; ++i) {
       float ms = 0.f;
@@ -1323,7 +1336,8 @@ int segments_enqueue(Context& c, const void* d_in, void* d_out, const std::vecto
   }
   GB_CUDA(c.small.ensure(small_need));
   GB_CUDA(c.A.ensure((size_t)N * E + kScratchSlack));
-  GB_CUDA(c.B.ensure((size_t)N * E + kScratchSlack));
+  // (the areas of a segment sorted on its own fit too: no growth later)
+  GB_CUDA(c.B.ensure((size_t)(E >= 8 && E <= 16 && N <= kSplitAreaMaxN ? split_area(N) : N) * E + kScratchSlack));
   uint32_t bi = 0;
   uint64_t nbig_records = 0;
   for (size_t i = 0; i < nseg; ++i) {
@@ -1404,6 +1418,8 @@ int segments_collect(Context& c, const uint32_t* h_errs, uint32_t nerrs) {
   g_stats.resplits = h[STAT_PUSHED];
   g_stats.bigbin_passes = h[STAT_BIGBIN];
   g_stats.engine = c.run_engine ? 1u : 0u;
+  g_stats.uniform_splits = h[CNT_UNIFORM] - h[CNT_UNIFORM + 1];
+  g_stats.uniform_fallbacks = h[CNT_UNIFORM + 1];
   return GBSORT_OK;
 }
 

@@ -741,12 +741,14 @@ __device__ __forceinline__ void push(SortTask* list, uint32_t* n, uint32_t cap, 
   else set_error(err, DEV_ERR_TASK_OVERFLOW);
 }
 
-// Copies of single-key ranges go to the local list in pieces of kCopyPiece.
-__device__ __forceinline__ void push_copy(const TaskLists& L, uint32_t start, uint32_t cnt, uint64_t lo, uint64_t hi,
-                                          uint32_t src, uint32_t* err) {
+// Copies of single-key ranges go to the local list in pieces of kCopyPiece:
+// records [from, from + cnt) of the buffer `flags` names to output
+// positions [start, start + cnt).
+__device__ __forceinline__ void push_copy(const TaskLists& L, uint32_t start, uint32_t from, uint32_t cnt,
+                                          uint64_t lo, uint64_t hi, uint32_t flags, uint32_t* err) {
   for (uint32_t s0 = 0; s0 < cnt; s0 += kCopyPiece)
-    push(L.local, L.nlocal, L.cap_local, make_task(start + s0, min(kCopyPiece, cnt - s0), lo, hi, src != 0, true),
-         err);
+    push(L.local, L.nlocal, L.cap_local,
+         make_task_at(start + s0, from + s0, min(kCopyPiece, cnt - s0), lo, hi, flags | TASK_COPY), err);
 }
 
 __global__ void k_build_tasks(const uint32_t* __restrict__ offsets, int grid,
@@ -761,9 +763,9 @@ __global__ void k_build_tasks(const uint32_t* __restrict__ offsets, int grid,
   atomicMax(stats + STAT_MAX_BUCKET, cnt);
   uint64_t lo = b == 0 ? 0ull : S[b - 1];
   uint64_t hi = b == nbuckets - 1 ? ~0ull : S[b] - 1;
-  if (lo == hi || cnt == 1) push_copy(L, start, cnt, lo, hi, 0u, err);
+  if (lo == hi || cnt == 1) push_copy(L, start, start, cnt, lo, hi, 0u, err);
   else if (cnt <= (uint32_t)kLocalMax) push(L.local, L.nlocal, L.cap_local, make_task(start, cnt, lo, hi, false, false), err);
-  else push(L.split_out, L.nsplit_out, L.cap_split, make_task(start, cnt, lo, hi, false, false), err);
+  else push(L.split_out, L.nsplit_out, L.cap_split, make_task_at(start, start, cnt, lo, hi, TASK_L1), err);
 }
 
 // Largest split task first: the level-1 buckets differ in size by tens of
@@ -891,6 +893,7 @@ struct SplitSmemT {
   SortTask next;
   uint32_t emit_base;  // the engine's reservation for this split's groups
   uint64_t bar[2];     // staged tiles: completion of each buffer's copy
+  uint32_t uflag;      // uniform splits: attempt decision, then a group outgrew its region
 };
 using SplitSmem = SplitSmemT<kSplitTileBytes>;
 using SplitSmemStaged = SplitSmemT<kSplitStageBytes>;
@@ -1480,8 +1483,9 @@ enum EngineState : uint32_t { ENGINE_HAVE = 0, ENGINE_DONE = 1 };
 // persistent engine's queue (EngineSink, below).
 struct RoundSink {
   const TaskLists& L;
-  __device__ void copy(uint32_t start, uint32_t cnt, uint64_t lo, uint64_t hi, uint32_t src_b, uint32_t* err) const {
-    push_copy(L, start, cnt, lo, hi, src_b, err);
+  __device__ void copy(uint32_t start, uint32_t from, uint32_t cnt, uint64_t lo, uint64_t hi, uint32_t flags,
+                       uint32_t* err) const {
+    push_copy(L, start, from, cnt, lo, hi, flags, err);
   }
   __device__ void local(const SortTask& t, uint32_t* err) const { push(L.local, L.nlocal, L.cap_local, t, err); }
   __device__ void split(const SortTask& t, uint32_t* err) const {
@@ -1545,6 +1549,143 @@ struct SplitTiles {
   }
 };
 
+// Uniform split of a level-1 bucket (records of 8-16 bytes, split rounds
+// with areas).  Its key range [lo, hi] is cut into G = ceil(m / kUniformTarget)
+// groups of equal width -- group g holds the keys whose offset x = key - lo
+// has floor(x G / S) = g, S = hi - lo + 1 -- and each group is scattered
+// into its own region of the bucket's area of scratch B (cap = area / G
+// records, a quarter above the mean), with no histogram pass: the regions
+// need no exact counts.  Keys this suits (the model's widest window and the
+// heavy-key count both zero: the sample saw a smooth distribution, and few
+// earlier attempts in this sort overflowed) fill the groups like a binomial
+// draw, so a region about five standard deviations above its mean size does
+// not fill; if one does, the attempt is void.  Returns 1 when the groups are
+// emitted, 0 to run the exact split instead (not attempted, or a region
+// overflowed), -1 if a staged wait ran out (the CTA must leave).
+constexpr uint32_t kUniformTarget = 1800;  // mean records of a uniform group (local sorts hold 2048)
+
+template <int EW, typename SM, typename Sink>
+__device__ int split_uniform(SM& sm, const HsortParams& p, const SortTask& task, const uint8_t* src, uint8_t* oth,
+                             uint32_t dpos, const Sink& L, uint32_t* stats, uint32_t* err, uint32_t& par) {
+  constexpr uint32_t E = EW * 4;
+  constexpr int SRPT = staged_split_tile<EW>() / kThreads;
+  const uint32_t m = task.count;
+  const uint32_t G = (m + kUniformTarget - 1) / kUniformTarget;
+  const uint32_t cap = (split_area(task.start + m) - split_area(task.start)) / max(G, 1u);
+  const uint32_t w = warp_id(), lane = lane_id();
+  uint64_t* glo = reinterpret_cast<uint64_t*>(sm.hist);  // G + 1 key offsets from lo, group starts
+  if (threadIdx.x == 0) {
+    bool go = p.uniform != nullptr && G >= 2 && G <= (uint32_t)kMaxGroups && task.hi - task.lo >= 16ull * G;
+    if (go) {
+      const uint32_t mean = (m + G - 1) / G;
+      go = *p.gate_widest == 0 && *p.gate_heavy == 0 && cap >= mean + 5 * (uint32_t)sqrtf((float)mean) + 16;
+    }
+    if (go) {
+      const uint32_t tried = *(volatile uint32_t*)&p.uniform[0], failed = *(volatile uint32_t*)&p.uniform[1];
+      go = 8ull * failed <= (uint64_t)tried + 8;
+    }
+    if (go) {
+      atomicAdd(&p.uniform[0], 1u);
+      const unsigned __int128 S = (unsigned __int128)(task.hi - task.lo) + 1;
+      sm.red[0] = (uint64_t)((((unsigned __int128)G) << 64) / S);  // M: floor(x M / 2^64) is g or g - 1
+    }
+    sm.uflag = go ? 1u : 0u;
+  }
+  __syncthreads();
+  if (!sm.uflag) return 0;
+  const uint64_t M = sm.red[0];
+  for (uint32_t g = threadIdx.x; g <= G; g += kThreads) {
+    const unsigned __int128 S = (unsigned __int128)(task.hi - task.lo) + 1;
+    const unsigned __int128 v = ((unsigned __int128)g * S + (G - 1)) / G;  // ceil(g S / G)
+    glo[g] = (v >> 64) ? ~0ull : (uint64_t)v;
+  }
+  const uint32_t g_me = threadIdx.x;
+  if (g_me < G) sm.cursor[g_me] = g_me * cap;
+  __syncthreads();
+  auto group_of = [&](uint64_t key) -> uint32_t {
+    const uint64_t x = key > task.lo ? key - task.lo : 0;
+    const unsigned long long q = __umul64hi(x, M);
+    uint32_t g = q < G ? (uint32_t)q : G - 1;
+    if (g + 1 < G && x >= glo[g + 1]) ++g;
+    return g;
+  };
+  using V = typename std::conditional<E % 16 == 0, uint4,
+                                      typename std::conditional<E % 8 == 0, uint2, uint32_t>::type>::type;
+  constexpr uint32_t VPR = E / sizeof(V);
+  const SplitTiles<EW> tiles{src, m, sm, par};
+  tiles.start();
+  for (uint32_t i = 0; i * tiles.T < m; ++i) {
+    const uint32_t nvalid = min(tiles.T, m - i * tiles.T);
+    const uint8_t* rb = tiles.wait(i, err);  // (a barrier: the last tile's rows are clear)
+    if (!rb) return -1;
+    uint32_t grp[SRPT], rank[SRPT], lead[SRPT];
+#pragma unroll
+    for (int r = 0; r < SRPT; ++r) {
+      const uint32_t e = w * 32 * SRPT + r * 32 + lane;
+      grp[r] = e < nvalid ? group_of(load_key_aligned4(rb + (size_t)e * E, p.key)) : kNoBucket;
+    }
+    warp_ranks<SRPT, kGroupBits>(grp, rank, lead, sm.gcnt);
+    __syncthreads();
+    uint32_t gtot;
+    tile_rank(g_me, 0, sm.gcnt, gtot);
+    const uint32_t goff = block_exclusive_scan<uint32_t>(gtot, sm.scan_tmp, nullptr);
+    sm.goff[g_me] = goff;
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < SRPT; ++r) {
+      if (grp[r] == kNoBucket) continue;
+      uint32_t all;
+      const uint32_t slot = sm.goff[grp[r]] + tile_rank(grp[r], rank[r], sm.gcnt, all);
+      if (slot >= nvalid) {  // impossible with consistent ranks
+        set_error(err, DEV_ERR_COUNT_MISMATCH);
+        continue;
+      }
+      sm.perm[slot] = (uint16_t)(w * 32 * SRPT + r * 32 + lane);
+      sm.sgrp[slot] = (uint16_t)grp[r];
+    }
+    __syncthreads();
+    for (uint32_t f = threadIdx.x; f < nvalid * VPR; f += kThreads) {
+      const uint32_t j = f / VPR, qw = f % VPR;
+      const uint32_t g = sm.sgrp[j] & (kMaxGroups - 1);
+      const uint32_t from = min((uint32_t)sm.perm[j], nvalid - 1);
+      const uint32_t dest = sm.cursor[g] + (j - sm.goff[g]);
+      if (g < G && dest < (g + 1) * cap)
+        reinterpret_cast<V*>(oth + (size_t)dest * E)[qw] = reinterpret_cast<const V*>(rb + (size_t)from * E)[qw];
+      else sm.uflag = 2;  // the group outgrew its region: the attempt is void
+    }
+    __syncthreads();
+    tiles.release(i);
+    if (g_me < G) sm.cursor[g_me] += gtot;
+    clear_rows<SRPT>(grp, lead, sm.gcnt);
+  }
+  __syncthreads();
+  if (sm.uflag != 1) {
+    if (threadIdx.x == 0) atomicAdd(&p.uniform[1], 1u);
+    __syncthreads();
+    return 0;
+  }
+  // each group's records: a task from its region to its place in the output
+  const uint32_t cnt = g_me < G ? sm.cursor[g_me] - g_me * cap : 0;
+  uint32_t total;
+  const uint32_t off = block_exclusive_scan<uint32_t>(cnt, sm.scan_tmp, &total);
+  if (threadIdx.x == 0 && total != m) set_error(err, DEV_ERR_COUNT_MISMATCH);
+  if (cnt) {
+    const uint64_t klo = task.lo + glo[g_me];
+    const uint64_t khi = g_me + 1 < G ? task.lo + glo[g_me + 1] - 1 : task.hi;
+    const uint32_t from = dpos + g_me * cap, start = task.start + off;
+    if (klo == khi || cnt == 1) {
+      L.copy(start, from, cnt, klo, khi, TASK_SRC_B, err);
+    } else if (cnt <= (uint32_t)kLocalMax) {
+      L.local(make_task_at(start, from, cnt, klo, khi, TASK_SRC_B), err);
+    } else {
+      atomicAdd(stats + STAT_PUSHED, 1u);
+      L.split(make_task_at(start, from, cnt, klo, khi, TASK_SRC_B), err);
+    }
+  }
+  __syncthreads();
+  return 1;
+}
+
 // One bucket split.  STAGED: the histogram and scatter passes stream the
 // bucket through shared memory (SplitTiles) instead of loading records
 // into registers; false if a staged wait ran out (the CTA must leave).
@@ -1553,10 +1694,37 @@ __device__ bool split_task(SM& sm, const HsortParams& p, const SortTask& task, c
                            uint32_t* stats, uint32_t* err, uint32_t& par) {
   constexpr uint32_t E = EW * 4;
   constexpr int RPT = Tile<EW>::kRpt, T = Tile<EW>::kSize;
-  const bool in_b = (task.flags & TASK_SRC_B) != 0;
-  const uint8_t* src = (in_b ? p.bufB : p.bufA) + (size_t)task.from * E;
-  uint8_t* oth = (in_b ? p.bufA : p.bufB) + (size_t)task.start * E;
+  const bool in_b = (task.flags & TASK_SRC_B) != 0, in_out = (task.flags & TASK_SRC_OUT) != 0;
+  const uint8_t* src = (in_b ? p.bufB : in_out ? p.out : p.bufA) + (size_t)task.from * E;
+  // where the groups go: by default the other scratch buffer at their final
+  // positions; with areas, a level-1 bucket goes to its area of B, and later
+  // rounds go from B or the output to A and from A to the output
+  uint8_t* dbuf = in_b ? p.bufA : p.bufB;
+  uint32_t dpos = task.start;
+  uint32_t dflags = in_b ? 0u : (uint32_t)TASK_SRC_B;  // where the emitted tasks' records lie
+  const bool areas = STAGED && p.areas != 0;
+  if (areas) {
+    if (task.flags & TASK_L1) {
+      dbuf = p.bufB;
+      dpos = split_area(task.start);
+      dflags = TASK_SRC_B;
+    } else if (in_b || in_out) {
+      dbuf = p.bufA;
+      dflags = 0;
+    } else {
+      dbuf = p.out;
+      dflags = TASK_SRC_OUT;
+    }
+  }
+  uint8_t* oth = dbuf + (size_t)dpos * E;
   const uint32_t m = task.count;
+  if constexpr (STAGED) {
+    if (areas && (task.flags & TASK_L1)) {
+      const int u = split_uniform<EW>(sm, p, task, src, oth, dpos, L, stats, err, par);
+      if (u < 0) return false;
+      if (u > 0) return true;
+    }
+  }
   int bits = bitlen64(task.hi - task.lo);
   int shift = bits > kSplitBits ? bits - kSplitBits : 0;
   uint32_t nbins = (uint32_t)((task.hi - task.lo) >> shift) + 1;
@@ -1888,14 +2056,13 @@ __device__ bool split_task(SM& sm, const HsortParams& p, const SortTask& task, c
       const uint64_t glo = refined ? fine_bin_lo(sm.hist, b0, blo, shift, nbins) : blo + ((uint64_t)b0 << shift);
       const uint64_t ghi = b1 >= sm.gfirst[kMaxGroups] ? bhi  // (the number of bins there)
                            : (refined ? fine_bin_lo(sm.hist, b1, blo, shift, nbins) : blo + ((uint64_t)b1 << shift)) - 1;
-      const uint32_t nsrc = in_b ? 0u : 1u;
       if (glo == ghi || s == 1) {
-        L.copy(task.start + g0, s, glo, ghi, nsrc, err);
+        L.copy(task.start + g0, dpos + g0, s, glo, ghi, dflags, err);
       } else if (s <= (uint32_t)kLocalMax) {
-        L.local(make_task(task.start + g0, s, glo, ghi, nsrc != 0, false), err);
+        L.local(make_task_at(task.start + g0, dpos + g0, s, glo, ghi, dflags), err);
       } else {
         atomicAdd(stats + STAT_PUSHED, 1u);
-        L.split(make_task(task.start + g0, s, glo, ghi, nsrc != 0, false), err);
+        L.split(make_task_at(task.start + g0, dpos + g0, s, glo, ghi, dflags), err);
       }
     }
     __syncthreads();
@@ -1938,13 +2105,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_split(HsortParams p, TaskLists 
       // out now (later rounds write scratch A at final positions, which may
       // cover a region); a copy piece is final, a small bucket becomes a
       // local task in scratch B
+      // (with areas, a small bucket goes to its area of B)
       constexpr uint32_t E = EW * 4;
       const bool copy = (task.flags & TASK_COPY) != 0;
-      block_copy_ilp<EW>(p.bufA + (size_t)task.from * E, (copy ? p.out : p.bufB) + (size_t)task.start * E,
+      const uint32_t to = split_staged<EW>() && p.areas ? split_area(task.start) : task.start;
+      block_copy_ilp<EW>(p.bufA + (size_t)task.from * E, copy ? p.out + (size_t)task.start * E : p.bufB + (size_t)to * E,
                          task.count, kThreads);
       if (!copy && threadIdx.x == 0) {
         __threadfence();
-        push(L.local, L.nlocal, L.cap_local, make_task(task.start, task.count, task.lo, task.hi, true, false), err);
+        push(L.local, L.nlocal, L.cap_local, make_task_at(task.start, to, task.count, task.lo, task.hi, TASK_SRC_B),
+             err);
       }
       __syncthreads();
       continue;
@@ -1994,14 +2164,15 @@ __global__ void __launch_bounds__(NT, local_ctas_per_sm<EW>()) k_local(HsortPara
         const uint32_t from = __shfl_sync(GB_FULL_MASK, nxt.from, 0);
         const uint32_t cnt = __shfl_sync(GB_FULL_MASK, nxt.count, 0);
         const uint32_t flags = __shfl_sync(GB_FULL_MASK, nxt.flags, 0);
-        const uint8_t* ns = ((flags & TASK_SRC_B) ? p.bufB : p.bufA) + (size_t)from * E;
+        const uint8_t* ns = ((flags & TASK_SRC_B) ? p.bufB : (flags & TASK_SRC_OUT) ? p.out : p.bufA) + (size_t)from * E;
         const uint8_t* ne = ns + (size_t)cnt * E;
         for (const uint8_t* q = (const uint8_t*)((uintptr_t)ns & ~(uintptr_t)127) + 128 * lane; q < ne;
              q += 128 * 32)
           asm volatile("prefetch.global.L2 [%0];" ::"l"(q));
       }
     }
-    const uint8_t* src = ((task.flags & TASK_SRC_B) ? p.bufB : p.bufA) + (size_t)task.from * E;
+    const uint8_t* src =
+        ((task.flags & TASK_SRC_B) ? p.bufB : (task.flags & TASK_SRC_OUT) ? p.out : p.bufA) + (size_t)task.from * E;
     uint8_t* out = p.out + (size_t)task.start * E;
     if ((task.flags & TASK_COPY) || task.count == 1) {
       block_copy_ilp<EW>(src, out, task.count, NT);
@@ -2039,7 +2210,9 @@ __global__ void __launch_bounds__(NT, 2) k_local_staged(HsortParams p, const Sor
   uint32_t* err = stats + STAT_SLOTS;
   const uint32_t nt = min(*ntasks, cap);
   auto staged = [](const SortTask& t) { return !(t.flags & TASK_COPY) && t.count > 1 && t.count <= (uint32_t)kLocalMax; };
-  auto source = [&](const SortTask& t) { return ((t.flags & TASK_SRC_B) ? p.bufB : p.bufA) + (size_t)t.from * E; };
+  auto source = [&](const SortTask& t) {
+    return ((t.flags & TASK_SRC_B) ? p.bufB : (t.flags & TASK_SRC_OUT) ? p.out : p.bufA) + (size_t)t.from * E;
+  };
   // the task's byte range rounded out to 16 bytes (the slack lies inside
   // the scratch allocations) into buffer `slot`
   auto issue = [&](const SortTask& t, int slot) {
@@ -2186,7 +2359,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_engine(HsortParams p, EngineQue
   EngineCtl& c = *reinterpret_cast<EngineCtl*>(smem_raw + engine_ctl_offset<EW>());
   uint32_t* err = stats + STAT_SLOTS;
   const EngineSink sink{q};
-  auto source = [&](const SortTask& t) { return ((t.flags & TASK_SRC_B) ? p.bufB : p.bufA) + (size_t)t.from * E; };
+  auto source = [&](const SortTask& t) {
+    return ((t.flags & TASK_SRC_B) ? p.bufB : (t.flags & TASK_SRC_OUT) ? p.out : p.bufA) + (size_t)t.from * E;
+  };
   auto issue = [&](const SortTask& t, uint32_t slot) {  // thread 0
     const uintptr_t a = (uintptr_t)source(t);
     const uintptr_t a0 = a & ~(uintptr_t)15;
@@ -2534,13 +2709,12 @@ __global__ void k_build_region_tasks(const uint32_t* __restrict__ region, const 
   const uint64_t hi = b == nbuckets - 1 ? ~0ull : S[b] - 1;
   if (lo == hi || cnt == 1) {  // copy pieces, each moved by one CTA of the first split round
     for (uint32_t s0 = 0; s0 < cnt; s0 += kCopyPiece) {
-      SortTask t = make_task(out_start[b] + s0, min(kCopyPiece, cnt - s0), lo, hi, false, true);
-      t.from = region[b] + s0;
+      SortTask t = make_task_at(out_start[b] + s0, region[b] + s0, min(kCopyPiece, cnt - s0), lo, hi,
+                                TASK_COPY | TASK_L1);
       push(L.split_out, L.nsplit_out, L.cap_split, t, err);
     }
   } else {
-    SortTask t = make_task(out_start[b], cnt, lo, hi, false, false);
-    t.from = region[b];
+    SortTask t = make_task_at(out_start[b], region[b], cnt, lo, hi, TASK_L1);
     push(L.split_out, L.nsplit_out, L.cap_split, t, err);
   }
 }

@@ -123,12 +123,20 @@ struct SortTask {        // one bucket or sub-bucket of the level-2 task engine
   uint32_t flags;        // TASK_* below
 };
 enum TaskFlags : uint32_t {
-  TASK_SRC_B = 1,  // the records are in scratch B (else scratch A)
-  TASK_COPY = 2,   // one key: copied, not sorted
+  TASK_SRC_B = 1,    // the records are in scratch B (else scratch A)
+  TASK_COPY = 2,     // one key: copied, not sorted
+  TASK_SRC_OUT = 4,  // the records are in the output buffer, at their final positions
+  TASK_L1 = 8,       // a level-1 bucket (round 0 of the split rounds)
 };
 __host__ __device__ inline SortTask make_task(uint32_t start, uint32_t count, uint64_t lo, uint64_t hi, bool in_b,
                                               bool copy) {
   return SortTask{start, count, lo, hi, start, (in_b ? (uint32_t)TASK_SRC_B : 0u) | (copy ? (uint32_t)TASK_COPY : 0u)};
+}
+// A task whose records lie at `from` of the buffer `flags` names, bound for
+// `start` of the next buffer (or the output).
+__host__ __device__ inline SortTask make_task_at(uint32_t start, uint32_t from, uint32_t count, uint64_t lo,
+                                                 uint64_t hi, uint32_t flags) {
+  return SortTask{start, count, lo, hi, from, flags};
 }
 
 // Keys heavy enough to own a single-key level-1 bucket worth three
@@ -163,7 +171,27 @@ struct HsortParams {
   uint32_t a_cap;      // records scratch A holds (n, or more for reserved bucket regions)
   uint32_t chunks;     // count chunks of the input (0: hsort_grid(n))
   const HeavyTable* heavy;  // heavy keys of the level-1 splitters (null: none)
+  // Uniform splits (records of 8-16 bytes, split rounds): a level-1 bucket
+  // may be cut into equal key ranges and scattered into regions of scratch B
+  // sized for them, without the histogram pass.  uniform: device words
+  // [tried, failed] (null: never); gate_words: the model's widest window and
+  // the heavy-key count, both zero for keys this suits.
+  uint32_t* uniform;
+  const uint32_t* gate_widest;
+  const uint32_t* gate_heavy;
+  // 1: the split rounds of records of 8-16 bytes give each level-1 bucket an
+  // area of scratch B (split_area) and ping-pong later rounds through A and
+  // the output; scratch B then holds split_area(n) records
+  uint32_t areas;
 };
+
+// Scratch B position of a level-1 bucket's area in the split rounds of
+// records of 8-16 bytes: bucket [start, start + m) owns B records
+// [split_area(start), split_area(start + m)), a quarter more than it holds,
+// so a split may give each group a region with room to spare.
+__host__ __device__ inline uint32_t split_area(uint32_t start) { return (uint32_t)((uint64_t)start + (start >> 2)); }
+// Largest n whose areas fit 32-bit record offsets.
+constexpr uint32_t kSplitAreaMaxN = 3435973836u;  // 0.8 * 2^32
 
 bool hsort_supported(uint32_t elsize);
 int hsort_grid(uint32_t n);

@@ -782,6 +782,36 @@ def test_host_sort_pipelined_4096_buckets(mp, regions, monkeypatch):
     assert hout.tobytes() == O.numpy_sorted(a, 'key').tobytes()
 
 
+@pytest.mark.parametrize("kind,method", [("uniform", "learned"), ("uniform", "plain"), ("intervals", "plain")])
+def test_uniform_bucket_splits(mp, kind, method):
+    """Level-1 buckets of 8-16 byte records whose keys spread evenly are cut
+    into equal key ranges and scattered into regions of their scratch area
+    without a histogram pass (uniform_splits); keys that bunch inside their
+    buckets (here short intervals 2^51 apart, four or five to a bucket)
+    overflow a group's region, and the bucket is split by its histogram
+    instead (uniform_fallbacks), until the failures stop further attempts.
+    Every key appears twice, so the stable order is checked too."""
+    rng = numpy.random.default_rng(61)
+    dt = numpy.dtype([('key', 'u8'), ('val', 'i8')])
+    n = 8_000_000
+    a = numpy.empty(n, dtype=dt)
+    if kind == "uniform":
+        a['key'] = rng.integers(0, 2**64, n, dtype=numpy.uint64, endpoint=False)
+    else:
+        k = rng.integers(0, 2**13, n, dtype=numpy.uint64)
+        a['key'] = (k << numpy.uint64(51)) + rng.integers(0, 2**40, n, dtype=numpy.uint64)
+    a['key'][1::2] = a['key'][0::2]
+    a['val'] = numpy.arange(n)
+    out = numpy.empty_like(a)
+    mp.sort(a, 'key', out=out, method=method)
+    st = mp.last_stats()
+    assert out.tobytes() == O.numpy_sorted(a, 'key').tobytes()
+    if kind == "uniform":
+        assert st["uniform_splits"] > 1000 and st["uniform_fallbacks"] == 0, st
+    else:
+        assert st["uniform_fallbacks"] > 0, st
+
+
 # ----------------------------------------------- bounded look-back wait --
 def test_lookback_wait_runs_out_and_reports(mp):
     """One LSD pass in which a tile never publishes its counts: the next
