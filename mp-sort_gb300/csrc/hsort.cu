@@ -1578,6 +1578,8 @@ __device__ int split_uniform(SM& sm, const HsortParams& p, const SortTask& task,
     bool go = p.uniform != nullptr && G >= 2 && G <= (uint32_t)kMaxGroups && task.hi - task.lo >= 16ull * G;
     if (go) {
       const uint32_t mean = (m + G - 1) / G;
+      // (without these gates, Zipf keys void 298 attempts before the failure
+      // count stops them: split 11.8 -> 13.1 ms)
       go = *p.gate_widest == 0 && *p.gate_heavy == 0 && cap >= mean + 5 * (uint32_t)sqrtf((float)mean) + 16;
     }
     if (go) {
