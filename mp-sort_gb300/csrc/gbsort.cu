@@ -691,6 +691,7 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
   p.a_cap = a_cap;
   p.chunks = (uint32_t)G;
   p.areas = areas ? 1u : 0u;
+  p.bkt = c.B.as<uint16_t>();  // scratch B is free during level 1
   static const bool uniform_off = getenv("GBSORT_UNIFORM_SPLITS") && atoi(getenv("GBSORT_UNIFORM_SPLITS")) == 0;
   p.uniform = areas && !uniform_off ? counters + CNT_UNIFORM : nullptr;
   p.gate_widest = counters + CNT_WIDEST;
@@ -761,17 +762,11 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
   }
   if (timing) GB_CUDA(cudaEventRecord(c.ev[1], st));
   const ModelDev* mp = lookup == LOOKUP_LEARNED ? &model : nullptr;
-  // the level-1 scatter: a learned sort enqueues it with the learned lookup
-  // and with the plain one, gated on the model's widest window -- wide
-  // windows (steep steps of heavy keys inside leaves) make the window search
-  // cost more than a binary search over splitters in shared memory -- and
-  // exactly one of the two does the work
+  // the level-1 scatter: each record to the bucket the count wrote for it
   auto scatter = [&](int c0, int c1, const uint32_t* skip) -> cudaError_t {
-    if (lookup != LOOKUP_LEARNED) return l1_scatter(p, lookup, S, nb, mp, counts, stats, st, c0, c1, skip);
-    cudaError_t e = l1_scatter(p, LOOKUP_LEARNED, S, nb, mp, counts, stats, st, c0, c1, skip, widest, 0);
-    if (e != cudaSuccess) return e;
-    return l1_scatter(p, LOOKUP_PLAIN, S, nb, nullptr, counts, stats, st, c0, c1, skip, widest, 1);
+    return l1_scatter(p, nb, counts, stats, st, c0, c1, skip);
   };
+
   // pipelined: each piece is counted and scattered into the reserved bucket
   // regions as soon as it has landed; if a bucket outgrows its region the
   // scatters stop and level 1 is redone exactly from the complete input

@@ -322,6 +322,7 @@ __device__ __forceinline__ uint32_t lookup(const LookupSmem& L, const ModelDev& 
 template <int LK>
 __device__ __forceinline__ uint8_t* load_lookup(uint8_t* smem, const uint64_t* S, int nbuckets,
                                                 const ModelDev& m, LookupSmem& L) {
+  if constexpr (LK == LOOKUP_IDS) return smem;  // the ids come with the records
   if constexpr (LK == LOOKUP_PLAIN) {
     L.S = reinterpret_cast<uint64_t*>(smem);
     for (int i = threadIdx.x; i < nbuckets - 1; i += blockDim.x) L.S[i] = S[i];
@@ -343,6 +344,7 @@ __device__ __forceinline__ uint8_t* load_lookup(uint8_t* smem, const uint64_t* S
 
 template <int LK>
 size_t lookup_smem_bytes(int nbuckets, const ModelDev* m) {
+  if (LK == LOOKUP_IDS) return 0;
   if (LK == LOOKUP_LEARNED) return 12 * ((size_t)1 << m->lbits);
   return 8 * (size_t)((nbuckets + 1) & ~1);
 }
@@ -374,11 +376,20 @@ __device__ __forceinline__ void count_range(const HsortParams& p, const LookupSm
       uint32_t i = base + u * kThreads + threadIdx.x;
       const bool v = i < ce;
       if constexpr (!HEAVY) {
-        if (v) atomicAdd(&hist[lookup<LK>(L, model, nbuckets, k[u], stats + STAT_WINDOW_MISS)], 1u);
+        if (v) {
+          const uint32_t b = lookup<LK>(L, model, nbuckets, k[u], stats + STAT_WINDOW_MISS);
+          atomicAdd(&hist[b], 1u);
+          if (p.bkt) p.bkt[i] = (uint16_t)b;
+        }
         continue;
       }
       uint32_t hw = v ? heavy_lookup(p.heavy, hprobes, k[u]) : 0;
-      if (v && !hw) atomicAdd(&hist[lookup<LK>(L, model, nbuckets, k[u], stats + STAT_WINDOW_MISS)], 1u);
+      uint32_t b = hw & kHeavyBucketMask;
+      if (v && !hw) {
+        b = lookup<LK>(L, model, nbuckets, k[u], stats + STAT_WINDOW_MISS);
+        atomicAdd(&hist[b], 1u);
+      }
+      if (v && p.bkt) p.bkt[i] = (uint16_t)b;
       // records of heavy keys: one match over the warp groups them, one
       // atomic per distinct key (many lanes adding to one counter
       // serialise; Zipf keys at 1e9 x 16 B: count 10.0 -> 8.7 ms against
@@ -580,9 +591,28 @@ __global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortP
   uint32_t* wdest = reinterpret_cast<uint32_t*>(q);
   if (!kCombine) q += 4 * (size_t)T;
   uint8_t* cnt = q;  // [nbuckets][kWarps]
+  q += (size_t)nbuckets * kWarps;
+  // LOOKUP_IDS: the bucket ids of the next two tiles come into shared memory
+  // by bulk asynchronous copies (no registers held for them)
+  uint16_t* idbuf = reinterpret_cast<uint16_t*>(q);  // [2][kIdBuf]
+  constexpr uint32_t kIdBuf = (T * 2 + 32 + 15) / 16 * 8;
+  uint64_t* ibar = reinterpret_cast<uint64_t*>(q + (LK == LOOKUP_IDS ? 4 * (size_t)kIdBuf : 0));
   for (int i = threadIdx.x; i < nbuckets * kWarps / 16; i += kThreads)
     reinterpret_cast<uint4*>(cnt)[i] = make_uint4(0, 0, 0, 0);
   const uint32_t hprobes = p.heavy ? p.heavy->probes : 0;
+  uint32_t ipar = 0;  // next completion parity of each id buffer
+  if constexpr (LK == LOOKUP_IDS) {
+    if (threadIdx.x == 0) {
+      mbar_init(&ibar[0], 1);
+      mbar_init(&ibar[1], 1);
+      mbar_init_fence();
+    }
+  }
+  // ids of the tile starting at record t (chunk end ce) into buffer b
+  auto issue_ids = [&](uint32_t t, uint32_t ce_, int b) {
+    const uint32_t cnt_ = min((uint32_t)T, ce_ - t);
+    bulk_load(idbuf + (size_t)b * kIdBuf, p.bkt + t, (cnt_ * 2 + 15) & ~15u, &ibar[b]);
+  };
 
   const uint32_t w = warp_id(), lane = lane_id();
   // the count kernel's chunks, several per CTA
@@ -596,6 +626,13 @@ __global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortP
   }
   __syncthreads();
 
+  if constexpr (LK == LOOKUP_IDS) {
+    if (threadIdx.x == 0) {  // (the barrier above ended every read of both buffers)
+      fence_proxy_async_smem();
+      if (cb < ce) issue_ids(cb, ce, 0);
+      if (cb + T < ce) issue_ids(cb + T, ce, 1);
+    }
+  }
   // the next tile's records are loaded while the current tile is ranked
   uint32_t nxt[kPre ? RPT : 1][EW];
   if constexpr (kPre) {
@@ -605,7 +642,13 @@ __global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortP
       if (cb + e < ce) RecIO<EW>::load_stream(p.in + (size_t)(cb + e) * E, nxt[r]);
     }
   }
-  for (uint32_t t0 = cb; t0 < ce; t0 += T) {
+  for (uint32_t t0 = cb, tk = 0; t0 < ce; t0 += T, ++tk) {
+    const int ib = (int)(tk & 1);
+    bool id_ok = true;
+    if constexpr (LK == LOOKUP_IDS) {
+      id_ok = mbar_wait_bounded(&ibar[ib], (ipar >> ib) & 1u, kBulkWaitPolls);
+      ipar ^= 1u << ib;
+    }
     const uint32_t nvalid = min((uint32_t)T, ce - t0);
     if (threadIdx.x == 0 && t0 + 2 * T < ce)
       prefetch_l2_range(p.in + (size_t)(t0 + 2 * T) * E, min((uint32_t)T, ce - t0 - 2 * T) * E);
@@ -613,30 +656,50 @@ __global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortP
     uint32_t bkt[RPT], rank[RPT];
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
+      const uint32_t et = w * 32 * RPT + r * 32 + lane;  // in the tile
+      bkt[r] = kNoBucket;
+      if constexpr (LK == LOOKUP_IDS) {
+        if (et < nvalid) bkt[r] = min((uint32_t)idbuf[(size_t)ib * kIdBuf + et], (uint32_t)nbuckets - 1);
+      }
       if constexpr (kPre) {
 #pragma unroll
         for (int q2 = 0; q2 < EW; ++q2) rec[r][q2] = nxt[r][q2];
-        uint32_t e = t0 + T + w * 32 * RPT + r * 32 + lane;
+        uint32_t e = t0 + T + et;
         if (e < ce) RecIO<EW>::load_stream(p.in + (size_t)e * E, nxt[r]);
       } else {
-        uint32_t e = t0 + w * 32 * RPT + r * 32 + lane;
+        uint32_t e = t0 + et;
         if (e < ce) RecIO<EW>::load_stream(p.in + (size_t)e * E, rec[r]);
       }
     }
+    if constexpr (LK != LOOKUP_IDS) {
 #pragma unroll
-    for (int r = 0; r < RPT; ++r) {
-      uint32_t e = w * 32 * RPT + r * 32 + lane;
-      bkt[r] = kNoBucket;
-      if (e < nvalid) {
-        uint64_t k = key_from_regs<EW>(rec[r], p.key);
-        const uint32_t hb = hprobes ? heavy_bucket(p.heavy, hprobes, k) : kNoHeavy;
-        bkt[r] = hb != kNoHeavy ? hb : lookup<LK>(L, model, nbuckets, k, stats + STAT_WINDOW_MISS);
+      for (int r = 0; r < RPT; ++r) {
+        uint32_t e = w * 32 * RPT + r * 32 + lane;
+        if (e < nvalid) {
+          uint64_t k = key_from_regs<EW>(rec[r], p.key);
+          const uint32_t hb = hprobes ? heavy_bucket(p.heavy, hprobes, k) : kNoHeavy;
+          bkt[r] = hb != kNoHeavy ? hb : lookup<LK>(L, model, nbuckets, k, stats + STAT_WINDOW_MISS);
+        }
       }
     }
-    // 1. ranks within the warp, in (r, lane) order
+    // 1. ranks within the warp, in (r, lane) order (a wait for ids that ran
+    // out leaves in-range ids behind: the CTA stops at the barrier)
     uint32_t lead[RPT];
     warp_ranks<RPT, kMaxBucketBits>(bkt, rank, lead, cnt);
-    __syncthreads();
+    if (!__syncthreads_and(id_ok)) {
+      if constexpr (LK == LOOKUP_IDS) {
+        if (threadIdx.x == 0) set_error(err, DEV_ERR_TIMEOUT);
+        mbar_wait_bounded(&ibar[ib], ((ipar >> ib) & 1u) ^ 1u, kBulkWaitPolls);  // (the parity flipped above)
+        if (t0 + T < ce) mbar_wait_bounded(&ibar[ib ^ 1], (ipar >> (ib ^ 1)) & 1u, kBulkWaitPolls);
+      }
+      return;
+    }
+    if constexpr (LK == LOOKUP_IDS) {  // every thread has read this tile's ids: the buffer takes tile + 2
+      if (threadIdx.x == 0 && t0 + 2 * T < ce) {
+        fence_proxy_async_smem();
+        issue_ids(t0 + 2 * T, ce, ib);
+      }
+    }
     // 2. rank in the tile = counts of the earlier warps + rank in the warp
     uint32_t tot[RPT], hold[RPT];
 #pragma unroll
@@ -711,7 +774,8 @@ size_t l1_scatter_smem(int nbuckets, const ModelDev* m) {
   const size_t words = 4 * (size_t)((nbuckets + 3) & ~3);
   const size_t combine = EW == 4 ? words + 16 * (size_t)nbuckets : 0;
   const size_t stage = EW == 4 ? 0 : (size_t)ScatterTile<EW>::kSize * (EW * 4 + 4);
-  return lookup_smem_bytes<LK>(nbuckets, m) + words + combine + stage + (size_t)nbuckets * kWarps;
+  const size_t ids = LK == LOOKUP_IDS ? 4 * (size_t)((ScatterTile<EW>::kSize * 2 + 32 + 15) / 16 * 8) + 16 : 0;
+  return lookup_smem_bytes<LK>(nbuckets, m) + words + combine + stage + (size_t)nbuckets * kWarps + ids;
 }
 
 // ------------------------------------------------------------- tasks -----
@@ -2603,11 +2667,10 @@ uint32_t hsort_chunk_begin(uint32_t n, int c, int chunks) {
   return c >= chunks ? n : chunk_begin(n, (uint32_t)c, (uint32_t)chunks);
 }
 
-cudaError_t l1_scatter(const HsortParams& p, int lookup_kind, const uint64_t* splitters, int nbuckets,
-                       const void* model, const uint32_t* offsets, uint32_t* stats, cudaStream_t stream, int c0,
-                       int c1, const uint32_t* skip_if, const uint32_t* gate, int gate_wide) {
+cudaError_t l1_scatter(const HsortParams& p, int nbuckets, const uint32_t* offsets, uint32_t* stats,
+                       cudaStream_t stream, int c0, int c1, const uint32_t* skip_if) {
   if (nbuckets < 1 || nbuckets > (1 << kMaxBucketBits)) return cudaErrorInvalidValue;  // ids rank in 12 bits
-  const ModelDev m = model ? *(const ModelDev*)model : ModelDev{};
+  if (!p.bkt) return cudaErrorInvalidValue;  // the count writes the bucket ids the scatter reads
   const int g = p.chunks ? (int)p.chunks : hsort_grid(p.n);
   if (c1 < 0) c1 = g;
   if (c1 <= c0) return cudaSuccess;
@@ -2615,23 +2678,13 @@ cudaError_t l1_scatter(const HsortParams& p, int lookup_kind, const uint64_t* sp
   cudaError_t e = cudaSuccess;
   bool ok = dispatch_ew(p.elsize, [&](auto ewc) {
     constexpr int EW = decltype(ewc)::value;
-    if (lookup_kind == LOOKUP_LEARNED) {
-      size_t sm = l1_scatter_smem<EW, LOOKUP_LEARNED>(nbuckets, &m);
-      e = set_smem((const void*)k_l1_scatter<EW, LOOKUP_LEARNED>, sm);
-      if (e == cudaSuccess)
-        k_l1_scatter<EW, LOOKUP_LEARNED><<<ctas, kThreads, sm, stream>>>(p, splitters, nbuckets, m, offsets, g,
-                                                                                  stats, (uint32_t)c0, (uint32_t)c1,
-                                                                                  skip_if, gate, gate_wide);
-      note_launches(1);
-    } else {
-      size_t sm = l1_scatter_smem<EW, LOOKUP_PLAIN>(nbuckets, &m);
-      e = set_smem((const void*)k_l1_scatter<EW, LOOKUP_PLAIN>, sm);
-      if (e == cudaSuccess)
-        k_l1_scatter<EW, LOOKUP_PLAIN><<<ctas, kThreads, sm, stream>>>(p, splitters, nbuckets, m, offsets, g,
-                                                                                stats, (uint32_t)c0, (uint32_t)c1,
-                                                                                skip_if, gate, gate_wide);
-      note_launches(1);
-    }
+    const ModelDev m{};
+    size_t sm = l1_scatter_smem<EW, LOOKUP_IDS>(nbuckets, &m);
+    e = set_smem((const void*)k_l1_scatter<EW, LOOKUP_IDS>, sm);
+    if (e == cudaSuccess)
+      k_l1_scatter<EW, LOOKUP_IDS><<<ctas, kThreads, sm, stream>>>(p, nullptr, nbuckets, m, offsets, g, stats,
+                                                                    (uint32_t)c0, (uint32_t)c1, skip_if, nullptr, 0);
+    note_launches(1);
   });
   if (!ok) return cudaErrorInvalidValue;
   if (e != cudaSuccess) return e;

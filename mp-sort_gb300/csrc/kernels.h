@@ -112,7 +112,8 @@ enum StatSlot : int {
   STAT_SLOTS = 8
 };
 
-enum Lookup : int { LOOKUP_PLAIN = 0, LOOKUP_LEARNED = 1 };
+// LOOKUP_IDS: the level-1 scatter reads the bucket ids the count wrote (HsortParams::bkt).
+enum Lookup : int { LOOKUP_PLAIN = 0, LOOKUP_LEARNED = 1, LOOKUP_IDS = 2 };
 
 struct SortTask {        // one bucket or sub-bucket of the level-2 task engine
   uint32_t start;        // first record in the destination buffers (the other scratch buffer, the output)
@@ -171,6 +172,9 @@ struct HsortParams {
   uint32_t a_cap;      // records scratch A holds (n, or more for reserved bucket regions)
   uint32_t chunks;     // count chunks of the input (0: hsort_grid(n))
   const HeavyTable* heavy;  // heavy keys of the level-1 splitters (null: none)
+  // level-1 bucket of every record: written by the count, read by the
+  // scatter (n entries; the scatter's scratch B is free during level 1)
+  uint16_t* bkt;
   // Uniform splits (records of 8-16 bytes, split rounds): a level-1 bucket
   // may be cut into equal key ranges and scattered into regions of scratch B
   // sized for them, without the histogram pass.  uniform: device words
@@ -229,14 +233,11 @@ cudaError_t bucket_caps(const uint64_t* sorted_sample, uint32_t s, const uint64_
 // + 1 and overflow[1], [2] its capacity and count.
 cudaError_t region_offsets(uint32_t* counts, int chunks, int nbuckets, const uint32_t* region, const uint32_t* cap,
                            uint32_t* total, int c0, int c1, uint32_t* overflow, cudaStream_t stream);
-// Scatter of chunks [c0, c1) (c1 < 0: all) to offsets[bucket][chunk]; does
-// nothing if *skip_if is set (a region overflow), nor, with a gate, unless
-// (*gate > kWideWindow) equals gate_wide (a learned sort launches the learned
-// and the plain lookup so gated on its widest window, and one of them runs).
-cudaError_t l1_scatter(const HsortParams& p, int lookup, const uint64_t* splitters, int nbuckets,
-                       const void* model, const uint32_t* offsets, uint32_t* stats, cudaStream_t stream,
-                       int c0 = 0, int c1 = -1, const uint32_t* skip_if = nullptr, const uint32_t* gate = nullptr,
-                       int gate_wide = 0);
+// Scatter of chunks [c0, c1) (c1 < 0: all) to offsets[bucket][chunk], each
+// record to the bucket l1_count wrote for it in p.bkt; does nothing if
+// *skip_if is set (a region overflow).
+cudaError_t l1_scatter(const HsortParams& p, int nbuckets, const uint32_t* offsets, uint32_t* stats,
+                       cudaStream_t stream, int c0 = 0, int c1 = -1, const uint32_t* skip_if = nullptr);
 // Level-2 task lists (device memory).  A split round consumes split_in and
 // appends to split_out and local; build_tasks appends to split_out and local.
 struct TaskListsHost {

@@ -169,6 +169,7 @@ extern "C" GBSORT_API int gbsort_sort_device_noalloc(const void* d_in, void* d_o
   p.elsize = E;
   p.key = key->word[0];
   p.a_cap = n;
+  p.bkt = reinterpret_cast<uint16_t*>(B);  // level-1 bucket ids (B is free until level 2)
 
   if (nb > 1) {
     NA_CUDA(sample_keys(p.in, n, E, p.key, s_eff, sA, st));
@@ -188,7 +189,7 @@ extern "C" GBSORT_API int gbsort_sort_device_noalloc(const void* d_in, void* d_o
   }
   NA_CUDA(l1_count(p, LOOKUP_PLAIN, S, nb, nullptr, counts, stats, st));
   NA_CUDA(exclusive_scan_u32(counts, counts, (size_t)nb * grid, scan_tmp, st));
-  NA_CUDA(l1_scatter(p, LOOKUP_PLAIN, S, nb, nullptr, counts, stats, st));
+  NA_CUDA(l1_scatter(p, nb, counts, stats, st));
   SortTask* lists[2] = {split0, split1};
   {
     TaskListsHost L{lists[1], nsplit + 1, lists[0], nsplit, local, nlocal, cap_split, cap_local};
