@@ -36,11 +36,6 @@ struct ModelDev {
   const CdfShape* shape;  // if set, kmin and lshift come from this device copy
 };
 
-// Above this widest window (buckets) a window search reads more splitters
-// from L1 than a binary search reads from shared memory (heavy keys make
-// steep steps inside leaves), so the level-1 scatter of a learned sort then
-// runs with the plain search (the choice is made on the device).
-constexpr uint32_t kWideWindow = 16;
 
 // kmin / lshift from the device copy of the shape, when there is one.
 __device__ __forceinline__ CdfShape resolve_shape(CdfShape sh) {

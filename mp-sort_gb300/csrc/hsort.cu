@@ -287,18 +287,6 @@ __device__ __forceinline__ uint32_t heavy_lookup(const HeavyTable* t, uint32_t p
   }
   return 0;
 }
-// The bucket of `key` if the table holds it, else kNoHeavy.
-constexpr uint32_t kNoHeavy = 0xffffffffu;
-__device__ __forceinline__ uint32_t heavy_bucket(const HeavyTable* t, uint32_t probes, uint64_t key) {
-  const uint32_t h = heavy_hash(key);
-  for (uint32_t j = 0; j < probes; ++j) {
-    const uint4 s = __ldg(reinterpret_cast<const uint4*>(&t->slot[(h + j) & (kHeavySlots - 1)]));
-    if (s.z == 0) break;
-    if ((((uint64_t)s.y << 32) | s.x) == key) return s.z - 1;
-  }
-  return kNoHeavy;
-}
-
 // ---------------------------------------------------------- lookups ------
 struct LookupSmem {
   uint64_t* S;
@@ -322,7 +310,6 @@ __device__ __forceinline__ uint32_t lookup(const LookupSmem& L, const ModelDev& 
 template <int LK>
 __device__ __forceinline__ uint8_t* load_lookup(uint8_t* smem, const uint64_t* S, int nbuckets,
                                                 const ModelDev& m, LookupSmem& L) {
-  if constexpr (LK == LOOKUP_IDS) return smem;  // the ids come with the records
   if constexpr (LK == LOOKUP_PLAIN) {
     L.S = reinterpret_cast<uint64_t*>(smem);
     for (int i = threadIdx.x; i < nbuckets - 1; i += blockDim.x) L.S[i] = S[i];
@@ -344,7 +331,6 @@ __device__ __forceinline__ uint8_t* load_lookup(uint8_t* smem, const uint64_t* S
 
 template <int LK>
 size_t lookup_smem_bytes(int nbuckets, const ModelDev* m) {
-  if (LK == LOOKUP_IDS) return 0;
   if (LK == LOOKUP_LEARNED) return 12 * ((size_t)1 << m->lbits);
   return 8 * (size_t)((nbuckets + 1) & ~1);
 }
@@ -529,6 +515,13 @@ struct ScatterTile {
   static constexpr bool kPrefetch = GB_SCATTER_PREFETCH != 0;
 };
 
+// u16 entries of one bucket-id buffer of the scatter: a tile's ids plus the
+// 16-byte rounding of a bulk copy.
+template <int EW>
+__host__ __device__ constexpr uint32_t scatter_id_buf() {
+  return (ScatterTile<EW>::kSize * 2 + 32 + 15) / 16 * 8;
+}
+
 // One 32-byte store (a whole DRAM sector, one memory request; two 16-byte
 // stores to scattered places cost a request each).  p is 32-byte aligned.
 __device__ __forceinline__ void store_sector(uint8_t* p, const uint4& a, const uint4& b) {
@@ -555,19 +548,13 @@ __device__ __forceinline__ void store_sector(uint8_t* p, const uint4& a, const u
 // destination starts a sector is held in shared memory (one slot per
 // bucket) and written together with its partner, the next tile's first
 // record of that bucket; slots still held at the chunk's end are flushed.
-template <int EW, int LK>
-__global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortParams p, const uint64_t* __restrict__ S,
-                                                             int nbuckets, ModelDev model,
-                                                             const uint32_t* __restrict__ offsets,
-                                                             int nchunks, uint32_t* __restrict__ stats,
-                                                             uint32_t c0, uint32_t c1,
-                                                             const uint32_t* __restrict__ skip_if,
-                                                             const uint32_t* __restrict__ gate, int gate_wide) {
+template <int EW>
+__global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortParams p, int nbuckets,
+                                                                           const uint32_t* __restrict__ offsets,
+                                                                           int nchunks, uint32_t* __restrict__ stats,
+                                                                           uint32_t c0, uint32_t c1,
+                                                                           const uint32_t* __restrict__ skip_if) {
   if (skip_if && *skip_if) return;  // a reserved region overflowed: the exact path redoes level 1
-  // gate: a learned sort launches this kernel with both lookups; the one
-  // that does not suit the model's widest window (kWideWindow) returns
-  if (gate && (*gate > kWideWindow) != (gate_wide != 0)) return;
-  model = resolve_model(model);
   uint32_t* err = stats + STAT_SLOTS;  // the error word follows the statistics
   constexpr int RPT = ScatterTile<EW>::kRpt, T = ScatterTile<EW>::kSize;
   constexpr bool kPre = ScatterTile<EW>::kPrefetch;
@@ -575,8 +562,7 @@ __global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortP
   constexpr uint32_t E = EW * 4;
   constexpr uint32_t kNoSlot = 0xffffffffu;
   extern __shared__ __align__(16) uint8_t smem[];
-  LookupSmem L;
-  uint8_t* q = load_lookup<LK>(smem, S, nbuckets, model, L);
+  uint8_t* q = smem;
   uint32_t* cursor = reinterpret_cast<uint32_t*>(q);
   q += 4 * (size_t)((nbuckets + 3) & ~3);
   uint32_t* held_at = reinterpret_cast<uint32_t*>(q);  // destination of the held record, or kNoSlot
@@ -592,21 +578,18 @@ __global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortP
   if (!kCombine) q += 4 * (size_t)T;
   uint8_t* cnt = q;  // [nbuckets][kWarps]
   q += (size_t)nbuckets * kWarps;
-  // LOOKUP_IDS: the bucket ids of the next two tiles come into shared memory
-  // by bulk asynchronous copies (no registers held for them)
+  // the bucket ids of the next two tiles come into shared memory by bulk
+  // asynchronous copies (no registers held for them)
   uint16_t* idbuf = reinterpret_cast<uint16_t*>(q);  // [2][kIdBuf]
-  constexpr uint32_t kIdBuf = (T * 2 + 32 + 15) / 16 * 8;
-  uint64_t* ibar = reinterpret_cast<uint64_t*>(q + (LK == LOOKUP_IDS ? 4 * (size_t)kIdBuf : 0));
+  constexpr uint32_t kIdBuf = scatter_id_buf<EW>();
+  uint64_t* ibar = reinterpret_cast<uint64_t*>(q + 4 * (size_t)kIdBuf);
   for (int i = threadIdx.x; i < nbuckets * kWarps / 16; i += kThreads)
     reinterpret_cast<uint4*>(cnt)[i] = make_uint4(0, 0, 0, 0);
-  const uint32_t hprobes = p.heavy ? p.heavy->probes : 0;
   uint32_t ipar = 0;  // next completion parity of each id buffer
-  if constexpr (LK == LOOKUP_IDS) {
-    if (threadIdx.x == 0) {
-      mbar_init(&ibar[0], 1);
-      mbar_init(&ibar[1], 1);
-      mbar_init_fence();
-    }
+  if (threadIdx.x == 0) {
+    mbar_init(&ibar[0], 1);
+    mbar_init(&ibar[1], 1);
+    mbar_init_fence();
   }
   // ids of the tile starting at record t (chunk end ce) into buffer b
   auto issue_ids = [&](uint32_t t, uint32_t ce_, int b) {
@@ -626,12 +609,10 @@ __global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortP
   }
   __syncthreads();
 
-  if constexpr (LK == LOOKUP_IDS) {
-    if (threadIdx.x == 0) {  // (the barrier above ended every read of both buffers)
-      fence_proxy_async_smem();
-      if (cb < ce) issue_ids(cb, ce, 0);
-      if (cb + T < ce) issue_ids(cb + T, ce, 1);
-    }
+  if (threadIdx.x == 0) {  // (the barrier above ended every read of both buffers)
+    fence_proxy_async_smem();
+    if (cb < ce) issue_ids(cb, ce, 0);
+    if (cb + T < ce) issue_ids(cb + T, ce, 1);
   }
   // the next tile's records are loaded while the current tile is ranked
   uint32_t nxt[kPre ? RPT : 1][EW];
@@ -644,11 +625,8 @@ __global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortP
   }
   for (uint32_t t0 = cb, tk = 0; t0 < ce; t0 += T, ++tk) {
     const int ib = (int)(tk & 1);
-    bool id_ok = true;
-    if constexpr (LK == LOOKUP_IDS) {
-      id_ok = mbar_wait_bounded(&ibar[ib], (ipar >> ib) & 1u, kBulkWaitPolls);
-      ipar ^= 1u << ib;
-    }
+    const bool id_ok = mbar_wait_bounded(&ibar[ib], (ipar >> ib) & 1u, kBulkWaitPolls);
+    ipar ^= 1u << ib;
     const uint32_t nvalid = min((uint32_t)T, ce - t0);
     if (threadIdx.x == 0 && t0 + 2 * T < ce)
       prefetch_l2_range(p.in + (size_t)(t0 + 2 * T) * E, min((uint32_t)T, ce - t0 - 2 * T) * E);
@@ -658,9 +636,7 @@ __global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortP
     for (int r = 0; r < RPT; ++r) {
       const uint32_t et = w * 32 * RPT + r * 32 + lane;  // in the tile
       bkt[r] = kNoBucket;
-      if constexpr (LK == LOOKUP_IDS) {
-        if (et < nvalid) bkt[r] = min((uint32_t)idbuf[(size_t)ib * kIdBuf + et], (uint32_t)nbuckets - 1);
-      }
+      if (et < nvalid) bkt[r] = min((uint32_t)idbuf[(size_t)ib * kIdBuf + et], (uint32_t)nbuckets - 1);
       if constexpr (kPre) {
 #pragma unroll
         for (int q2 = 0; q2 < EW; ++q2) rec[r][q2] = nxt[r][q2];
@@ -671,34 +647,20 @@ __global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortP
         if (e < ce) RecIO<EW>::load_stream(p.in + (size_t)e * E, rec[r]);
       }
     }
-    if constexpr (LK != LOOKUP_IDS) {
-#pragma unroll
-      for (int r = 0; r < RPT; ++r) {
-        uint32_t e = w * 32 * RPT + r * 32 + lane;
-        if (e < nvalid) {
-          uint64_t k = key_from_regs<EW>(rec[r], p.key);
-          const uint32_t hb = hprobes ? heavy_bucket(p.heavy, hprobes, k) : kNoHeavy;
-          bkt[r] = hb != kNoHeavy ? hb : lookup<LK>(L, model, nbuckets, k, stats + STAT_WINDOW_MISS);
-        }
-      }
-    }
     // 1. ranks within the warp, in (r, lane) order (a wait for ids that ran
     // out leaves in-range ids behind: the CTA stops at the barrier)
     uint32_t lead[RPT];
     warp_ranks<RPT, kMaxBucketBits>(bkt, rank, lead, cnt);
     if (!__syncthreads_and(id_ok)) {
-      if constexpr (LK == LOOKUP_IDS) {
-        if (threadIdx.x == 0) set_error(err, DEV_ERR_TIMEOUT);
-        mbar_wait_bounded(&ibar[ib], ((ipar >> ib) & 1u) ^ 1u, kBulkWaitPolls);  // (the parity flipped above)
-        if (t0 + T < ce) mbar_wait_bounded(&ibar[ib ^ 1], (ipar >> (ib ^ 1)) & 1u, kBulkWaitPolls);
-      }
+      if (threadIdx.x == 0) set_error(err, DEV_ERR_TIMEOUT);
+      mbar_wait_bounded(&ibar[ib], ((ipar >> ib) & 1u) ^ 1u, kBulkWaitPolls);  // (the parity flipped above)
+      if (t0 + T < ce) mbar_wait_bounded(&ibar[ib ^ 1], (ipar >> (ib ^ 1)) & 1u, kBulkWaitPolls);
       return;
     }
-    if constexpr (LK == LOOKUP_IDS) {  // every thread has read this tile's ids: the buffer takes tile + 2
-      if (threadIdx.x == 0 && t0 + 2 * T < ce) {
-        fence_proxy_async_smem();
-        issue_ids(t0 + 2 * T, ce, ib);
-      }
+    // every thread has read this tile's ids: the buffer takes the tile after next
+    if (threadIdx.x == 0 && t0 + 2 * T < ce) {
+      fence_proxy_async_smem();
+      issue_ids(t0 + 2 * T, ce, ib);
     }
     // 2. rank in the tile = counts of the earlier warps + rank in the warp
     uint32_t tot[RPT], hold[RPT];
@@ -769,13 +731,13 @@ __global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortP
   }
 }
 
-template <int EW, int LK>
-size_t l1_scatter_smem(int nbuckets, const ModelDev* m) {
+template <int EW>
+size_t l1_scatter_smem(int nbuckets) {
   const size_t words = 4 * (size_t)((nbuckets + 3) & ~3);
   const size_t combine = EW == 4 ? words + 16 * (size_t)nbuckets : 0;
   const size_t stage = EW == 4 ? 0 : (size_t)ScatterTile<EW>::kSize * (EW * 4 + 4);
-  const size_t ids = LK == LOOKUP_IDS ? 4 * (size_t)((ScatterTile<EW>::kSize * 2 + 32 + 15) / 16 * 8) + 16 : 0;
-  return lookup_smem_bytes<LK>(nbuckets, m) + words + combine + stage + (size_t)nbuckets * kWarps + ids;
+  const size_t ids = 4 * (size_t)scatter_id_buf<EW>() + 16;  // two id buffers and their mbarriers
+  return words + combine + stage + (size_t)nbuckets * kWarps + ids;
 }
 
 // ------------------------------------------------------------- tasks -----
@@ -2678,12 +2640,11 @@ cudaError_t l1_scatter(const HsortParams& p, int nbuckets, const uint32_t* offse
   cudaError_t e = cudaSuccess;
   bool ok = dispatch_ew(p.elsize, [&](auto ewc) {
     constexpr int EW = decltype(ewc)::value;
-    const ModelDev m{};
-    size_t sm = l1_scatter_smem<EW, LOOKUP_IDS>(nbuckets, &m);
-    e = set_smem((const void*)k_l1_scatter<EW, LOOKUP_IDS>, sm);
+    size_t sm = l1_scatter_smem<EW>(nbuckets);
+    e = set_smem((const void*)k_l1_scatter<EW>, sm);
     if (e == cudaSuccess)
-      k_l1_scatter<EW, LOOKUP_IDS><<<ctas, kThreads, sm, stream>>>(p, nullptr, nbuckets, m, offsets, g, stats,
-                                                                    (uint32_t)c0, (uint32_t)c1, skip_if, nullptr, 0);
+      k_l1_scatter<EW><<<ctas, kThreads, sm, stream>>>(p, nbuckets, offsets, g, stats, (uint32_t)c0, (uint32_t)c1,
+                                                        skip_if);
     note_launches(1);
   });
   if (!ok) return cudaErrorInvalidValue;

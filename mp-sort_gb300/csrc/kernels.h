@@ -112,8 +112,7 @@ enum StatSlot : int {
   STAT_SLOTS = 8
 };
 
-// LOOKUP_IDS: the level-1 scatter reads the bucket ids the count wrote (HsortParams::bkt).
-enum Lookup : int { LOOKUP_PLAIN = 0, LOOKUP_LEARNED = 1, LOOKUP_IDS = 2 };
+enum Lookup : int { LOOKUP_PLAIN = 0, LOOKUP_LEARNED = 1 };
 
 struct SortTask {        // one bucket or sub-bucket of the level-2 task engine
   uint32_t start;        // first record in the destination buffers (the other scratch buffer, the output)
