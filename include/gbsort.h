@@ -82,6 +82,7 @@ typedef struct gbsort_stats {
                                     without a histogram pass (smooth keys) */
     uint32_t uniform_fallbacks;  /* such attempts in which a group outgrew its region: the bucket was
                                     then split by its histogram (same result) */
+    uint32_t deep_splits;        /* records of 8-16 bytes: splits in the third split round or later */
 } gbsort_stats;
 
 /* OR into `method`: hash the records (gbsort_multiset_hash_device) before

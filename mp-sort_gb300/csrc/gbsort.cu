@@ -939,6 +939,7 @@ int hsort_collect(Context& c) {
   g_stats.engine = c.run_engine ? 1u : 0u;
   g_stats.uniform_splits = h[CNT_UNIFORM] - h[CNT_UNIFORM + 1];
   g_stats.uniform_fallbacks = h[CNT_UNIFORM + 1];
+  g_stats.deep_splits = h[STAT_DEEP];
   if (c.run_timing)
     for (int i = 0; i < 6; ++i) {
       float ms = 0.f;
@@ -1415,6 +1416,7 @@ int segments_collect(Context& c, const uint32_t* h_errs, uint32_t nerrs) {
   g_stats.engine = c.run_engine ? 1u : 0u;
   g_stats.uniform_splits = h[CNT_UNIFORM] - h[CNT_UNIFORM + 1];
   g_stats.uniform_fallbacks = h[CNT_UNIFORM + 1];
+  g_stats.deep_splits = h[STAT_DEEP];
   return GBSORT_OK;
 }
 

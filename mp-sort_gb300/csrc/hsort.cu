@@ -1731,6 +1731,7 @@ __device__ bool split_task(SM& sm, const HsortParams& p, const SortTask& task, c
   uint32_t dpos = task.start;
   uint32_t dflags = in_b ? 0u : (uint32_t)TASK_SRC_B;  // where the emitted tasks' records lie
   const bool areas = STAGED && p.areas != 0;
+  if (areas && threadIdx.x == 0 && !(task.flags & TASK_L1) && !in_b) atomicAdd(stats + STAT_DEEP, 1u);
   if (areas) {
     if (task.flags & TASK_L1) {
       dbuf = p.bufB;

@@ -109,7 +109,8 @@ enum StatSlot : int {
   STAT_WINDOW_MISS = 5,  // learned lookups whose window missed (full search ran)
   STAT_MAX_BUCKET = 6,   // largest level-1 bucket
   STAT_REFINED = 7,      // splits whose crowded bins were cut finer
-  STAT_SLOTS = 8
+  STAT_DEEP = 8,         // splits of a third round or later (with areas: A to the output and back)
+  STAT_SLOTS = 9
 };
 
 enum Lookup : int { LOOKUP_PLAIN = 0, LOOKUP_LEARNED = 1 };

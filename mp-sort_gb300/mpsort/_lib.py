@@ -42,7 +42,8 @@ class Stats(ctypes.Structure):
                 ("splitter_fallback", ctypes.c_uint32), ("heavy_keys", ctypes.c_uint32),
                 ("refined_splits", ctypes.c_uint32), ("pipelined", ctypes.c_uint32),
                 ("region_overflow", ctypes.c_uint32), ("engine", ctypes.c_uint32),
-                ("uniform_splits", ctypes.c_uint32), ("uniform_fallbacks", ctypes.c_uint32)]
+                ("uniform_splits", ctypes.c_uint32), ("uniform_fallbacks", ctypes.c_uint32),
+                ("deep_splits", ctypes.c_uint32)]
 
     STAGES = ("splitters", "count", "scan", "scatter", "split", "local")
 

@@ -812,6 +812,35 @@ def test_uniform_bucket_splits(mp, kind, method):
         assert st["uniform_fallbacks"] > 0, st
 
 
+@pytest.mark.parametrize("method", ["plain", "learned"])
+def test_deep_split_rounds(mp, method):
+    """A run of 5000 consecutive keys with one outlier at every power of two
+    above it, in a uniform background: each split round narrows the run's
+    key range only down to the next outlier, so the run stays one crowded
+    group for several rounds.  With 16-byte records the third and later
+    rounds go from scratch A to the output and back (the level-1 areas of
+    scratch B hold their groups until the local sorts), and local sorts read
+    their input from the output itself (deep_splits counts those rounds'
+    splits).  Same stable order as the oracle's."""
+    rng = numpy.random.default_rng(67)
+    dt = numpy.dtype([('key', 'u8'), ('val', 'i8')])
+    n = 20_000_000
+    a = numpy.empty(n, dtype=dt)
+    a['key'] = rng.integers(0, 2**64, n, dtype=numpy.uint64, endpoint=False)
+    x = numpy.uint64(2**63 + 12345)
+    run = x + numpy.arange(5000, dtype=numpy.uint64)
+    outliers = x + (numpy.uint64(1) << numpy.arange(13, 59, dtype=numpy.uint64))
+    special = numpy.concatenate([run, run[:1000], outliers])  # (with equal keys)
+    pos = rng.choice(n, size=len(special), replace=False)
+    a['key'][pos] = special
+    a['val'] = numpy.arange(n)
+    out = numpy.empty_like(a)
+    mp.sort(a, 'key', out=out, method=method)
+    st = mp.last_stats()
+    assert out.tobytes() == O.numpy_sorted(a, 'key').tobytes()
+    assert st["deep_splits"] > 0, st
+
+
 # ----------------------------------------------- bounded look-back wait --
 def test_lookback_wait_runs_out_and_reports(mp):
     """One LSD pass in which a tile never publishes its counts: the next
