@@ -656,9 +656,13 @@ int hsort_enqueue(Context& c, const void* d_in, void* d_out, uint32_t n, uint32_
   // areas: the split rounds of records of 8-16 bytes give each level-1
   // bucket an area of scratch B a quarter larger than the bucket (uniform
   // splits scatter into regions there); the persistent engine does not
-  const bool areas = elsize % 4 == 0 && elsize >= 8 && elsize <= 16 && n <= kSplitAreaMaxN &&
-                     (hp || !use_engine(elsize, knobs.level2, false));
+  bool areas = elsize % 4 == 0 && elsize >= 8 && elsize <= 16 && n <= kSplitAreaMaxN &&
+               (hp || !use_engine(elsize, knobs.level2, false));
   GB_CUDA(c.A.ensure((size_t)a_cap * elsize + kScratchSlack));
+  if (areas && c.B.ensure((size_t)split_area(n) * elsize + kScratchSlack) != cudaSuccess) {
+    cudaGetLastError();  // no room for the areas: the splits write at final positions
+    areas = false;
+  }
   GB_CUDA(c.B.ensure((size_t)(areas ? split_area(n) : n) * elsize + kScratchSlack));
   const uint32_t cap_split = (uint32_t)nb + n / 4096 + 4096;
   const uint32_t cap_local = 4u * (uint32_t)nb + n / 512 + 65536;
