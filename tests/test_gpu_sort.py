@@ -812,6 +812,38 @@ def test_uniform_bucket_splits(mp, kind, method):
         assert st["uniform_fallbacks"] > 0, st
 
 
+@pytest.mark.parametrize("layout", [
+    [('key', 'u8')],                                  # 8 bytes
+    [('key', 'i8'), ('v', 'u4')],                     # 12 bytes, signed key
+    [('v', 'u4'), ('key', 'u4'), ('w', 'u8')],        # 16 bytes, 4-byte key at offset 4
+])
+def test_uniform_splits_record_sizes_in_place(mp, layout):
+    """Uniform bucket splits and the split areas for the other record sizes
+    of the staged path (8 and 12 bytes) and a 4-byte key, sorted in place
+    (the output is the input buffer, which level 1 has consumed before any
+    split writes it)."""
+    import torch
+    from mpsort import device
+    rng = numpy.random.default_rng(71)
+    dt = numpy.dtype(layout)
+    n = 6_000_003
+    a = numpy.zeros(n, dtype=dt)
+    info = numpy.iinfo(dt['key'].base)
+    a['key'] = rng.integers(info.min, info.max, n, dtype=dt['key'].base, endpoint=True)
+    a['key'][7::3] = a['key'][0:(n - 7 + 2) // 3]  # equal keys
+    for f in dt.names:
+        if f != 'key':
+            a[f] = numpy.arange(n).astype(dt[f].base)
+    d = torch.from_numpy(a.view(numpy.uint8).copy()).cuda()
+    device.sort(d.data_ptr(), d.data_ptr(), n, dt, 'key', 'learned', torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    st = mp.last_stats()
+    got = d.cpu().numpy().view(dt)
+    assert got.tobytes() == O.numpy_sorted(a, 'key').tobytes()
+    if dt['key'].itemsize == 8:
+        assert st["uniform_splits"] > 0, st
+
+
 @pytest.mark.parametrize("method", ["plain", "learned"])
 def test_deep_split_rounds(mp, method):
     """A run of 5000 consecutive keys with one outlier at every power of two
