@@ -1337,10 +1337,27 @@ __device__ void local_sort_staged(LocalSmemP<NT>& sm, const uint8_t* rb, uint8_t
     if (e < m) sm.keyB[sm.cnt[bin[r]] + slot[r]] = pk[r];
   }
   __syncthreads();
-  for (uint32_t i = threadIdx.x; i < m; i += NT) {
-    const uint64_t v = sm.keyB[i];
-    const uint32_t d = (uint32_t)(v >> shift);
-    const uint32_t b0 = sm.cnt[d], b1 = sm.cnt[d + 1];
+  // each thread's PER positions in bin order, their loads batched so that
+  // the chains keyB -> bin bounds -> record of the PER positions overlap
+  uint64_t vv[PER];
+  uint32_t lo_[PER], hi_[PER];
+#pragma unroll
+  for (int r = 0; r < PER; ++r) {
+    const uint32_t i = r * NT + threadIdx.x;
+    vv[r] = i < m ? sm.keyB[i] : 0;
+  }
+#pragma unroll
+  for (int r = 0; r < PER; ++r) {
+    const uint32_t d = (uint32_t)(vv[r] >> shift);
+    lo_[r] = sm.cnt[d];
+    hi_[r] = sm.cnt[d + 1];
+  }
+#pragma unroll
+  for (int r = 0; r < PER; ++r) {
+    const uint32_t i = r * NT + threadIdx.x;
+    if (i >= m) continue;
+    const uint64_t v = vv[r];
+    const uint32_t b0 = lo_[r], b1 = hi_[r];
     if (b1 - b0 > (uint32_t)kInsertMax) {  // a crowded bin: further passes below
       if (i == b0) {
         const uint32_t q = atomicAdd(&sm.nbig, 1u);
@@ -1352,9 +1369,9 @@ __device__ void local_sort_staged(LocalSmemP<NT>& sm, const uint8_t* rb, uint8_t
     }
     uint32_t at = i;
     if (b1 - b0 > 1) {
-      uint32_t r = 0;
-      for (uint32_t j = b0; j < b1; ++j) r += sm.keyB[j] < v;
-      at = b0 + r;
+      uint32_t rk = 0;
+      for (uint32_t j = b0; j < b1; ++j) rk += sm.keyB[j] < v;
+      at = b0 + rk;
     }
     if (drop) sm.keyA[at] = v;
     else put(at, (uint32_t)(v & kIdx));
