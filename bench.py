@@ -70,21 +70,28 @@ def ncu_bytes_per_record(summary):
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle samples during the timed region."""
+    """nvidia-smi clock / throttle samples during the timed region.
+
+    The timed region begins only after nvidia-smi's first sample has arrived,
+    so that its start-up (NVML initialisation,
+    which competes with the sort's host thread for the driver) stays outside
+    the timed region; `window(t0, t1)` then keeps the samples taken inside it."""
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 100
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
-        self.lines = []
+        self.lines = []          # (arrival time, csv line)
+        self.bounds = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -94,7 +101,27 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.monotonic(), line.strip()))
+
+    def ready(self, timeout_s=15.0):
+        """Wait (bounded) for the first sample: nvidia-smi is up."""
+        t_end = time.monotonic() + timeout_s
+        while self.proc and not self.lines and time.monotonic() < t_end:
+            time.sleep(0.01)
+
+    def window(self, t0, t1):
+        self.bounds = (t0, t1)
+
+    def _in_window(self):
+        if self.bounds is None:
+            return [ln for _, ln in self.lines]
+        t0, t1 = self.bounds
+        inside = [ln for ts, ln in self.lines if t0 <= ts <= t1]
+        if inside:
+            return inside
+        # a region shorter than the period: the first sample after it
+        after = [ln for ts, ln in self.lines if ts > t1]
+        return after[:1]
 
     def __exit__(self, *a):
         if self.proc:
@@ -107,7 +134,7 @@ class ClockSampler:
     def summary(self):
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self._in_window():
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -172,10 +199,12 @@ def run_ours(args):
     parity = W.device_parity(torch, rec, out, n)
 
     stats_steps = []
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
     with ClockSampler(local) as clk:
+        clk.ready()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        t0 = time.monotonic()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -184,6 +213,8 @@ def run_ours(args):
             stats_steps.append(mpsort.last_stats())
         e1.record(stream)
         torch.cuda.synchronize()
+        clk.window(t0, time.monotonic())
+        time.sleep(2 * ClockSampler.PERIOD_MS / 1e3)
     ms = max_over_ranks(e0.elapsed_time(e1))
     if world > 1:
         torch.distributed.barrier()
