@@ -497,8 +497,15 @@ struct Tile {
 #ifndef GB_SCATTER_RPT
 #define GB_SCATTER_RPT 16
 #endif
+// Records of 20 bytes and more: each thread also holds the next tile's
+// records in registers (loaded while the current tile is ranked; 5e8 x 40 B
+// scatter 22.1 ms against 23.9 ms without).  Records of 8-16 bytes come
+// from L2 instead (each tile is prefetched two tiles ahead): with the
+// register copy the kernel spills at 64 registers, and 1e9 x 16 B scatters
+// in 17.38 ms against 17.19 ms without.  GB_SCATTER_PREFETCH=0 / 1 forces
+// either form.
 #ifndef GB_SCATTER_PREFETCH
-#define GB_SCATTER_PREFETCH 1
+#define GB_SCATTER_PREFETCH -1
 #endif
 #ifndef GB_SCATTER_CTAS
 #define GB_SCATTER_CTAS 2  // level-1 scatter CTAs per SM (the register budget follows)
@@ -512,7 +519,7 @@ struct ScatterTile {
                               : (GB_SCATTER_RPT / EW) < 1 ? 1
                               : ((GB_SCATTER_RPT / EW) > 7 ? 7 : (GB_SCATTER_RPT / EW));
   static constexpr int kSize = kThreads * kRpt;
-  static constexpr bool kPrefetch = GB_SCATTER_PREFETCH != 0;
+  static constexpr bool kPrefetch = GB_SCATTER_PREFETCH < 0 ? EW >= 5 : GB_SCATTER_PREFETCH != 0;
 };
 
 // u16 entries of one bucket-id buffer of the scatter: a tile's ids plus the
@@ -524,10 +531,33 @@ __host__ __device__ constexpr uint32_t scatter_id_buf() {
 
 // One 32-byte store (a whole DRAM sector, one memory request; two 16-byte
 // stores to scattered places cost a request each).  p is 32-byte aligned.
+// No memory clobber: the kernels that use it never read the sectors they
+// write, so the loads around it may move across it.
 __device__ __forceinline__ void store_sector(uint8_t* p, const uint4& a, const uint4& b) {
   asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "r"(a.x), "r"(a.y), "r"(a.z),
-               "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w)
-               : "memory");
+               "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w));
+}
+
+// Unrolled iterations of a staged split's write-out loop: four at 12 and 16
+// bytes a record (no spills), two at 8 (four would spill).
+template <int EW>
+__host__ __device__ constexpr int split_outs_unroll() {
+  return EW >= 3 ? 4 : 2;
+}
+
+// Global stores with no memory clobber, for write-outs whose destinations
+// the kernel never reads back: the shared-memory loads of the following
+// records may move above them (a store through a plain pointer, which might
+// address shared memory, keeps every later shared-memory load below it).
+__device__ __forceinline__ void st_global(uint4* p, const uint4& v) {
+  asm volatile("st.global.v4.b32 [%0], {%1, %2, %3, %4};" ::"l"(__cvta_generic_to_global(p)), "r"(v.x), "r"(v.y),
+               "r"(v.z), "r"(v.w));
+}
+__device__ __forceinline__ void st_global(uint2* p, const uint2& v) {
+  asm volatile("st.global.v2.b32 [%0], {%1, %2};" ::"l"(__cvta_generic_to_global(p)), "r"(v.x), "r"(v.y));
+}
+__device__ __forceinline__ void st_global(uint32_t* p, uint32_t v) {
+  asm volatile("st.global.b32 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "r"(v));
 }
 
 // Stable scatter of each chunk into its buckets.  Per tile of T records
@@ -663,38 +693,60 @@ __global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortP
       issue_ids(t0 + 2 * T, ce, ib);
     }
     // 2. rank in the tile = counts of the earlier warps + rank in the warp
-    uint32_t tot[RPT], hold[RPT];
+    uint32_t tot[RPT];
+    uint32_t holds = 0;  // bit r: row r starts a sector whose partner comes later
+    if constexpr (!kCombine) {  // each record to the staged tile, its destination beside it
 #pragma unroll
-    for (int r = 0; r < RPT; ++r) {
-      tot[r] = 0;
-      hold[r] = kNoSlot;
-      if (!kCombine) wdest[w * 32 * RPT + r * 32 + lane] = kNoSlot;
-      if (bkt[r] == kNoBucket) continue;
-      uint32_t all;
-      const uint32_t at = tile_rank(bkt[r], rank[r], cnt, all);
-      const uint32_t dest = cursor[bkt[r]] + at;
-      tot[r] = at + 1 == all ? all : 0;  // the run's last record advances the cursor
-      if (dest >= p.a_cap) {
-        set_error(err, DEV_ERR_COUNT_MISMATCH);
-        continue;
-      }
-      uint8_t* to = p.bufA + (size_t)dest * E;
-      if constexpr (!kCombine) {
+      for (int r = 0; r < RPT; ++r) {
+        tot[r] = 0;
         const uint32_t e = w * 32 * RPT + r * 32 + lane;
-        RecIO<EW>::store(stage + (size_t)e * E, rec[r]);
-        wdest[e] = dest;
-        continue;
-      } else {
-        if ((dest & 1u) == 0 && at + 1 == all) {  // starts a sector whose partner comes later
-          hold[r] = dest;
+        wdest[e] = kNoSlot;
+        if (bkt[r] == kNoBucket) continue;
+        uint32_t all;
+        const uint32_t at = tile_rank(bkt[r], rank[r], cnt, all);
+        const uint32_t dest = cursor[bkt[r]] + at;
+        tot[r] = at + 1 == all ? all : 0;  // the run's last record advances the cursor
+        if (dest >= p.a_cap) {
+          set_error(err, DEV_ERR_COUNT_MISMATCH);
           continue;
         }
-        if ((dest & 1u) && at == 0 && held_at[bkt[r]] == dest - 1) {  // completes a held sector
+        RecIO<EW>::store(stage + (size_t)e * E, rec[r]);
+        wdest[e] = dest;
+      }
+    } else {
+      // 16-byte records, stored from registers: every row's table reads
+      // come first (they are independent, so they are in flight together),
+      // then the stores; rank[] becomes the destination
+      uint32_t completes = 0;  // bit r: row r completes its bucket's held sector
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) {
+        tot[r] = 0;
+        if (bkt[r] == kNoBucket) continue;
+        uint32_t all;
+        const uint32_t at = tile_rank(bkt[r], rank[r], cnt, all);
+        rank[r] = cursor[bkt[r]] + at;
+        tot[r] = at + 1 == all ? all : 0;
+        if ((rank[r] & 1u) && at == 0 && held_at[bkt[r]] == rank[r] - 1) completes |= 1u << r;
+      }
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) {
+        if (bkt[r] == kNoBucket) continue;
+        const uint32_t dest = rank[r];
+        if (dest >= p.a_cap) {
+          set_error(err, DEV_ERR_COUNT_MISMATCH);
+          continue;
+        }
+        uint8_t* to = p.bufA + (size_t)dest * E;
+        if ((dest & 1u) == 0 && tot[r]) {
+          holds |= 1u << r;
+          continue;
+        }
+        if ((completes >> r) & 1u) {
           store_sector(to - 16, held[bkt[r]], make_uint4(rec[r][0], rec[r][1], rec[r][2], rec[r][3]));
           continue;
         }
+        RecIO<EW>::store(to, rec[r]);
       }
-      RecIO<EW>::store(to, rec[r]);
     }
     __syncthreads();
     if constexpr (!kCombine) {
@@ -713,9 +765,9 @@ __global__ void __launch_bounds__(kThreads, GB_SCATTER_CTAS) k_l1_scatter(HsortP
     for (int r = 0; r < RPT; ++r) {
       if (tot[r]) cursor[bkt[r]] += tot[r];
       if constexpr (kCombine) {
-        if (hold[r] != kNoSlot) {
+        if ((holds >> r) & 1u) {
           held[bkt[r]] = make_uint4(rec[r][0], rec[r][1], rec[r][2], rec[r][3]);
-          held_at[bkt[r]] = hold[r];
+          held_at[bkt[r]] = rank[r];
         } else if (bkt[r] != kNoBucket && tot[r]) {
           held_at[bkt[r]] = kNoSlot;  // the run ended on a completed sector
         }
@@ -950,6 +1002,59 @@ __device__ __forceinline__ void block_minmax(uint64_t& mn, uint64_t& mx, uint64_
   __syncthreads();
 }
 
+// Places the packed words at positions [a, a+s) of keyA in order when they
+// span fewer than 2^kLocalBits values from mn -- a run of equal keys, whose
+// words differ only in their input indices: each word sets its bit in a
+// bitmap of the span, and its rank is the number of set bits below it (the
+// words are distinct).  Four barriers and no bin counters to clear or scan,
+// where a counting pass over the span takes five and both.  sm.cnt holds
+// the bitmap and its prefix counts; the words go through keyB.
+template <int NT, typename SM>
+__device__ __forceinline__ void local_bitmap_place(SM& sm, uint32_t a, uint32_t s, uint64_t mn) {
+  constexpr int PER = kLocalMax / NT;
+  constexpr int kWords = (1 << kLocalBits) / 32;
+  static_assert(kWords == 64, "two bitmap words per lane of one warp");
+  uint32_t* bits = sm.cnt;
+  uint32_t* below = sm.cnt + kWords;  // set bits in the words before each word
+  for (int i = threadIdx.x; i < kWords; i += NT) bits[i] = 0;
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < PER; ++r) {
+    const uint32_t e = r * NT + threadIdx.x;
+    if (e < s) {
+      const uint32_t d = (uint32_t)(sm.keyA[a + e] - mn);
+      atomicOr(&bits[d >> 5], 1u << (d & 31));
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const uint32_t lane = threadIdx.x;
+    const uint32_t c0 = __popc(bits[2 * lane]), c1 = __popc(bits[2 * lane + 1]);
+    uint32_t inc = c0 + c1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(GB_FULL_MASK, inc, o);
+      if (lane >= (uint32_t)o) inc += t;
+    }
+    below[2 * lane] = inc - c0 - c1;
+    below[2 * lane + 1] = inc - c1;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < PER; ++r) {
+    const uint32_t e = r * NT + threadIdx.x;
+    if (e < s) {
+      const uint64_t kv = sm.keyA[a + e];
+      const uint32_t d = (uint32_t)(kv - mn), wd = d >> 5;
+      const uint32_t at = below[wd] + __popc(bits[wd] & ((1u << (d & 31)) - 1u));
+      sm.keyB[a + min(at, s - 1)] = kv;
+    }
+  }
+  __syncthreads();
+  for (uint32_t e = threadIdx.x; e < s; e += NT) sm.keyA[a + e] = sm.keyB[a + e];
+  __syncthreads();
+}
+
 // One counting pass over positions [a, a+s) of keyA / idxA, in place: every
 // element takes a slot in its bin, (key - mn) >> shift, by a shared-memory
 // atomic (the order inside a bin is arbitrary), lands in keyB / idxB at its
@@ -966,6 +1071,12 @@ __device__ __noinline__ void local_msd_pass(SM& sm, uint32_t a, uint32_t s, uint
   constexpr int kBins = 1 << kLocalBits;
   constexpr int PER = kLocalMax / NT;
   static_assert(kLocalMax <= kBins, "input indices must fit the bins");
+  if constexpr (PACKED) {
+    if (mx - mn < (uint64_t)kBins) {  // (block-wide bounds: every thread takes this branch)
+      local_bitmap_place<NT>(sm, a, s, mn);
+      return;
+    }
+  }
   const int bits = bitlen64(mx - mn);
   const int shift = bits > kLocalBits ? bits - kLocalBits : 0;
   for (int i = threadIdx.x; i < kBins; i += NT) sm.cnt[i] = 0;
@@ -1304,7 +1415,7 @@ __device__ void local_sort_staged(LocalSmemP<NT>& sm, const uint8_t* rb, uint8_t
   auto put = [&](uint32_t at, uint32_t from) {  // record `from` of rb to output position `at`
 #pragma unroll
     for (uint32_t q = 0; q < VPR; ++q)
-      reinterpret_cast<V*>(dst + (size_t)at * E)[q] = reinterpret_cast<const V*>(rb + (size_t)from * E)[q];
+      st_global(reinterpret_cast<V*>(dst + (size_t)at * E) + q, reinterpret_cast<const V*>(rb + (size_t)from * E)[q]);
   };
   const uint64_t range = hi - lo;
   const int rbits = bitlen64(range);
@@ -1692,15 +1803,20 @@ __device__ int split_uniform(SM& sm, const HsortParams& p, const SortTask& task,
       sm.sgrp[slot] = (uint16_t)grp[r];
     }
     __syncthreads();
-    for (uint32_t f = threadIdx.x; f < nvalid * VPR; f += kThreads) {
+    bool over = false;
+#pragma unroll (split_outs_unroll<EW>())
+    for (uint32_t k = 0; k < (SplitTiles<EW>::T * VPR + kThreads - 1) / kThreads; ++k) {
+      const uint32_t f = threadIdx.x + k * kThreads;
+      if (f >= nvalid * VPR) break;
       const uint32_t j = f / VPR, qw = f % VPR;
       const uint32_t g = sm.sgrp[j] & (kMaxGroups - 1);
       const uint32_t from = min((uint32_t)sm.perm[j], nvalid - 1);
       const uint32_t dest = sm.cursor[g] + (j - sm.goff[g]);
       if (g < G && dest < (g + 1) * cap)
-        reinterpret_cast<V*>(oth + (size_t)dest * E)[qw] = reinterpret_cast<const V*>(rb + (size_t)from * E)[qw];
-      else sm.uflag = 2;  // the group outgrew its region: the attempt is void
+        st_global(reinterpret_cast<V*>(oth + (size_t)dest * E) + qw, reinterpret_cast<const V*>(rb + (size_t)from * E)[qw]);
+      else over = true;
     }
+    if (over) sm.uflag = 2;  // a group outgrew its region: the attempt is void
     __syncthreads();
     tiles.release(i);
     if (g_me < G) sm.cursor[g_me] += gtot;
@@ -1989,15 +2105,20 @@ __device__ bool split_task(SM& sm, const HsortParams& p, const SortTask& task, c
         sm.sgrp[slot] = (uint16_t)grp[r];
       }
       __syncthreads();
-      for (uint32_t f = threadIdx.x; f < nvalid * VPR; f += kThreads) {
+      bool bad = false;
+#pragma unroll (split_outs_unroll<EW>())
+      for (uint32_t k = 0; k < (SplitTiles<EW>::T * VPR + kThreads - 1) / kThreads; ++k) {
+        const uint32_t f = threadIdx.x + k * kThreads;
+        if (f >= nvalid * VPR) break;
         const uint32_t j = f / VPR, qw = f % VPR;
         const uint32_t g = sm.sgrp[j] & (kMaxGroups - 1);
         const uint32_t from = min((uint32_t)sm.perm[j], nvalid - 1);
         const uint32_t dest = sm.cursor[g] + (j - sm.goff[g]);
         if (dest < m)
-          reinterpret_cast<V*>(oth + (size_t)dest * E)[qw] = reinterpret_cast<const V*>(rb + (size_t)from * E)[qw];
-        else set_error(err, DEV_ERR_COUNT_MISMATCH);
+          st_global(reinterpret_cast<V*>(oth + (size_t)dest * E) + qw, reinterpret_cast<const V*>(rb + (size_t)from * E)[qw]);
+        else bad = true;
       }
+      if (bad) set_error(err, DEV_ERR_COUNT_MISMATCH);
       __syncthreads();
       tiles.release(i);
       sm.cursor[g_me] += gtot;
@@ -2052,14 +2173,19 @@ __device__ bool split_task(SM& sm, const HsortParams& p, const SortTask& task, c
       using V = typename std::conditional<E % 16 == 0, uint4,
                                           typename std::conditional<E % 8 == 0, uint2, uint32_t>::type>::type;
       constexpr uint32_t VPR = E / sizeof(V);
-      for (uint32_t f = threadIdx.x; f < nvalid * VPR; f += kThreads) {
+      bool bad = false;
+#pragma unroll 1
+      for (uint32_t k = 0; k < (T * VPR + kThreads - 1) / kThreads; ++k) {
+        const uint32_t f = threadIdx.x + k * kThreads;
+        if (f >= nvalid * VPR) break;
         const uint32_t i = f / VPR, qw = f % VPR;
         const uint32_t g = sm.sgrp[i];
         const uint32_t dest = sm.cursor[g] + (i - sm.goff[g]);
         if (dest < m)
-          reinterpret_cast<V*>(oth + (size_t)dest * E)[qw] = reinterpret_cast<const V*>(sm.stage + (size_t)i * E)[qw];
-        else set_error(err, DEV_ERR_COUNT_MISMATCH);
+          st_global(reinterpret_cast<V*>(oth + (size_t)dest * E) + qw, reinterpret_cast<const V*>(sm.stage + (size_t)i * E)[qw]);
+        else bad = true;
       }
+      if (bad) set_error(err, DEV_ERR_COUNT_MISMATCH);
     }
     __syncthreads();
     sm.cursor[g_me] += gtot;

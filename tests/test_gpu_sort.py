@@ -844,6 +844,34 @@ def test_uniform_splits_record_sizes_in_place(mp, layout):
         assert st["uniform_splits"] > 0, st
 
 
+@pytest.mark.parametrize("layout", [
+    [('key', '<u8'), ('val', '<i8')],
+    [('key', '<i8'), ('val', '<u4')],
+    [('key', '<u4'), ('val', '<u4')],
+])
+def test_local_runs_of_equal_keys(mp, layout):
+    """20,000 distinct keys of about 150 copies each (plus a uniform rest):
+    the local sorts of the staged path (8, 12 and 16-byte records) meet
+    runs of equal keys longer than an insertion bin, whose packed words
+    differ only in their input indices; such a bin is put in order by a
+    bitmap of its indices instead of a counting pass.  Same stable order as
+    the oracle's, and the statistics count the crowded bins."""
+    rng = numpy.random.default_rng(73)
+    dt = numpy.dtype(layout)
+    n = 3_000_001
+    a = numpy.zeros(n, dtype=dt)
+    info = numpy.iinfo(dt['key'].base)
+    vals = rng.integers(info.min, info.max, 20_000, dtype=dt['key'].base, endpoint=True)
+    a['key'] = rng.integers(info.min, info.max, n, dtype=dt['key'].base, endpoint=True)
+    pick = rng.random(n) < 0.97
+    a['key'][pick] = vals[rng.integers(0, len(vals), int(pick.sum()))]
+    a['val'] = numpy.arange(n).astype(dt['val'].base)
+    for method in ("plain", "learned"):
+        check(mp, a, 'key', method)
+        st = mp.last_stats()
+        assert st["bigbin_passes"] > 0, st
+
+
 @pytest.mark.parametrize("method", ["plain", "learned"])
 def test_deep_split_rounds(mp, method):
     """A run of 5000 consecutive keys with one outlier at every power of two
