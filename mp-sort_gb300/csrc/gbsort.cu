@@ -595,30 +595,11 @@ bool use_engine(uint32_t elsize, int level2, bool segments) {
   return segments;
 }
 
-// Level 2 from the initial tasks in split[0] (count in nsplit[0]) and the
-// local list: one persistent engine launch, or the split rounds and then one
-// pass over every local task.
-int run_level2(const HsortParams& p, const Level2& l2, uint32_t* stats, uint32_t* err, cudaStream_t st) {
-  if (use_engine(p.elsize, 0, true)) {
-    GB_CUDA(run_engine(p, l2.round(0), l2.qtask, l2.qready, l2.qctl, l2.qcap, stats, err, st));
-    return GBSORT_OK;
-  }
-  for (int r = 0; r < kSplitRounds; ++r) {
-    TaskListsHost L = l2.round(r);
-    GB_CUDA(cudaMemsetAsync(L.nsplit_out, 0, sizeof(uint32_t), st));
-    GB_CUDA(run_split_round(p, L, l2.work, stats, err, st));
-  }
-  GB_CUDA(run_local(p, l2.local, l2.nlocal, l2.cap_local, l2.work, stats, st));
-  return GBSORT_OK;
-}
-
 uint32_t hsort_sample_size(uint32_t n, int nb, const Knobs& knobs) {
   const uint64_t spb = knobs.sample_per_bucket ? (uint64_t)knobs.sample_per_bucket : 128;
   return nb > 1 ? (uint32_t)std::min<uint64_t>(n, std::max<uint64_t>(4096, (uint64_t)nb * spb)) : 0;
 }
 
-// Bytes of the small device buffer a histogram sort of n records uses
-// (G: count chunks).
 // Leaves of the learned CDF model of the histogram sort: 2^12.  Finer
 // leaves narrow the lookup windows of clustered keys (5e8 x 40 B Morton
 // keys: count 3.62 ms with 2^11 leaves, 3.40 ms with 2^12); uniform and
@@ -626,6 +607,8 @@ uint32_t hsort_sample_size(uint32_t n, int nb, const Knobs& knobs) {
 // per leaf in shared memory.
 constexpr int kModelLeafBits = 12;
 
+// Bytes of the small device buffer a histogram sort of n records uses
+// (G: count chunks).
 size_t hsort_small_bytes(uint32_t n, uint32_t elsize, const Knobs& knobs, int G) {
   const int nb = choose_buckets(n, elsize, knobs);
   const uint32_t s = hsort_sample_size(n, nb, knobs);

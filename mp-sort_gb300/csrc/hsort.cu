@@ -1584,26 +1584,8 @@ __device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-struct EngineSink {
+struct EngineSink {  // the persistent engine's queue: a split publishes its groups by engine_emit
   const EngineQueue& q;
-  __device__ void push(const SortTask& t, uint32_t* err) const {
-    atomicAdd(q.pending, 1u);  // pending first: it never undercounts
-    const uint32_t at = atomicAdd(q.tail, 1u);
-    if (at >= q.cap) {
-      set_error(err, DEV_ERR_TASK_OVERFLOW);
-      atomicSub(q.pending, 1u);
-      return;
-    }
-    q.task[at] = t;
-    __threadfence();
-    st_release_u32(&q.ready[at], 1u);
-  }
-  __device__ void copy(uint32_t start, uint32_t cnt, uint64_t lo, uint64_t hi, uint32_t src_b, uint32_t* err) const {
-    for (uint32_t s0 = 0; s0 < cnt; s0 += kCopyPiece)
-      push(make_task(start + s0, min(kCopyPiece, cnt - s0), lo, hi, src_b != 0, true), err);
-  }
-  __device__ void local(const SortTask& t, uint32_t* err) const { push(t, err); }
-  __device__ void split(const SortTask& t, uint32_t* err) const { push(t, err); }
 };
 
 constexpr uint32_t kEngineWaitPolls = 1u << 24;
