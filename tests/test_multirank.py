@@ -52,3 +52,28 @@ def test_reference_arm_prints_on_rank0_only(rank, tmp_path):
         assert line["e2e"]["h2d_bytes_per_step"] == 0
     else:
         assert lines == []
+
+
+def test_clock_sampler_keeps_the_timed_region():
+    """The clock record of a bench line: only the nvidia-smi samples that
+    arrived inside the timed region count (the sampler starts before it),
+    throttle reasons are read from those, and a region shorter than the
+    sampling period takes the first sample after it."""
+    sys.path.insert(0, REPO)
+    import bench
+    c = bench.ClockSampler(0)
+    row = "0, {mhz}, 2070, 900.00, 0x0, Not Active, Not Active, Not Active, {cap}"
+    c.lines = [(1.00, row.format(mhz=1200, cap="Not Active")),   # before: start-up
+               (1.10, row.format(mhz=2070, cap="Not Active")),
+               (1.20, row.format(mhz=2060, cap="Active")),
+               (1.30, row.format(mhz=2070, cap="Not Active")),
+               (1.45, row.format(mhz=900, cap="Not Active"))]    # after: idle
+    c.window(1.05, 1.35)
+    s = c.summary()
+    assert s["samples"] == 3 and s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["sw_power_cap"]
+    c.window(1.31, 1.40)  # no sample inside: the first one after
+    s = c.summary()
+    assert s["samples"] == 1 and s["sm_mhz"] == 900.0 and s["reasons"] == []
+    c.window(2.0, 2.1)  # nothing inside or after
+    assert c.summary()["samples"] == 0
