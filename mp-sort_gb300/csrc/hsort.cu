@@ -1012,9 +1012,10 @@ __device__ __forceinline__ void block_minmax(uint64_t& mn, uint64_t& mx, uint64_
 // span fewer than 2^kLocalBits values from mn -- a run of equal keys, whose
 // words differ only in their input indices: each word sets its bit in a
 // bitmap of the span, and its rank is the number of set bits below it (the
-// words are distinct).  Four barriers and no bin counters to clear or scan,
-// where a counting pass over the span takes five and both.  sm.cnt holds
-// the bitmap and its prefix counts; the words go through keyB.
+// words are distinct).  As many barriers as a counting pass over the span,
+// but 64 bitmap words to clear and prefix-count where the pass clears and
+// scans 2048 bin counters.  sm.cnt holds the bitmap and its prefix counts;
+// the words go through keyB.
 template <int NT, typename SM>
 __device__ __forceinline__ void local_bitmap_place(SM& sm, uint32_t a, uint32_t s, uint64_t mn) {
   constexpr int PER = kLocalMax / NT;
